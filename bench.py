@@ -1,0 +1,369 @@
+#!/usr/bin/env python
+"""Benchmark of the GSEA permutation pipeline on GB300.
+
+Metric: enrichment scores per second (gene sets x permutations) on the
+20,000 genes x 200 samples x 1,000 gene sets x 1,000 permutations workload
+(twopass_signal2noise, fp32), synthetic seeded data.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = one pass of the pipeline (permutation -> metric -> sort -> ES ->
+statistics) over the whole workload.
+
+* value          K*P / device time of one step, inputs resident in HBM, CUDA
+                 events on the launching stream, L2 flushed (256 MB write)
+                 between steps, outside the timed events.
+* e2e            the same metric through the C ABI from pinned host buffers:
+                 gsea_plan_run_host copies the inputs in, runs the pipeline
+                 and copies ES + statistics out, every step.
+* roofline       the dominant stage's algorithmic bytes per launch / its
+                 average device time, against MEASURED_PEAKS.json.
+* cpu_baseline   the reference's CPU path (its own build where it runs on
+                 this machine, else the oracle port of it) on a bounded sample
+                 of permutations, all host cores.
+Under torchrun (N > 1) every rank runs the same workload on its own GPU over a
+distinct permutation range (weak scaling, no collective on the data path); the
+time is the maximum over ranks and the value the sum of all ranks' scores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC_NAME = "enrichment scores/sec (sets x perms)"
+UNIT = "ES/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--metric", default="twopass_signal2noise")
+    ap.add_argument("--precision", type=int, default=32)
+    ap.add_argument("--form", choices=["plain", "chosen"], default="plain")
+    ap.add_argument("--workload", choices=["full", "small"], default="full")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU-baseline sample time")
+    return ap.parse_args()
+
+
+def workload(name):
+    from cudagsea_gb300 import synthetic
+    return synthetic.full() if name == "full" else synthetic.small()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_record():
+    path = os.path.join(ROOT, "profiles", "ncu_traffic_full_20000x200.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def stage_bytes(d, P, esize, ranks16):
+    """Algorithmic (compulsory) bytes of each stage for P permutations."""
+    G, S, K = d.num_genes, d.num_samples, d.num_sets
+    nnz = int(d.set_offsets[-1])
+    rb = 2 if ranks16 else 4
+    words = (S + 31) // 32
+    return {
+        "permute": S + 4 * words * P,
+        "metric": esize * G * S + 4 * words * P + esize * G * P,
+        "sort": esize * G * P + (rb + esize) * G * P,
+        "es": (rb + esize) * G * P + 8 * (K + 1) + 4 * nnz + esize * K * P,
+        "stats": 4 * esize * K * P,
+    }
+
+
+def cpu_sample(d, metric_id, double, target_s, use_ref):
+    """Time the CPU path on a sample of the permutations; returns (ES/s, sample P, seconds, kind)."""
+    import numpy as np
+    import oracle
+    kind = "reference" if use_ref else "port"
+    P = 4
+    while True:
+        t0 = time.perf_counter()
+        if use_ref:
+            oracle.ref_gsea(metric_id, d.exprs, d.labels, d.set_offsets, d.set_genes, P, double=double)
+        else:
+            oracle.gsea(metric_id, d.exprs, d.labels, d.set_offsets, d.set_genes, P, double=double)
+        dt = time.perf_counter() - t0
+        if dt >= 0.3 * target_s or P >= 512:
+            return d.num_sets * P / dt, P, dt, kind
+        P = min(512, max(P * 2, int(P * target_s / max(dt, 1e-3))))
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import oracle
+    from cudagsea_gb300.api import METRICS
+    oracle.build()
+    d = workload(args.workload)
+    mid = METRICS.index(args.metric)
+    double = args.precision == 64
+    use_ref = oracle.ref_available()
+    ncores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(ncores))
+    # size one step's sample to about 2 s of CPU work
+    _, P, dt, kind = cpu_sample(d, mid, double, 2.0, use_ref)
+    for _ in range(args.warmup):
+        (oracle.ref_gsea if use_ref else oracle.gsea)(mid, d.exprs, d.labels, d.set_offsets, d.set_genes, P,
+                                                       double=double)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        (oracle.ref_gsea if use_ref else oracle.gsea)(mid, d.exprs, d.labels, d.set_offsets, d.set_genes, P,
+                                                       double=double)
+        times.append(time.perf_counter() - t0)
+    mean = sum(times) / len(times)
+    value = d.num_sets * P / mean
+    sample = f"{P} of {d.num_perms} permutations per step, all {d.num_sets} sets, {d.name}"
+    out = {
+        "impl": "reference", "metric": METRIC_NAME, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if double else "f32", "data": "synthetic",
+        "config": {"workload": d.name, "metric_string": args.metric, "precision": args.precision},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]),
+                         "kind": kind, "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    world, rank, local = dist_env()
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    from cudagsea_gb300 import api, build
+    from cudagsea_gb300 import _native as N
+    build.build()
+    torch.cuda.set_device(local)
+    d = workload(args.workload)
+    P, K = d.num_perms, d.num_sets
+    double = args.precision == 64
+    esize = 8 if double else 4
+    form = N.FORM_CHOSEN if args.form == "chosen" else N.FORM_PLAIN
+    plan = api.Plan(d.num_genes, d.num_samples, K, P, args.metric, precision=args.precision, form=form,
+                    perm_offset=rank * P, device=local)
+    plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+    plan.set_profiling(True)
+    stream = torch.cuda.Stream(device=local)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    for _ in range(args.warmup):
+        plan.execute(stream.cuda_stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    stage_sum = {s: 0.0 for s in N.STAGES}
+    launches = 0
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()  # evict L2 between timed steps (outside the events)
+            starts[i].record(stream)
+            plan.execute(stream.cuda_stream)
+            ends[i].record(stream)
+            st = plan.stage_times()
+            for k, v in st.items():
+                stage_sum[k] += v
+            launches += plan.last_launches()
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    mean_ms = sum(step_ms) / len(step_ms)
+    if world > 1:
+        t = torch.tensor([mean_ms], dtype=torch.float64, device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        mean_ms = float(t.item())
+    value = world * K * P / (mean_ms / 1e3)
+
+    # ---- end to end through the C ABI, pinned host buffers
+    hx = N.lib()
+    import ctypes
+
+    def pinned(nbytes):
+        p = ctypes.c_void_p()
+        N.check(hx.gsea_host_alloc(nbytes, ctypes.byref(p)))
+        return p
+
+    dt = np.float64 if double else np.float32
+    arrs = {"x": np.ascontiguousarray(d.exprs, dt), "l": d.labels, "o": d.set_offsets, "g": d.set_genes}
+    pins = {}
+    for k, a in arrs.items():
+        p = pinned(a.nbytes)
+        ctypes.memmove(p, a.ctypes.data, a.nbytes)
+        pins[k] = p
+    es_b = pinned(esize * K * P)
+    st_b = pinned(esize * 5 * K)
+    plan.set_profiling(False)
+
+    def e2e_step():
+        N.check(hx.gsea_plan_run_host(plan._h, pins["x"], pins["l"], pins["o"], pins["g"], es_b, st_b))
+
+    for _ in range(args.warmup):
+        e2e_step()
+    if world > 1:
+        torch.distributed.barrier()
+    e2e_t = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_mean = sum(e2e_t) / len(e2e_t)
+    if world > 1:
+        t = torch.tensor([e2e_mean], dtype=torch.float64, device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_mean = float(t.item())
+    e2e_value = world * K * P / e2e_mean
+    h2d = sum(a.nbytes for a in arrs.values())
+    d2h = esize * K * P + esize * 5 * K
+    for p in list(pins.values()) + [es_b, st_b]:
+        hx.gsea_host_free(p)
+
+    # ---- roofline of the dominant stage
+    stage_avg = {k: v / args.steps for k, v in stage_sum.items()}
+    dominant = max(stage_avg, key=stage_avg.get)
+    sb = stage_bytes(d, P, esize, plan.ranks16)
+    peak, peak_kind = peaks()
+    achieved = sb[dominant] / (stage_avg[dominant] / 1e3) / 1e9
+    tr = traffic_record().get(dominant)
+    roof = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": tr, "peak_source": peak_kind,
+            "algorithmic_bytes": sb[dominant], "avg_ms": stage_avg[dominant]}
+
+    out = None
+    if rank == 0:
+        cpu = None
+        if world == 1 and not args.no_cpu_baseline:
+            import oracle
+            oracle.build()
+            use_ref = oracle.ref_available()
+            os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+            v, Ps, secs, kind = cpu_sample(d, api.METRICS.index(args.metric), double, args.cpu_seconds, use_ref)
+            cpu = {"value": v, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": kind,
+                   "sample": f"{Ps} of {P} permutations, all {K} sets, {secs:.1f} s"}
+        out = {
+            "metric": METRIC_NAME, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if double else "f32", "data": "synthetic",
+            "config": {"workload": d.name, "metric_string": args.metric, "form": args.form,
+                       "precision": args.precision, "l2": "256 MB write between timed steps",
+                       "parallelism": f"perm-shard x{world}"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": roof,
+            "stages_ms": stage_avg,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": launches,
+        }
+        print(json.dumps(out), flush=True)
+    plan.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

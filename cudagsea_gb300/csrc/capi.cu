@@ -1,0 +1,646 @@
+// capi.cu -- the C ABI of libgsea103 (include/gsea103.h): plans, one-shot
+// runs, devices, errors and the .es dump.
+//
+// The pipeline orchestration replaces gsea_proxy<> (src/cudaGSEA_wrapper.cu:
+// 179-401).  Differences by design:
+//   * inputs stay resident on the device; permutations run in batches sized
+//     by a memory budget rather than by free RAM (batch_scheduler.cuh:24-33),
+//     and gene sets are not batched at all: every set of a permutation batch is
+//     scored by one kernel from the CSR membership lists;
+//   * the statistics run on the device;
+//   * errors are returned as status codes with a per-thread message instead of
+//     exit().
+#include <atomic>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/gsea103.h"
+#include "kernels.h"
+
+namespace gsea {
+static std::atomic<long long> g_launches{0};
+int64_t launches_take() { return g_launches.exchange(0); }
+void launches_add(int64_t n) { g_launches.fetch_add(n); }
+}  // namespace gsea
+
+namespace {
+
+thread_local std::string t_error;
+
+int fail(int status, const std::string& msg) {
+    t_error = msg;
+    return status;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    if (e == cudaErrorMemoryAllocation)
+        return fail(GSEA_ERR_OUT_OF_MEMORY, std::string(what) + ": " + cudaGetErrorString(e));
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+        return fail(GSEA_ERR_NO_DEVICE, std::string(what) + ": " + cudaGetErrorString(e));
+    return fail(GSEA_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define GSEA_CUDA(call, what)                        \
+    do {                                             \
+        cudaError_t e_ = (call);                     \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+// Host-side fault injection for the error paths: GSEA_FAULT=alloc|launch|d2h
+// makes the matching step of the next call fail with GSEA_ERR_INJECTED.  No
+// device fault is ever provoked.
+bool injected(const char* stage) {
+    const char* f = std::getenv("GSEA_FAULT");
+    return f && std::strcmp(f, stage) == 0;
+}
+
+const char* const kMetricNames[GSEA_NUM_METRICS] = {
+    "naive_diff_of_classes",   "naive_ratio_of_classes",      "naive_log2_ratio_of_classes",
+    "stable_diff_of_classes",  "stable_ratio_of_classes",     "stable_log2_ratio_of_classes",
+    "onepass_signal2noise",    "onepass_t_test",              "twopass_signal2noise",
+    "twopass_t_test",          "stable_signal2noise",         "stable_t_test",
+    "overkill_signal2noise",   "overkill_t_test"};
+
+constexpr size_t kBatchBudget = size_t(4) << 30;  // bytes of per-permutation buffers
+
+}  // namespace
+
+namespace gsea {
+void set_last_error(const char* msg) { t_error = msg ? msg : ""; }
+}  // namespace gsea
+
+struct gsea_plan_s {
+    gsea_config cfg;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    size_t tsize = 4;
+    int words = 0;
+    int64_t pb = 0;  // permutations per batch
+    bool ranks16 = true;
+    bool debug = false;
+    bool inputs_set = false;
+    int64_t nA = 0, nB = 0;
+    int64_t nnz = 0, nnz_cap = 0;
+    int64_t last_launches = 0;
+    // device buffers
+    void* exprs = nullptr;
+    uint8_t* labels = nullptr;
+    int64_t* set_off = nullptr;
+    int32_t* set_genes = nullptr;
+    uint32_t* masks = nullptr;
+    void* keys = nullptr;
+    void* ranks = nullptr;
+    void* sorted = nullptr;
+    uint32_t* order = nullptr;
+    void* sort_scratch = nullptr;
+    size_t sort_scratch_bytes = 0;
+    void* es = nullptr;
+    void* stats = nullptr;
+    void* stats_scratch = nullptr;
+    size_t stats_scratch_bytes = 0;
+    // stage timing (gsea_plan_set_profiling): events recorded at every stage
+    // boundary of the last execute, tagged with the stage they close
+    bool profile = false;
+    std::vector<cudaEvent_t> events;
+    std::vector<int> event_stage;
+    size_t events_used = 0;
+};
+
+namespace {
+
+int validate_config(const gsea_config* c) {
+    if (!c) return fail(GSEA_ERR_INVALID_ARGUMENT, "null config");
+    if (c->num_genes < 1 || c->num_genes > (int64_t)1 << 30)
+        return fail(GSEA_ERR_INVALID_ARGUMENT, "num_genes out of range");
+    if (c->num_samples < 2 || c->num_samples > 6400)
+        return fail(GSEA_ERR_INVALID_ARGUMENT, "num_samples must be in [2, 6400]");
+    if (c->num_sets < 1 || c->num_sets > (int64_t)1 << 30)
+        return fail(GSEA_ERR_INVALID_ARGUMENT, "num_sets must be >= 1");
+    if (c->num_perms < 1 || c->num_perms > (int64_t)1 << 31)
+        return fail(GSEA_ERR_INVALID_ARGUMENT, "num_perms must be >= 1");
+    if (c->metric < 0 || c->metric >= GSEA_NUM_METRICS)
+        return fail(GSEA_ERR_UNKNOWN_METRIC, "unknown metric id");
+    if (c->precision != 32 && c->precision != 64)
+        return fail(GSEA_ERR_INVALID_ARGUMENT, "precision must be 32 or 64");
+    if (c->form != GSEA_FORM_PLAIN && c->form != GSEA_FORM_CHOSEN)
+        return fail(GSEA_ERR_INVALID_ARGUMENT, "unknown form");
+    if (c->perm_offset < 0 || c->perm_batch < 0)
+        return fail(GSEA_ERR_INVALID_ARGUMENT, "negative perm_offset / perm_batch");
+    return GSEA_OK;
+}
+
+// record a stage-boundary event (no-op unless profiling)
+int mark(gsea_plan_s* p, int stage, cudaStream_t st) {
+    if (!p->profile) return GSEA_OK;
+    if (p->events_used == p->events.size()) {
+        cudaEvent_t e;
+        GSEA_CUDA(cudaEventCreate(&e), "cudaEventCreate");
+        p->events.push_back(e);
+        p->event_stage.push_back(0);
+    }
+    p->event_stage[p->events_used] = stage;
+    GSEA_CUDA(cudaEventRecord(p->events[p->events_used++], st), "cudaEventRecord");
+    return GSEA_OK;
+}
+
+void free_plan_buffers(gsea_plan_s* p) {
+    void* bufs[] = {p->exprs, p->labels, p->set_off, p->set_genes, p->masks, p->keys, p->ranks,
+                    p->sorted, p->order, p->sort_scratch, p->es, p->stats, p->stats_scratch};
+    for (void* b : bufs)
+        if (b) cudaFree(b);
+    p->exprs = p->labels = nullptr;
+    p->set_off = nullptr;
+    p->set_genes = nullptr;
+    p->masks = nullptr;
+    p->keys = p->ranks = p->sorted = nullptr;
+    p->order = nullptr;
+    p->sort_scratch = p->es = p->stats = p->stats_scratch = nullptr;
+}
+
+template <class Ptr>
+int dev_alloc(Ptr** ptr, size_t bytes, const char* what) {
+    if (injected("alloc")) return fail(GSEA_ERR_INJECTED, std::string("injected allocation failure: ") + what);
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return cuda_fail(e, what);
+    }
+    *ptr = static_cast<Ptr*>(p);
+    return GSEA_OK;
+}
+
+int use_device(const gsea_plan_s* p) {
+    GSEA_CUDA(cudaSetDevice(p->device), "cudaSetDevice");
+    return GSEA_OK;
+}
+
+int alloc_order(gsea_plan_s* p) {
+    if (p->order) return GSEA_OK;
+    return dev_alloc(&p->order, sizeof(uint32_t) * (size_t)p->pb * p->cfg.num_genes, "order buffer");
+}
+
+int upload_sets(gsea_plan_s* p, const int64_t* off, const int32_t* genes, cudaStream_t st, bool async) {
+    const int64_t K = p->cfg.num_sets;
+    if (!off || !genes) return fail(GSEA_ERR_INVALID_ARGUMENT, "null gene-set arrays");
+    if (off[0] != 0) return fail(GSEA_ERR_INVALID_INPUT, "set_offsets[0] must be 0");
+    for (int64_t k = 0; k < K; k++)
+        if (off[k + 1] < off[k]) return fail(GSEA_ERR_INVALID_INPUT, "set_offsets must be non-decreasing");
+    const int64_t nnz = off[K];
+    if (nnz > p->nnz_cap) {
+        if (p->set_genes) cudaFree(p->set_genes);
+        p->set_genes = nullptr;
+        int rc = dev_alloc(&p->set_genes, sizeof(int32_t) * (size_t)nnz, "set genes");
+        if (rc) return rc;
+        p->nnz_cap = nnz;
+    }
+    p->nnz = nnz;
+    if (async) {
+        GSEA_CUDA(cudaMemcpyAsync(p->set_off, off, sizeof(int64_t) * (K + 1), cudaMemcpyHostToDevice, st), "copy set offsets");
+        if (nnz) GSEA_CUDA(cudaMemcpyAsync(p->set_genes, genes, sizeof(int32_t) * nnz, cudaMemcpyHostToDevice, st), "copy set genes");
+    } else {
+        GSEA_CUDA(cudaMemcpy(p->set_off, off, sizeof(int64_t) * (K + 1), cudaMemcpyHostToDevice), "copy set offsets");
+        if (nnz) GSEA_CUDA(cudaMemcpy(p->set_genes, genes, sizeof(int32_t) * nnz, cudaMemcpyHostToDevice), "copy set genes");
+    }
+    return GSEA_OK;
+}
+
+int count_labels(gsea_plan_s* p, const uint8_t* labels) {
+    int64_t a = 0, b = 0;
+    for (int64_t s = 0; s < p->cfg.num_samples; s++) {
+        if (labels[s] == 0) a++;
+        else if (labels[s] == 1) b++;
+        else return fail(GSEA_ERR_INVALID_INPUT, "labels must be 0 or 1");
+    }
+    if (a == 0 || b == 0) return fail(GSEA_ERR_INVALID_INPUT, "both classes need at least one sample");
+    p->nA = a;
+    p->nB = b;
+    return GSEA_OK;
+}
+
+template <class T>
+int execute_t(gsea_plan_s* p, cudaStream_t st) {
+    const gsea_config& c = p->cfg;
+    const int G = (int)c.num_genes, S = (int)c.num_samples, K = (int)c.num_sets;
+    const int64_t P = c.num_perms;
+    if (injected("launch")) return fail(GSEA_ERR_INJECTED, "injected launch failure");
+    gsea::launches_take();
+    gsea::SortBuffers sb;
+    sb.ranks = p->ranks;
+    sb.ranks16 = p->ranks16;
+    sb.sorted_abs = p->sorted;
+    sb.order = p->debug ? p->order : nullptr;
+    sb.scratch = p->sort_scratch;
+    sb.scratch_bytes = p->sort_scratch_bytes;
+    p->events_used = 0;
+    int rc = mark(p, -1, st);
+    if (rc) return rc;
+    for (int64_t b0 = 0; b0 < P; b0 += p->pb) {
+        const int nb = (int)(P - b0 < p->pb ? P - b0 : p->pb);
+        GSEA_CUDA(gsea::launch_permute(p->labels, S, nb, c.perm_offset + b0, c.seed, p->masks, p->words, st),
+                  "permute kernel");
+        if ((rc = mark(p, 0, st))) return rc;
+        GSEA_CUDA(gsea::launch_metric<T>(c.metric, static_cast<const T*>(p->exprs), G, S, p->masks, p->words,
+                                         nb, p->nA, p->nB, static_cast<T*>(p->keys), st),
+                  "metric kernel");
+        if ((rc = mark(p, 1, st))) return rc;
+        GSEA_CUDA(gsea::launch_sort<T>(static_cast<const T*>(p->keys), G, nb, c.ascending != 0, sb, st),
+                  "sort kernel");
+        if ((rc = mark(p, 2, st))) return rc;
+        GSEA_CUDA(gsea::launch_es<T>(p->ranks, p->ranks16, static_cast<const T*>(p->sorted), G, nb, p->set_off,
+                                     p->set_genes, K, static_cast<T*>(p->es), P, b0, st),
+                  "enrichment kernel");
+        if ((rc = mark(p, 3, st))) return rc;
+    }
+    GSEA_CUDA(gsea::launch_stats<T>(static_cast<const T*>(p->es), K, P, static_cast<T*>(p->stats),
+                                    p->stats_scratch, st),
+              "statistics kernels");
+    if ((rc = mark(p, 4, st))) return rc;
+    p->last_launches = gsea::launches_take();
+    return GSEA_OK;
+}
+
+int write_dump(const char* prefix, const void* es, int64_t K, int64_t P, int precision, char* path_out,
+               size_t path_len) {
+    if (!prefix || !*prefix) return fail(GSEA_ERR_INVALID_ARGUMENT, "empty dump prefix");
+    std::string name = std::string(prefix) + "_" + std::to_string(K) + "_" + std::to_string(P) + "_" +
+                       std::to_string(precision) + ".es";
+    FILE* f = std::fopen(name.c_str(), "wb");
+    if (!f) return fail(GSEA_ERR_IO, "cannot open " + name);
+    const size_t bytes = (size_t)K * (size_t)P * (precision / 8);
+    const size_t wrote = std::fwrite(es, 1, bytes, f);
+    std::fclose(f);
+    if (wrote != bytes) return fail(GSEA_ERR_IO, "short write to " + name);
+    if (path_out && path_len) {
+        std::strncpy(path_out, name.c_str(), path_len - 1);
+        path_out[path_len - 1] = 0;
+    }
+    return GSEA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gsea_status_string(int s) {
+    switch (s) {
+        case GSEA_OK: return "success";
+        case GSEA_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case GSEA_ERR_UNKNOWN_METRIC: return "unknown metric";
+        case GSEA_ERR_CUDA: return "CUDA error";
+        case GSEA_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case GSEA_ERR_NO_DEVICE: return "no CUDA device";
+        case GSEA_ERR_IO: return "I/O error";
+        case GSEA_ERR_UNSUPPORTED: return "unsupported";
+        case GSEA_ERR_INJECTED: return "injected fault";
+        case GSEA_ERR_INVALID_INPUT: return "invalid input data";
+        default: return "unknown status";
+    }
+}
+
+const char* gsea_last_error(void) { return t_error.c_str(); }
+
+int gsea_metric_id(const char* m) {
+    if (!m) return -1;
+    for (int i = 0; i < GSEA_NUM_METRICS; i++)
+        if (std::strcmp(m, kMetricNames[i]) == 0) return i;
+    return -1;
+}
+
+const char* gsea_metric_name(int id) {
+    return (id >= 0 && id < GSEA_NUM_METRICS) ? kMetricNames[id] : nullptr;
+}
+
+void gsea_config_init(gsea_config* c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->metric = GSEA_ONEPASS_SIGNAL2NOISE;  // CLI default (src/cudaGSEA.cu:90-94)
+    c->precision = 32;
+    c->seed = 42;
+    c->device = -1;
+    c->form = GSEA_FORM_PLAIN;
+}
+
+int gsea_device_count(int* count) {
+    if (!count) return fail(GSEA_ERR_INVALID_ARGUMENT, "null count");
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *count = 0;
+        return cuda_fail(e, "cudaGetDeviceCount");
+    }
+    *count = n;
+    return GSEA_OK;
+}
+
+int gsea_device_string(int device, char* buf, size_t len) {
+    if (!buf || !len) return fail(GSEA_ERR_INVALID_ARGUMENT, "null buffer");
+    cudaDeviceProp prop;
+    GSEA_CUDA(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
+    const size_t gib = ((size_t)prop.totalGlobalMem + (1ull << 30) - 1) >> 30;
+    std::snprintf(buf, len, "device %d: %s with %zu GiB RAM", device, prop.name, gib);
+    return GSEA_OK;
+}
+
+int gsea_get_device(int* device) {
+    if (!device) return fail(GSEA_ERR_INVALID_ARGUMENT, "null device");
+    GSEA_CUDA(cudaGetDevice(device), "cudaGetDevice");
+    return GSEA_OK;
+}
+
+int gsea_set_device(int device, int* active) {
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) cudaGetLastError();  // fall back to the current device
+    int cur = 0;
+    GSEA_CUDA(cudaGetDevice(&cur), "cudaGetDevice");
+    if (active) *active = cur;
+    if (cur != device) return fail(GSEA_ERR_INVALID_ARGUMENT, "invalid device id, staying on device " + std::to_string(cur));
+    return GSEA_OK;
+}
+
+int gsea_host_alloc(size_t bytes, void** ptr) {
+    if (!ptr) return fail(GSEA_ERR_INVALID_ARGUMENT, "null pointer");
+    GSEA_CUDA(cudaMallocHost(ptr, bytes ? bytes : 16), "cudaMallocHost");
+    return GSEA_OK;
+}
+
+int gsea_host_free(void* ptr) {
+    if (ptr) GSEA_CUDA(cudaFreeHost(ptr), "cudaFreeHost");
+    return GSEA_OK;
+}
+
+int gsea_plan_create(const gsea_config* cfg, gsea_plan* out) {
+    if (!out) return fail(GSEA_ERR_INVALID_ARGUMENT, "null plan pointer");
+    *out = nullptr;
+    int rc = validate_config(cfg);
+    if (rc) return rc;
+    if (injected("alloc")) return fail(GSEA_ERR_INJECTED, "injected allocation failure: plan");
+    if (cfg->form == GSEA_FORM_CHOSEN)
+        return fail(GSEA_ERR_UNSUPPORTED, "the tensor-core form is not available in this build");
+    gsea_plan_s* p = new (std::nothrow) gsea_plan_s();
+    if (!p) return fail(GSEA_ERR_OUT_OF_MEMORY, "host allocation");
+    p->cfg = *cfg;
+    if (cfg->device >= 0) {
+        cudaError_t e = cudaSetDevice(cfg->device);
+        if (e != cudaSuccess) { delete p; return cuda_fail(e, "cudaSetDevice"); }
+    }
+    cudaError_t e = cudaGetDevice(&p->device);
+    if (e != cudaSuccess) { cudaGetLastError(); delete p; return cuda_fail(e, "cudaGetDevice"); }
+    const int64_t G = cfg->num_genes, S = cfg->num_samples, K = cfg->num_sets, P = cfg->num_perms;
+    p->tsize = cfg->precision == 64 ? 8 : 4;
+    p->words = (int)((S + 31) / 32);
+    p->ranks16 = G <= 65536;
+    const size_t per_perm = (size_t)G * (2 * p->tsize + (p->ranks16 ? 2 : 4)) + 4 * (size_t)p->words;
+    int64_t pb = cfg->perm_batch > 0 ? cfg->perm_batch : (int64_t)(kBatchBudget / per_perm);
+    if (pb < 1) pb = 1;
+    if (pb > P) pb = P;
+    p->pb = pb;
+    e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete p; return cuda_fail(e, "cudaStreamCreate"); }
+    const size_t T = p->tsize;
+    if ((rc = dev_alloc(&p->exprs, T * G * S, "expression table")) ||
+        (rc = dev_alloc(&p->labels, (size_t)S, "labels")) ||
+        (rc = dev_alloc(&p->set_off, sizeof(int64_t) * (K + 1), "set offsets")) ||
+        (rc = dev_alloc(&p->masks, 4 * (size_t)p->words * pb, "label masks")) ||
+        (rc = dev_alloc(&p->keys, T * (size_t)G * pb, "metric keys")) ||
+        (rc = dev_alloc(&p->ranks, (p->ranks16 ? 2 : 4) * (size_t)G * pb, "ranks")) ||
+        (rc = dev_alloc(&p->sorted, T * (size_t)G * pb, "sorted weights")) ||
+        (rc = dev_alloc(&p->es, T * (size_t)K * P, "enrichment scores")) ||
+        (rc = dev_alloc(&p->stats, T * 5 * (size_t)K, "statistics"))) {
+        free_plan_buffers(p);
+        cudaStreamDestroy(p->stream);
+        delete p;
+        return rc;
+    }
+    p->sort_scratch_bytes = cfg->precision == 64 ? gsea::sort_scratch_bytes<double>((int)G, (int)pb)
+                                                 : gsea::sort_scratch_bytes<float>((int)G, (int)pb);
+    p->stats_scratch_bytes = cfg->precision == 64 ? gsea::stats_scratch_bytes<double>((int)K, P)
+                                                  : gsea::stats_scratch_bytes<float>((int)K, P);
+    if ((p->sort_scratch_bytes && (rc = dev_alloc(&p->sort_scratch, p->sort_scratch_bytes, "sort scratch"))) ||
+        (rc = dev_alloc(&p->stats_scratch, p->stats_scratch_bytes, "statistics scratch"))) {
+        free_plan_buffers(p);
+        cudaStreamDestroy(p->stream);
+        delete p;
+        return rc;
+    }
+    *out = p;
+    return GSEA_OK;
+}
+
+int gsea_plan_destroy(gsea_plan p) {
+    if (!p) return GSEA_OK;
+    cudaSetDevice(p->device);
+    cudaStreamSynchronize(p->stream);
+    for (cudaEvent_t e : p->events) cudaEventDestroy(e);
+    free_plan_buffers(p);
+    cudaStreamDestroy(p->stream);
+    delete p;
+    return GSEA_OK;
+}
+
+int gsea_plan_set_inputs(gsea_plan p, const void* exprs, const uint8_t* labels, const int64_t* set_offsets,
+                         const int32_t* set_genes) {
+    if (!p || !exprs || !labels) return fail(GSEA_ERR_INVALID_ARGUMENT, "null argument");
+    int rc = use_device(p);
+    if (rc) return rc;
+    if ((rc = count_labels(p, labels))) return rc;
+    GSEA_CUDA(cudaStreamSynchronize(p->stream), "stream sync");
+    const size_t xbytes = p->tsize * (size_t)p->cfg.num_genes * p->cfg.num_samples;
+    GSEA_CUDA(cudaMemcpy(p->exprs, exprs, xbytes, cudaMemcpyHostToDevice), "copy expression table");
+    GSEA_CUDA(cudaMemcpy(p->labels, labels, (size_t)p->cfg.num_samples, cudaMemcpyHostToDevice), "copy labels");
+    if ((rc = upload_sets(p, set_offsets, set_genes, p->stream, false))) return rc;
+    p->inputs_set = true;
+    return GSEA_OK;
+}
+
+int gsea_plan_execute(gsea_plan p, void* stream) {
+    if (!p) return fail(GSEA_ERR_INVALID_ARGUMENT, "null plan");
+    if (!p->inputs_set) return fail(GSEA_ERR_INVALID_ARGUMENT, "plan inputs were not set");
+    int rc = use_device(p);
+    if (rc) return rc;
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : p->stream;
+    return p->cfg.precision == 64 ? execute_t<double>(p, st) : execute_t<float>(p, st);
+}
+
+int gsea_plan_synchronize(gsea_plan p) {
+    if (!p) return fail(GSEA_ERR_INVALID_ARGUMENT, "null plan");
+    int rc = use_device(p);
+    if (rc) return rc;
+    GSEA_CUDA(cudaStreamSynchronize(p->stream), "stream sync");
+    GSEA_CUDA(cudaDeviceSynchronize(), "device sync");
+    return GSEA_OK;
+}
+
+int gsea_plan_read(gsea_plan p, void* es_out, void* stats_out) {
+    if (!p) return fail(GSEA_ERR_INVALID_ARGUMENT, "null plan");
+    int rc = use_device(p);
+    if (rc) return rc;
+    GSEA_CUDA(cudaDeviceSynchronize(), "device sync");
+    if (injected("d2h")) return fail(GSEA_ERR_INJECTED, "injected device-to-host failure");
+    const size_t T = p->tsize;
+    if (es_out)
+        GSEA_CUDA(cudaMemcpy(es_out, p->es, T * (size_t)p->cfg.num_sets * p->cfg.num_perms, cudaMemcpyDeviceToHost),
+                  "copy enrichment scores");
+    if (stats_out)
+        GSEA_CUDA(cudaMemcpy(stats_out, p->stats, T * 5 * (size_t)p->cfg.num_sets, cudaMemcpyDeviceToHost),
+                  "copy statistics");
+    return GSEA_OK;
+}
+
+int gsea_plan_run_host(gsea_plan p, const void* exprs, const uint8_t* labels, const int64_t* set_offsets,
+                       const int32_t* set_genes, void* es_out, void* stats_out) {
+    if (!p || !exprs || !labels) return fail(GSEA_ERR_INVALID_ARGUMENT, "null argument");
+    int rc = use_device(p);
+    if (rc) return rc;
+    if ((rc = count_labels(p, labels))) return rc;
+    cudaStream_t st = p->stream;
+    const size_t T = p->tsize;
+    const size_t xbytes = T * (size_t)p->cfg.num_genes * p->cfg.num_samples;
+    GSEA_CUDA(cudaMemcpyAsync(p->exprs, exprs, xbytes, cudaMemcpyHostToDevice, st), "copy expression table");
+    GSEA_CUDA(cudaMemcpyAsync(p->labels, labels, (size_t)p->cfg.num_samples, cudaMemcpyHostToDevice, st), "copy labels");
+    if ((rc = upload_sets(p, set_offsets, set_genes, st, true))) return rc;
+    p->inputs_set = true;
+    rc = p->cfg.precision == 64 ? execute_t<double>(p, st) : execute_t<float>(p, st);
+    if (rc) return rc;
+    if (injected("d2h")) return fail(GSEA_ERR_INJECTED, "injected device-to-host failure");
+    if (es_out)
+        GSEA_CUDA(cudaMemcpyAsync(es_out, p->es, T * (size_t)p->cfg.num_sets * p->cfg.num_perms,
+                                  cudaMemcpyDeviceToHost, st), "copy enrichment scores");
+    if (stats_out)
+        GSEA_CUDA(cudaMemcpyAsync(stats_out, p->stats, T * 5 * (size_t)p->cfg.num_sets, cudaMemcpyDeviceToHost, st),
+                  "copy statistics");
+    GSEA_CUDA(cudaStreamSynchronize(st), "stream sync");
+    return GSEA_OK;
+}
+
+int gsea_plan_buffer(gsea_plan p, int which, void** dev_ptr, size_t* bytes) {
+    if (!p || !dev_ptr) return fail(GSEA_ERR_INVALID_ARGUMENT, "null argument");
+    const size_t T = p->tsize, G = (size_t)p->cfg.num_genes, pb = (size_t)p->pb;
+    void* ptr = nullptr;
+    size_t n = 0;
+    switch (which) {
+        case GSEA_BUF_EXPRS: ptr = p->exprs; n = T * G * p->cfg.num_samples; break;
+        case GSEA_BUF_LABEL_MASKS: ptr = p->masks; n = 4 * (size_t)p->words * pb; break;
+        case GSEA_BUF_KEYS: ptr = p->keys; n = T * G * pb; break;
+        case GSEA_BUF_RANKS: ptr = p->ranks; n = (p->ranks16 ? 2 : 4) * G * pb; break;
+        case GSEA_BUF_ORDER: ptr = p->order; n = p->order ? 4 * G * pb : 0; break;
+        case GSEA_BUF_ES: ptr = p->es; n = T * (size_t)p->cfg.num_sets * p->cfg.num_perms; break;
+        case GSEA_BUF_STATS: ptr = p->stats; n = T * 5 * (size_t)p->cfg.num_sets; break;
+        case GSEA_BUF_SORTED: ptr = p->sorted; n = T * G * pb; break;
+        default: return fail(GSEA_ERR_INVALID_ARGUMENT, "unknown buffer id");
+    }
+    *dev_ptr = ptr;
+    if (bytes) *bytes = n;
+    return GSEA_OK;
+}
+
+int gsea_plan_read_buffer(gsea_plan p, int which, void* host_dst, size_t bytes) {
+    if (!host_dst) return fail(GSEA_ERR_INVALID_ARGUMENT, "null destination");
+    void* src = nullptr;
+    size_t n = 0;
+    int rc = gsea_plan_buffer(p, which, &src, &n);
+    if (rc) return rc;
+    if ((rc = use_device(p))) return rc;
+    GSEA_CUDA(cudaDeviceSynchronize(), "device sync");
+    if (!src || n == 0) return fail(GSEA_ERR_INVALID_ARGUMENT, "buffer not allocated");
+    GSEA_CUDA(cudaMemcpy(host_dst, src, bytes < n ? bytes : n, cudaMemcpyDeviceToHost), "copy buffer");
+    return GSEA_OK;
+}
+
+int gsea_plan_info(gsea_plan p, int64_t* perm_batch, int* ranks16) {
+    if (!p) return fail(GSEA_ERR_INVALID_ARGUMENT, "null plan");
+    if (perm_batch) *perm_batch = p->pb;
+    if (ranks16) *ranks16 = p->ranks16 ? 1 : 0;
+    return GSEA_OK;
+}
+
+int gsea_plan_set_debug(gsea_plan p, int keep) {
+    if (!p) return fail(GSEA_ERR_INVALID_ARGUMENT, "null plan");
+    int rc = use_device(p);
+    if (rc) return rc;
+    p->debug = keep != 0;
+    if (p->debug) return alloc_order(p);
+    return GSEA_OK;
+}
+
+int gsea_plan_set_profiling(gsea_plan p, int on) {
+    if (!p) return fail(GSEA_ERR_INVALID_ARGUMENT, "null plan");
+    p->profile = on != 0;
+    return GSEA_OK;
+}
+
+int gsea_plan_stage_times(gsea_plan p, double* ms) {
+    if (!p || !ms) return fail(GSEA_ERR_INVALID_ARGUMENT, "null argument");
+    for (int i = 0; i < GSEA_NUM_STAGES; i++) ms[i] = 0.0;
+    if (!p->profile || p->events_used < 2) return fail(GSEA_ERR_INVALID_ARGUMENT, "no profiled execute");
+    int rc = use_device(p);
+    if (rc) return rc;
+    GSEA_CUDA(cudaEventSynchronize(p->events[p->events_used - 1]), "cudaEventSynchronize");
+    for (size_t i = 1; i < p->events_used; i++) {
+        float t = 0.f;
+        GSEA_CUDA(cudaEventElapsedTime(&t, p->events[i - 1], p->events[i]), "cudaEventElapsedTime");
+        const int stage = p->event_stage[i];
+        if (stage >= 0 && stage < GSEA_NUM_STAGES) ms[stage] += t;
+    }
+    return GSEA_OK;
+}
+
+int gsea_plan_last_launches(gsea_plan p, int64_t* launches) {
+    if (!p || !launches) return fail(GSEA_ERR_INVALID_ARGUMENT, "null argument");
+    *launches = p->last_launches;
+    return GSEA_OK;
+}
+
+int gsea_write_es_dump(const char* prefix, const void* es, int64_t K, int64_t P, int precision, char* path_out,
+                       size_t path_len) {
+    if (!es || K < 1 || P < 1 || (precision != 32 && precision != 64))
+        return fail(GSEA_ERR_INVALID_ARGUMENT, "invalid dump arguments");
+    return write_dump(prefix, es, K, P, precision, path_out, path_len);
+}
+
+int gsea_run(const gsea_config* cfg, const void* exprs, const uint8_t* labels, const int64_t* set_offsets,
+             const int32_t* set_genes, void* es_out, void* stats_out, const char* dump_prefix) {
+    gsea_plan p = nullptr;
+    int rc = gsea_plan_create(cfg, &p);
+    if (rc) return rc;
+    std::vector<unsigned char> es_tmp;
+    const bool dump = dump_prefix && *dump_prefix;
+    void* es_dst = es_out;
+    if (dump && !es_dst) {
+        es_tmp.resize(p->tsize * (size_t)cfg->num_sets * cfg->num_perms);
+        es_dst = es_tmp.data();
+    }
+    rc = gsea_plan_run_host(p, exprs, labels, set_offsets, set_genes, es_dst, stats_out);
+    if (!rc && dump) rc = write_dump(dump_prefix, es_dst, cfg->num_sets, cfg->num_perms, cfg->precision, nullptr, 0);
+    const std::string keep = t_error;
+    gsea_plan_destroy(p);
+    t_error = keep;
+    return rc;
+}
+
+int gsea_run_f32(const float* exprs, int64_t G, int64_t S, const uint8_t* labels, const int64_t* off,
+                 const int32_t* genes, int64_t K, int64_t P, int metric, int ascending, float* es_out,
+                 float* stats_out, const char* dump_prefix) {
+    gsea_config c;
+    gsea_config_init(&c);
+    c.num_genes = G; c.num_samples = S; c.num_sets = K; c.num_perms = P;
+    c.metric = metric; c.ascending = ascending; c.precision = 32;
+    return gsea_run(&c, exprs, labels, off, genes, es_out, stats_out, dump_prefix);
+}
+
+int gsea_run_f64(const double* exprs, int64_t G, int64_t S, const uint8_t* labels, const int64_t* off,
+                 const int32_t* genes, int64_t K, int64_t P, int metric, int ascending, double* es_out,
+                 double* stats_out, const char* dump_prefix) {
+    gsea_config c;
+    gsea_config_init(&c);
+    c.num_genes = G; c.num_samples = S; c.num_sets = K; c.num_perms = P;
+    c.metric = metric; c.ascending = ascending; c.precision = 64;
+    return gsea_run(&c, exprs, labels, off, genes, es_out, stats_out, dump_prefix);
+}
+
+}  // extern "C"

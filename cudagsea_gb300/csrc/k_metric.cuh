@@ -1,0 +1,226 @@
+// k_metric.cuh -- plain-form class statistics and ranking metric.
+//
+// For every (permutation, gene) the kernel accumulates class-A / class-B
+// statistics over the samples in index order and finalises one of the 14
+// reference metrics, reproducing the reference arithmetic operation by
+// operation (src/include/functors.cuh:10-433, dispatch
+// src/include/correlate_genes.cuh:166-295):
+//
+//   accumulators  naive (87-124)   kahan (126-176)  onepass (178-229)
+//                 twopass (232-295) overkill (297-375) knuth (377-433)
+//   combiners     difference (10-15) quotient (17-22) log2 quotient (24-29)
+//                 signal2noise, fixlow (31-54)  T test, fixlow (57-80)
+//
+// All statistics are biased (the reference never forwards `biased`, so the
+// accumulators use their default biased=true).  Every product is rounded
+// before it is added (Exact<T>), matching the reference's CPU arithmetic.
+//
+// Work decomposition (GB300): a thread owns one gene and PB permutations.
+// Each expression value x[s][g] is loaded once per PB permutations (coalesced
+// across the genes of a warp, patient-major table) and the class bit of each
+// permutation is a warp-uniform bit of a shared-memory mask word, so the
+// class selection never diverges.
+#pragma once
+#include "common.cuh"
+#include "kernels.h"
+
+namespace gsea {
+
+enum AccKind { ACC_NAIVE, ACC_KAHAN, ACC_ONEPASS, ACC_TWOPASS, ACC_KNUTH, ACC_OVERKILL };
+enum CombKind { COMB_DIFF, COMB_RATIO, COMB_LOG2, COMB_S2N, COMB_TTEST };
+
+template <class T, int COMB>
+__device__ __forceinline__ T combine(T mA, T vA, T nA, T mB, T vB, T nB) {
+    using E = Exact<T>;
+    if (COMB == COMB_DIFF) return E::sub(mA, mB);
+    if (COMB == COMB_RATIO) return E::div(mA, mB);
+    if (COMB == COMB_LOG2) return E::log2q(E::div(mA, mB));
+    if (COMB == COMB_S2N) {
+        T sA = E::sqrt(vA), sB = E::sqrt(vB);
+        const T lowA = E::low(0.2, cuabs(mA));
+        const T lowB = E::low(0.2, cuabs(mB));
+        sA = lowA < sA ? sA : lowA;
+        sB = lowB < sB ? sB : lowB;
+        return E::div(E::sub(mA, mB), E::add(sA, sB));
+    }
+    // COMB_TTEST
+    T wA = vA, wB = vB;
+    const T lowA = E::low(0.04, cuabs(mA));
+    const T lowB = E::low(0.04, cuabs(mB));
+    wA = lowA < wA ? wA : lowA;
+    wB = lowB < wB ? wB : lowB;
+    return E::div(E::sub(mA, mB), E::sqrt(E::add(E::div(wA, nA), E::div(wB, nB))));
+}
+
+template <int ACC, int COMB, class T, int PB>
+__global__ void __launch_bounds__(128)
+metric_kernel(const T* __restrict__ X, int G, int S, const uint32_t* __restrict__ masks, int words,
+              int num_perms, T nA, T nB, T* __restrict__ keys) {
+    using E = Exact<T>;
+    extern __shared__ uint32_t sm_masks[];  // [PB][words]
+    const int p0 = blockIdx.y * PB;
+    for (int i = threadIdx.x; i < PB * words; i += blockDim.x) {
+        const int j = i / words, w = i - j * words;
+        sm_masks[i] = (p0 + j < num_perms) ? masks[(int64_t)(p0 + j) * words + w] : 0u;
+    }
+    __syncthreads();
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= G) return;
+    const T* xg = X + g;
+
+    T mA[PB], mB[PB], vA[PB], vB[PB], cA[PB], cB[PB];
+    int iA[PB], iB[PB];
+#pragma unroll
+    for (int j = 0; j < PB; j++) {
+        mA[j] = mB[j] = vA[j] = vB[j] = cA[j] = cB[j] = T(0);
+        iA[j] = iB[j] = 0;
+    }
+
+    // ---------------- pass 1 ----------------
+    for (int s0 = 0, w = 0; s0 < S; s0 += 32, w++) {
+        uint32_t mw[PB];
+#pragma unroll
+        for (int j = 0; j < PB; j++) mw[j] = sm_masks[j * words + w];
+        const int n = min(32, S - s0);
+        for (int t = 0; t < n; t++) {
+            const T x = __ldg(xg + (int64_t)(s0 + t) * G);
+            T xx = T(0);
+            if (ACC == ACC_ONEPASS) xx = E::mul(x, x);
+#pragma unroll
+            for (int j = 0; j < PB; j++) {
+                const bool l = (mw[j] >> t) & 1u;  // class A <=> permuted label 0
+                if (ACC == ACC_NAIVE) {
+                    mA[j] = E::add(mA[j], E::mul(l ? T(1) : T(0), x));
+                    mB[j] = E::add(mB[j], E::mul(l ? T(0) : T(1), x));
+                } else if (ACC == ACC_KAHAN || ACC == ACC_OVERKILL) {
+                    const T acc = l ? mA[j] : mB[j];
+                    const T alpha = E::sub(x, l ? cA[j] : cB[j]);
+                    const T beta = E::add(acc, alpha);
+                    const T kk = E::sub(E::sub(beta, acc), alpha);
+                    if (l) { cA[j] = kk; mA[j] = beta; } else { cB[j] = kk; mB[j] = beta; }
+                } else if (ACC == ACC_ONEPASS) {
+                    if (l) { mA[j] = E::add(mA[j], x); vA[j] = E::add(vA[j], xx); }
+                    else   { mB[j] = E::add(mB[j], x); vB[j] = E::add(vB[j], xx); }
+                } else if (ACC == ACC_TWOPASS) {
+                    if (l) mA[j] = E::add(mA[j], x); else mB[j] = E::add(mB[j], x);
+                } else {  // ACC_KNUTH
+                    if (l) {
+                        iA[j]++;
+                        const T d = E::sub(x, mA[j]);
+                        mA[j] = E::add(mA[j], E::div(d, (T)iA[j]));
+                        vA[j] = E::add(vA[j], E::mul(d, E::sub(x, mA[j])));
+                    } else {
+                        iB[j]++;
+                        const T d = E::sub(x, mB[j]);
+                        mB[j] = E::add(mB[j], E::div(d, (T)iB[j]));
+                        vB[j] = E::add(vB[j], E::mul(d, E::sub(x, mB[j])));
+                    }
+                }
+            }
+        }
+    }
+
+    if (ACC != ACC_KNUTH) {
+#pragma unroll
+        for (int j = 0; j < PB; j++) { mA[j] = E::div(mA[j], nA); mB[j] = E::div(mB[j], nB); }
+    }
+    if (ACC == ACC_ONEPASS) {
+#pragma unroll
+        for (int j = 0; j < PB; j++) {
+            vA[j] = E::sub(E::div(vA[j], nA), E::mul(mA[j], mA[j]));
+            vB[j] = E::sub(E::div(vB[j], nB), E::mul(mB[j], mB[j]));
+        }
+    }
+
+    // ---------------- pass 2 (twopass, overkill) ----------------
+    if (ACC == ACC_TWOPASS || ACC == ACC_OVERKILL) {
+        // cA/cB hold the sums of deviations (overkill's aux) from here on
+#pragma unroll
+        for (int j = 0; j < PB; j++) cA[j] = cB[j] = T(0);
+        for (int s0 = 0, w = 0; s0 < S; s0 += 32, w++) {
+            uint32_t mw[PB];
+#pragma unroll
+            for (int j = 0; j < PB; j++) mw[j] = sm_masks[j * words + w];
+            const int n = min(32, S - s0);
+            for (int t = 0; t < n; t++) {
+                const T x = __ldg(xg + (int64_t)(s0 + t) * G);
+#pragma unroll
+                for (int j = 0; j < PB; j++) {
+                    const bool l = (mw[j] >> t) & 1u;
+                    const T d = E::sub(x, l ? mA[j] : mB[j]);
+                    const T dd = E::mul(d, d);
+                    if (l) {
+                        if (ACC == ACC_OVERKILL) cA[j] = E::add(cA[j], d);
+                        vA[j] = E::add(vA[j], dd);
+                    } else {
+                        if (ACC == ACC_OVERKILL) cB[j] = E::add(cB[j], d);
+                        vB[j] = E::add(vB[j], dd);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < PB; j++) {
+            if (ACC == ACC_OVERKILL) {
+                vA[j] = E::sub(vA[j], E::div(E::mul(cA[j], cA[j]), nA));
+                vB[j] = E::sub(vB[j], E::div(E::mul(cB[j], cB[j]), nB));
+            }
+            vA[j] = E::div(vA[j], nA);
+            vB[j] = E::div(vB[j], nB);
+        }
+    }
+    if (ACC == ACC_KNUTH) {
+#pragma unroll
+        for (int j = 0; j < PB; j++) { vA[j] = E::div(vA[j], nA); vB[j] = E::div(vB[j], nB); }
+    }
+
+#pragma unroll
+    for (int j = 0; j < PB; j++) {
+        if (p0 + j < num_perms)
+            keys[(int64_t)(p0 + j) * G + g] = combine<T, COMB>(mA[j], vA[j], nA, mB[j], vB[j], nB);
+    }
+}
+
+template <int ACC, int COMB, class T>
+cudaError_t launch_metric_t(const T* X, int G, int S, const uint32_t* masks, int words,
+                            int num_perms, int64_t nA, int64_t nB, T* keys, cudaStream_t st) {
+    constexpr int PB = 8;
+    const int threads = 128;
+    dim3 grid((G + threads - 1) / threads, (num_perms + PB - 1) / PB);
+    const size_t smem = sizeof(uint32_t) * PB * words;
+    metric_kernel<ACC, COMB, T, PB><<<grid, threads, smem, st>>>(X, G, S, masks, words, num_perms,
+                                                                 (T)nA, (T)nB, keys);
+    launches_add(1);
+    return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_metric_impl(int metric, const T* X, int G, int S, const uint32_t* masks,
+                               int words, int num_perms, int64_t nA, int64_t nB, T* keys,
+                               cudaStream_t st) {
+    if (num_perms <= 0) return cudaSuccess;
+#define GSEA_M(ID, A, C)                                                                        \
+    case ID:                                                                                   \
+        return launch_metric_t<A, C, T>(X, G, S, masks, words, num_perms, nA, nB, keys, st);
+    switch (metric) {
+        GSEA_M(0, ACC_NAIVE, COMB_DIFF)
+        GSEA_M(1, ACC_NAIVE, COMB_RATIO)
+        GSEA_M(2, ACC_NAIVE, COMB_LOG2)
+        GSEA_M(3, ACC_KAHAN, COMB_DIFF)
+        GSEA_M(4, ACC_KAHAN, COMB_RATIO)
+        GSEA_M(5, ACC_KAHAN, COMB_LOG2)
+        GSEA_M(6, ACC_ONEPASS, COMB_S2N)
+        GSEA_M(7, ACC_ONEPASS, COMB_TTEST)
+        GSEA_M(8, ACC_TWOPASS, COMB_S2N)
+        GSEA_M(9, ACC_TWOPASS, COMB_TTEST)
+        GSEA_M(10, ACC_KNUTH, COMB_S2N)
+        GSEA_M(11, ACC_KNUTH, COMB_TTEST)
+        GSEA_M(12, ACC_OVERKILL, COMB_S2N)
+        GSEA_M(13, ACC_OVERKILL, COMB_TTEST)
+        default:
+            return cudaErrorInvalidValue;
+    }
+#undef GSEA_M
+}
+
+}  // namespace gsea

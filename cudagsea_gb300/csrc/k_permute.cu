@@ -1,0 +1,107 @@
+// k_permute.cu -- on-device label permutations.
+//
+// Permutation p (global index q = perm_offset + p) shuffles the label vector
+// with a Fisher-Yates pass driven by a fast-KISS generator seeded with
+// q + seed, exactly as correlate_gpu does on thread 0 of each block
+// (src/include/correlate_genes.cuh:44-56; generator src/include/rngpu/rngpu.hpp:
+// 27-38 hash, 145-178 KISS, 288-303 shuffle).  Permutation 0 is the identity.
+// The generator is counter-based in q: any permutation range can be produced
+// independently, which is what shards and perm batches rely on.
+//
+// Output: one bit per sample, bit set <=> class A (permuted label 0), the
+// form the metric kernels consume.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace gsea {
+namespace {
+
+__device__ __forceinline__ uint32_t nv_hash(uint32_t x) {
+    x = (x + 0x7ed55d16u) + (x << 12);
+    x = (x ^ 0xc761c23cu) ^ (x >> 19);
+    x = (x + 0x165667b1u) + (x << 5);
+    x = (x + 0xd3a2646cu) ^ (x << 9);
+    x = (x + 0xfd7046c5u) + (x << 3);
+    x = (x ^ 0xb55a4f09u) ^ (x >> 16);
+    return x;
+}
+
+struct Kiss {
+    uint32_t x, y, z, w, c;
+    __device__ __forceinline__ explicit Kiss(uint32_t seed) {
+        w = seed ? seed : 0xFFFFFFFFu;
+        x = y = z = 0;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            x = nv_hash(w);
+            y = nv_hash(x);
+            z = nv_hash(y);
+            w = nv_hash(z);
+        }
+        c = 0;
+    }
+    __device__ __forceinline__ uint32_t next() {
+        y ^= y << 5;
+        y ^= y >> 7;
+        y ^= y << 22;
+        const int32_t t = (int32_t)(z + w + c);
+        z = w;
+        c = t < 0;
+        w = (uint32_t)t & 2147483647u;
+        x += 1411392427u;
+        return x + y + w;
+    }
+};
+
+constexpr int kPermThreads = 32;
+
+// one thread per permutation; the label vector of each thread lives in
+// shared memory, interleaved by thread
+__global__ void __launch_bounds__(kPermThreads)
+permute_kernel(const uint8_t* __restrict__ labels, int S, int64_t num_perms, int64_t perm_offset,
+               uint32_t seed, uint32_t* __restrict__ masks, int words) {
+    extern __shared__ uint8_t lab[];  // [S][kPermThreads]
+    const int t = threadIdx.x;
+    const int64_t p = (int64_t)blockIdx.x * kPermThreads + t;
+    for (int s = 0; s < S; s++) lab[s * kPermThreads + t] = labels[s];
+    if (p >= num_perms) return;
+    const uint64_t q = (uint64_t)(perm_offset + p);
+    if (q != 0) {
+        Kiss rng((uint32_t)(q + seed));
+        for (int i = S - 1; i >= 1; i--) {
+            // (double)u * (i+1) / 2^32 truncated: the product is exact in
+            // double for i+1 < 2^21, so it equals the integer (u*(i+1)) >> 32
+            const uint32_t u = rng.next();
+            const int r = (int)(((uint64_t)u * (uint64_t)(i + 1)) >> 32);
+            const uint8_t a = lab[i * kPermThreads + t];
+            lab[i * kPermThreads + t] = lab[r * kPermThreads + t];
+            lab[r * kPermThreads + t] = a;
+        }
+    }
+    uint32_t* out = masks + p * words;
+    for (int w = 0; w < words; w++) {
+        uint32_t m = 0;
+        const int s_end = min(S, (w + 1) * 32);
+        for (int s = w * 32; s < s_end; s++)
+            m |= (uint32_t)(lab[s * kPermThreads + t] == 0) << (s - w * 32);
+        out[w] = m;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_permute(const uint8_t* labels, int S, int64_t num_perms, int64_t perm_offset,
+                           uint32_t seed, uint32_t* masks, int words, cudaStream_t st) {
+    if (num_perms <= 0) return cudaSuccess;
+    const size_t smem = (size_t)S * kPermThreads;
+    if (smem > 200 * 1024) return cudaErrorInvalidValue;
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(permute_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int64_t blocks = (num_perms + kPermThreads - 1) / kPermThreads;
+    permute_kernel<<<(unsigned)blocks, kPermThreads, smem, st>>>(labels, S, num_perms, perm_offset,
+                                                               seed, masks, words);
+    launches_add(1);
+    return cudaGetLastError();
+}
+
+}  // namespace gsea

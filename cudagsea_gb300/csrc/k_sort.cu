@@ -1,0 +1,373 @@
+// k_sort.cu -- per-permutation stable ranking of genes by metric.
+//
+// Replaces pathway_sort_gpu (src/include/batched_sort.cuh:91-269), which runs
+// CUB's DeviceSegmentedRadixSort in descending order on (metric, gene id)
+// pairs, 128 segments per call.  Here one CTA owns one permutation's segment
+// and runs an LSD radix sort with 8-bit digits on the IEEE radix key:
+//
+//   * stable, so tied metrics keep ascending gene order (CUB's semantics);
+//   * -0.0 ranks below +0.0 and NaNs sit at the two ends, as with CUB;
+//   * digit ranks inside a warp come from __match_any_sync (warp-uniform,
+//     deterministic), ranks across warps from a digit-major scan of per-warp
+//     counters in shared memory.
+//
+// Two variants:
+//   sort_regs_kernel   the whole segment lives in registers (1024 threads x
+//                      ITEMS keys); each pass exchanges keys and gene ids
+//                      through one shared-memory buffer.  fp32, G <= 20,480.
+//   sort_tiled_kernel  any key width and any G: the segment ping-pongs
+//                      between two per-CTA global (L2-resident) buffers and
+//                      each pass streams it in tiles of 4,096 items.
+//
+// Outputs per permutation: ranks[g] (position of gene g), sorted_abs[r]
+// (|metric| of the gene at position r, the running-sum weight of
+// enrichment_scores.cuh:146,183) and optionally order[r] (gene at position r).
+#include "common.cuh"
+#include "kernels.h"
+
+namespace gsea {
+namespace {
+
+constexpr int kThreads = 1024;
+constexpr int kWarps = kThreads / 32;
+
+template <class U>
+__device__ __forceinline__ uint32_t digit_of(U key, int shift) {
+    return (uint32_t)(key >> shift) & 0xFFu;
+}
+
+// inverse of RadixKey<T>::from
+template <class T>
+__device__ __forceinline__ T value_of(typename RadixKey<T>::U key, bool descending);
+template <>
+__device__ __forceinline__ float value_of<float>(uint32_t key, bool descending) {
+    uint32_t u = descending ? ~key : key;
+    u = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    return __uint_as_float(u);
+}
+template <>
+__device__ __forceinline__ double value_of<double>(unsigned long long key, bool descending) {
+    unsigned long long u = descending ? ~key : key;
+    u = (u & 0x8000000000000000ull) ? (u & 0x7fffffffffffffffull) : ~u;
+    return __longlong_as_double((long long)u);
+}
+
+template <class RankT, class T>
+__device__ __forceinline__ void emit(int64_t base, int pos, uint32_t gene, T v, RankT* ranks,
+                                     T* sorted_abs, uint32_t* order) {
+    ranks[base + gene] = (RankT)pos;
+    sorted_abs[base + pos] = cuabs(v);
+    if (order) order[base + pos] = gene;
+}
+
+// Digit-major exclusive scan of cnt[w][d] (w < kWarps, d < 256).  On return
+// cnt[w][d] is the first destination of warp w's items with digit d and
+// tot[d] the digit total.  With base == nullptr the destinations are those of
+// a sort of this tile alone (digit prefix + earlier warps); with base they are
+// base[d] + earlier warps, base[d] being the running output offset of digit d.
+// Must be called by all threads; contains __syncthreads().
+__device__ void scan_counters(uint32_t (*cnt)[256], uint32_t* tot, const uint32_t* base,
+                              uint32_t* warp_sums) {
+    const int tid = threadIdx.x;
+    uint32_t run = 0;
+    if (tid < 256) {
+        for (int w = 0; w < kWarps; w++) {
+            const uint32_t c = cnt[w][tid];
+            cnt[w][tid] = run;
+            run += c;
+        }
+        tot[tid] = run;
+    }
+    if (base) {
+        if (tid < 256) {
+            const uint32_t b = base[tid];
+            for (int w = 0; w < kWarps; w++) cnt[w][tid] += b;
+        }
+        __syncthreads();
+        return;
+    }
+    // exclusive scan of the 256 totals (8 warps of 32)
+    uint32_t incl = run;
+    if (tid < 256) {
+        const int lane = tid & 31;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFullMask, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) warp_sums[tid >> 5] = incl;
+    }
+    __syncthreads();
+    if (tid < 256) {
+        uint32_t before = 0;
+        for (int w = 0; w < (tid >> 5); w++) before += warp_sums[w];
+        const uint32_t excl = before + incl - run;
+        for (int w = 0; w < kWarps; w++) cnt[w][tid] += excl;
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+template <class T, class RankT, int ITEMS>
+__global__ void __launch_bounds__(kThreads, 1)
+sort_regs_kernel(const T* __restrict__ keys, int G, int num_perms, bool descending,
+                 RankT* __restrict__ ranks, T* __restrict__ sorted_abs, uint32_t* __restrict__ order) {
+    using U = typename RadixKey<T>::U;
+    constexpr int TILE = kThreads * ITEMS;
+    extern __shared__ __align__(16) unsigned char smem[];
+    U* exch = reinterpret_cast<U*>(smem);                                   // [TILE]
+    uint16_t* dst16 = reinterpret_cast<uint16_t*>(smem + sizeof(U) * TILE);  // [TILE]
+    uint32_t(*cnt)[256] = reinterpret_cast<uint32_t(*)[256]>(smem + (sizeof(U) + 2) * TILE);
+    uint32_t* tot = reinterpret_cast<uint32_t*>(cnt + kWarps);
+    uint32_t* warp_sums = tot + 256;
+    uint32_t* flag = warp_sums + 8;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t lt = lanemask_lt();
+    const int my0 = warp * 32 * ITEMS + lane;  // slot of item i: my0 + 32*i
+    if (threadIdx.x == 0) *flag = 0u;
+    __syncthreads();
+
+    for (int p = blockIdx.x; p < num_perms; p += gridDim.x) {
+        const T* kp = keys + (int64_t)p * G;
+        U key[ITEMS];
+        uint32_t val[ITEMS];
+#pragma unroll
+        for (int i = 0; i < ITEMS; i++) {
+            const int pos = my0 + 32 * i;
+            key[i] = pos < G ? RadixKey<T>::from(kp[pos], descending) : ~U(0);
+            val[i] = (uint32_t)pos;
+        }
+        for (int shift = 0; shift < 8 * (int)sizeof(U); shift += 8) {
+            for (int d = lane; d < 256; d += 32) cnt[warp][d] = 0;
+            __syncwarp();
+#pragma unroll
+            for (int i = 0; i < ITEMS; i++) {
+                const uint32_t dig = digit_of(key[i], shift);
+                const uint32_t peers = __match_any_sync(kFullMask, dig);
+                const uint32_t before = cnt[warp][dig];
+                dst16[my0 + 32 * i] = (uint16_t)(before + __popc(peers & lt));
+                __syncwarp();
+                if ((peers & lt) == 0) cnt[warp][dig] = before + __popc(peers);
+                __syncwarp();
+            }
+            __syncthreads();
+            scan_counters(cnt, tot, nullptr, warp_sums);
+            if (threadIdx.x < 256 && tot[threadIdx.x] == (uint32_t)TILE) *flag = 1u;
+            __syncthreads();
+            const bool skip = *flag != 0u;
+            __syncthreads();
+            if (threadIdx.x == 0) *flag = 0u;
+            if (skip) continue;  // every item has the same digit: order unchanged
+#pragma unroll
+            for (int i = 0; i < ITEMS; i++) {
+                const uint32_t dig = digit_of(key[i], shift);
+                const uint32_t d = cnt[warp][dig] + dst16[my0 + 32 * i];
+                dst16[my0 + 32 * i] = (uint16_t)d;
+                exch[d] = key[i];
+            }
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < ITEMS; i++) key[i] = exch[my0 + 32 * i];
+            __syncthreads();
+            uint32_t* exv = reinterpret_cast<uint32_t*>(exch);
+#pragma unroll
+            for (int i = 0; i < ITEMS; i++) exv[dst16[my0 + 32 * i]] = val[i];
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < ITEMS; i++) val[i] = exv[my0 + 32 * i];
+            __syncthreads();
+        }
+        const int64_t base = (int64_t)p * G;
+#pragma unroll
+        for (int i = 0; i < ITEMS; i++) {
+            const int pos = my0 + 32 * i;
+            if (val[i] < (uint32_t)G)
+                emit<RankT, T>(base, pos, val[i], value_of<T>(key[i], descending), ranks, sorted_abs,
+                               order);
+        }
+    }
+}
+
+template <class T, int ITEMS>
+size_t regs_smem_bytes() {
+    using U = typename RadixKey<T>::U;
+    return (sizeof(U) + 2) * (size_t)kThreads * ITEMS + sizeof(uint32_t) * (kWarps * 256 + 256 + 8 + 4);
+}
+
+// ---------------------------------------------------------------------------
+constexpr int kTileItems = 4;
+constexpr int kTile = kThreads * kTileItems;
+
+template <class T, class RankT>
+__global__ void __launch_bounds__(kThreads, 1)
+sort_tiled_kernel(const T* __restrict__ keys, int G, int num_perms, bool descending,
+                  RankT* __restrict__ ranks, T* __restrict__ sorted_abs, uint32_t* __restrict__ order,
+                  unsigned char* __restrict__ scratch) {
+    using U = typename RadixKey<T>::U;
+    __shared__ uint32_t cnt[kWarps][256];
+    __shared__ uint32_t hist[256];
+    __shared__ uint32_t base[256];
+    __shared__ uint32_t tot[256];
+    __shared__ uint32_t warp_sums[8];
+    __shared__ uint32_t skip_flag;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t lt = lanemask_lt();
+    const size_t per_cta = (sizeof(U) + sizeof(uint32_t)) * 2 * (size_t)G;
+    unsigned char* mine = scratch + per_cta * blockIdx.x;
+    U* kA = reinterpret_cast<U*>(mine);
+    U* kB = kA + G;
+    uint32_t* vA = reinterpret_cast<uint32_t*>(kB + G);
+    uint32_t* vB = vA + G;
+
+    for (int p = blockIdx.x; p < num_perms; p += gridDim.x) {
+        const T* kp = keys + (int64_t)p * G;
+        for (int i = tid; i < G; i += kThreads) {
+            kA[i] = RadixKey<T>::from(kp[i], descending);
+            vA[i] = (uint32_t)i;
+        }
+        __syncthreads();
+        for (int shift = 0; shift < 8 * (int)sizeof(U); shift += 8) {
+            if (tid < 256) hist[tid] = 0;
+            if (tid == 0) skip_flag = 0;
+            __syncthreads();
+            for (int i = tid; i < G; i += kThreads) atomicAdd(&hist[digit_of(kA[i], shift)], 1u);
+            __syncthreads();
+            // exclusive scan of hist into base
+            {
+                uint32_t v = tid < 256 ? hist[tid] : 0u, incl = v;
+                if (tid < 256) {
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint32_t y = __shfl_up_sync(kFullMask, incl, o);
+                        if (lane >= o) incl += y;
+                    }
+                    if (lane == 31) warp_sums[warp] = incl;
+                    if (v == (uint32_t)G) skip_flag = 1;
+                }
+                __syncthreads();
+                if (tid < 256) {
+                    uint32_t before = 0;
+                    for (int w = 0; w < warp; w++) before += warp_sums[w];
+                    base[tid] = before + incl - v;
+                }
+                __syncthreads();
+            }
+            const bool skip = skip_flag != 0u;
+            __syncthreads();  // every thread has read the flag before it is reset
+            if (skip) continue;  // uniform: every key has the same digit
+            for (int t0 = 0; t0 < G; t0 += kTile) {
+                for (int d = lane; d < 256; d += 32) cnt[warp][d] = 0;
+                __syncwarp();
+                U k[kTileItems];
+                uint32_t v[kTileItems], r[kTileItems], dg[kTileItems];
+#pragma unroll
+                for (int i = 0; i < kTileItems; i++) {
+                    const int pos = t0 + warp * 32 * kTileItems + 32 * i + lane;
+                    const bool valid = pos < G;
+                    k[i] = valid ? kA[pos] : U(0);
+                    v[i] = valid ? vA[pos] : 0u;
+                    dg[i] = valid ? digit_of(k[i], shift) : 256u;
+                    const uint32_t peers = __match_any_sync(kFullMask, dg[i]);
+                    uint32_t before = 0;
+                    if (valid) before = cnt[warp][dg[i]];
+                    r[i] = before + __popc(peers & lt);
+                    __syncwarp();
+                    if (valid && (peers & lt) == 0) cnt[warp][dg[i]] = before + __popc(peers);
+                    __syncwarp();
+                }
+                __syncthreads();
+                scan_counters(cnt, tot, base, warp_sums);
+#pragma unroll
+                for (int i = 0; i < kTileItems; i++) {
+                    if (dg[i] < 256u) {
+                        const uint32_t d = cnt[warp][dg[i]] + r[i];
+                        kB[d] = k[i];
+                        vB[d] = v[i];
+                    }
+                }
+                if (tid < 256) base[tid] += tot[tid];
+                __syncthreads();
+            }
+            __syncthreads();
+            U* tk = kA; kA = kB; kB = tk;
+            uint32_t* tv = vA; vA = vB; vB = tv;
+        }
+        const int64_t b = (int64_t)p * G;
+        for (int pos = tid; pos < G; pos += kThreads)
+            emit<RankT, T>(b, pos, vA[pos], value_of<T>(kA[pos], descending), ranks, sorted_abs, order);
+        __syncthreads();
+        // restore the buffer roles for the next permutation
+        kA = reinterpret_cast<U*>(mine);
+        kB = kA + G;
+        vA = reinterpret_cast<uint32_t*>(kB + G);
+        vB = vA + G;
+    }
+}
+
+int g_num_sms = 0;
+int num_sms() {
+    if (g_num_sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_num_sms <= 0) g_num_sms = 1;
+    }
+    return g_num_sms;
+}
+
+template <class T, class RankT, int ITEMS>
+cudaError_t launch_regs(const T* keys, int G, int P, bool desc, const SortBuffers& o, cudaStream_t st) {
+    const size_t smem = regs_smem_bytes<T, ITEMS>();
+    auto kern = sort_regs_kernel<T, RankT, ITEMS>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int grid = P < 4 * num_sms() ? P : 4 * num_sms();
+    kern<<<grid, kThreads, smem, st>>>(keys, G, P, desc, static_cast<RankT*>(o.ranks),
+                                       static_cast<T*>(o.sorted_abs), o.order);
+    launches_add(1);
+    return cudaGetLastError();
+}
+
+template <class T, class RankT>
+cudaError_t launch_sort_t(const T* keys, int G, int P, bool desc, const SortBuffers& o, cudaStream_t st) {
+    if (sizeof(T) == 4) {
+        if (G <= kThreads * 4) return launch_regs<T, RankT, 4>(keys, G, P, desc, o, st);
+        if (G <= kThreads * 8) return launch_regs<T, RankT, 8>(keys, G, P, desc, o, st);
+        if (G <= kThreads * 12) return launch_regs<T, RankT, 12>(keys, G, P, desc, o, st);
+        if (G <= kThreads * 16) return launch_regs<T, RankT, 16>(keys, G, P, desc, o, st);
+        if (G <= kThreads * 20) return launch_regs<T, RankT, 20>(keys, G, P, desc, o, st);
+    }
+    const int grid = P < num_sms() ? P : num_sms();
+    if (o.scratch_bytes < sort_scratch_bytes<T>(G, P)) return cudaErrorInvalidValue;
+    sort_tiled_kernel<T, RankT><<<grid, kThreads, 0, st>>>(keys, G, P, desc, static_cast<RankT*>(o.ranks),
+                                                          static_cast<T*>(o.sorted_abs), o.order,
+                                                          static_cast<unsigned char*>(o.scratch));
+    launches_add(1);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+template <class T>
+size_t sort_scratch_bytes(int G, int num_perms) {
+    using U = typename RadixKey<T>::U;
+    if (sizeof(T) == 4 && G <= kThreads * 20) return 0;
+    const int grid = num_perms < num_sms() ? num_perms : num_sms();
+    return (sizeof(U) + sizeof(uint32_t)) * 2 * (size_t)G * (size_t)(grid > 0 ? grid : 1);
+}
+template size_t sort_scratch_bytes<float>(int, int);
+template size_t sort_scratch_bytes<double>(int, int);
+
+template <class T>
+cudaError_t launch_sort(const T* keys, int G, int num_perms, bool ascending, const SortBuffers& out,
+                        cudaStream_t st) {
+    if (num_perms <= 0) return cudaSuccess;
+    if (out.ranks16) return launch_sort_t<T, uint16_t>(keys, G, num_perms, !ascending, out, st);
+    return launch_sort_t<T, uint32_t>(keys, G, num_perms, !ascending, out, st);
+}
+template cudaError_t launch_sort<float>(const float*, int, int, bool, const SortBuffers&, cudaStream_t);
+template cudaError_t launch_sort<double>(const double*, int, int, bool, const SortBuffers&, cudaStream_t);
+
+}  // namespace gsea

@@ -1,0 +1,56 @@
+// kernels.h -- host-side launchers of the libgsea103 kernels.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gsea {
+
+// Label permutation: masks[p][w] bit s == 1 <=> permuted label of sample s is
+// 0 (class A) for global permutation perm_offset + p.
+cudaError_t launch_permute(const uint8_t* labels, int S, int64_t num_perms, int64_t perm_offset,
+                           uint32_t seed, uint32_t* masks, int words, cudaStream_t st);
+
+// Plain-form class statistics + metric: keys[p][g] for p < num_perms.
+template <class T>
+cudaError_t launch_metric(int metric, const T* exprs, int G, int S, const uint32_t* masks,
+                          int words, int num_perms, int64_t nA, int64_t nB, T* keys,
+                          cudaStream_t st);
+
+// Per-permutation stable sort of keys (descending unless ascending):
+//   ranks[p][g]   position of gene g (uint16 when G <= 65536, else uint32)
+//   sorted[p][r]  |key| of the gene at position r
+//   order[p][r]   gene at position r (optional, may be null)
+struct SortBuffers {
+    void* ranks;          // uint16_t* or uint32_t*
+    bool ranks16;
+    void* sorted_abs;     // T*
+    uint32_t* order;      // optional
+    void* scratch;        // per-CTA ping-pong buffers for the tiled variant
+    size_t scratch_bytes;
+};
+template <class T>
+size_t sort_scratch_bytes(int G, int num_perms);
+template <class T>
+cudaError_t launch_sort(const T* keys, int G, int num_perms, bool ascending, const SortBuffers& out,
+                        cudaStream_t st);
+
+// Enrichment scores es[k][perm_col0 + p] (row stride es_stride) from ranks and
+// sorted |keys| of num_perms permutations.
+template <class T>
+cudaError_t launch_es(const void* ranks, bool ranks16, const T* sorted_abs, int G, int num_perms,
+                      const int64_t* set_offsets, const int32_t* set_genes, int K, T* es,
+                      int64_t es_stride, int64_t perm_col0, cudaStream_t st);
+
+// Final statistics (ES, NES, NP, FWER, FDR) from es[K][P]; scratch sized by
+// stats_scratch_bytes.
+template <class T>
+size_t stats_scratch_bytes(int K, int64_t P);
+template <class T>
+cudaError_t launch_stats(const T* es, int K, int64_t P, T* stats, void* scratch, cudaStream_t st);
+
+// number of kernel launches issued by the launchers above since the last reset
+int64_t launches_take();
+void launches_add(int64_t n);
+
+}  // namespace gsea

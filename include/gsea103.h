@@ -1,0 +1,209 @@
+/*
+ * gsea103.h -- C ABI of libgsea103.so, the GB300 (sm_103a) implementation of
+ * cudaGSEA's GSEA permutation pipeline.
+ *
+ * Every entry point returns a gsea_status (0 = success) and never exits the
+ * process; the reference instead calls exit() on CUDA errors and unknown
+ * metrics (src/include/cuda_helpers.cuh:10-17, correlate_genes.cuh:292-295).
+ * A human-readable message for the last failure on the calling thread is
+ * available from gsea_last_error().
+ *
+ * Layouts (identical to the reference's R path):
+ *   exprs   patient-major [num_samples][num_genes]
+ *           (src/cudaGSEA_wrapper.cu:229-236 keeps R's column-major table as is)
+ *   labels  uint8 [num_samples], 0 = class A, 1 = class B
+ *   sets    CSR over gene indices: set k = set_genes[set_offsets[k] ..
+ *           set_offsets[k+1]); indices outside [0, num_genes) are ignored and
+ *           duplicates collapse, as create_bitmaps does for unknown symbols
+ *           (src/include/create_bitmaps.cuh:13-65)
+ *   es      [num_sets][num_perms] row-major, permutation 0 = observed labels
+ *           (the .es dump layout, src/include/dump_binary.cuh:10-30)
+ *   stats   struct of arrays [5][num_sets]: ES, NES, NP, FWER, FDR
+ *           (src/include/statistics.cuh:46-117; FDR is filled here, the
+ *           reference leaves it NaN)
+ */
+#ifndef GSEA103_H
+#define GSEA103_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GSEA103_VERSION_MAJOR 0
+#define GSEA103_VERSION_MINOR 1
+
+typedef enum {
+    GSEA_OK = 0,
+    GSEA_ERR_INVALID_ARGUMENT = 1,
+    GSEA_ERR_UNKNOWN_METRIC = 2,      /* reference: exit(1), correlate_genes.cuh:292-295 */
+    GSEA_ERR_CUDA = 3,                /* reference: CUERR -> exit(1)                    */
+    GSEA_ERR_OUT_OF_MEMORY = 4,
+    GSEA_ERR_NO_DEVICE = 5,
+    GSEA_ERR_IO = 6,                  /* reference: exit codes 2-9, error_codes.cuh     */
+    GSEA_ERR_UNSUPPORTED = 7,
+    GSEA_ERR_INJECTED = 8,            /* host-side fault injection (GSEA_FAULT)         */
+    GSEA_ERR_INVALID_INPUT = 9        /* data checks of checkInput (cudaGSEA_wrapper.cpp:156-227) */
+} gsea_status;
+
+/* metric ids in the order of the reference's dispatch (correlate_genes.cuh:166-291) */
+typedef enum {
+    GSEA_NAIVE_DIFF_OF_CLASSES = 0,
+    GSEA_NAIVE_RATIO_OF_CLASSES = 1,
+    GSEA_NAIVE_LOG2_RATIO_OF_CLASSES = 2,
+    GSEA_STABLE_DIFF_OF_CLASSES = 3,
+    GSEA_STABLE_RATIO_OF_CLASSES = 4,
+    GSEA_STABLE_LOG2_RATIO_OF_CLASSES = 5,
+    GSEA_ONEPASS_SIGNAL2NOISE = 6,
+    GSEA_ONEPASS_T_TEST = 7,
+    GSEA_TWOPASS_SIGNAL2NOISE = 8,
+    GSEA_TWOPASS_T_TEST = 9,
+    GSEA_STABLE_SIGNAL2NOISE = 10,
+    GSEA_STABLE_T_TEST = 11,
+    GSEA_OVERKILL_SIGNAL2NOISE = 12,
+    GSEA_OVERKILL_T_TEST = 13,
+    GSEA_NUM_METRICS = 14
+} gsea_metric;
+
+/* pipeline form */
+typedef enum {
+    GSEA_FORM_PLAIN = 0,   /* bit-exact SIMT class statistics in the reference's operation order */
+    GSEA_FORM_CHOSEN = 1   /* tensor-core (tcgen05) class statistics, FP64 finalisation          */
+} gsea_form;
+
+typedef struct {
+    int64_t num_genes;     /* G */
+    int64_t num_samples;   /* S */
+    int64_t num_sets;      /* K */
+    int64_t num_perms;     /* P, permutation 0 = observed labels */
+    int32_t metric;        /* gsea_metric */
+    int32_t precision;     /* 32 (float, like gsea_single_proxy) or 64 (double) */
+    int32_t ascending;     /* 0 = descending ranking (reference default), 1 = ascending */
+    int32_t form;          /* gsea_form */
+    int64_t perm_offset;   /* global index of this plan's first permutation (sharding) */
+    int64_t perm_batch;    /* permutations per device batch, 0 = automatic */
+    uint32_t seed;         /* permutation seed, 42 in the reference (configuration.cuh:29) */
+    int32_t device;        /* CUDA device ordinal, -1 = current device */
+} gsea_config;
+
+typedef struct gsea_plan_s* gsea_plan;
+
+/* ---- errors / metadata ----------------------------------------------------- */
+const char* gsea_status_string(int status);
+/* message of the last failure on this thread ("" if none) */
+const char* gsea_last_error(void);
+/* "naive_diff_of_classes" ... -> id, -1 if unknown.
+ * Replaces the string dispatch of correllate_genes_gpu (correlate_genes.cuh:166-295). */
+int gsea_metric_id(const char* metric_string);
+const char* gsea_metric_name(int metric_id);
+/* default configuration: precision 32, descending, plain form, seed 42 */
+void gsea_config_init(gsea_config* cfg);
+
+/* ---- CUDA devices (replace listCudaDevices_proxy / getCudaDevice_proxy /
+ *      setCudaDevice_proxy, src/cudaGSEA_wrapper.cuh:31-33) ---------------- */
+int gsea_device_count(int* count);
+/* "device <id>: <name> with <n> GiB RAM", as create_device_string_helper
+ * (src/cudaGSEA_wrapper.cu:87-104) */
+int gsea_device_string(int device, char* buf, size_t buflen);
+int gsea_get_device(int* device);
+/* returns the active device in *active (falls back like setCudaDevice_proxy) */
+int gsea_set_device(int device, int* active);
+
+/* ---- one-shot host API (replaces gsea_proxy<>, src/cudaGSEA_wrapper.cu:179-401)
+ * Host buffers in, host buffers out; device memory is allocated and freed
+ * inside the call.  es_out may be NULL; stats_out (5*K) may be NULL.  A
+ * non-empty dump_prefix writes <prefix>_<K>_<P>_<32|64>.es before the
+ * statistics, as gsea_proxy does (cudaGSEA_wrapper.cu:384-390).           */
+int gsea_run(const gsea_config* cfg, const void* exprs, const uint8_t* labels,
+             const int64_t* set_offsets, const int32_t* set_genes,
+             void* es_out, void* stats_out, const char* dump_prefix);
+int gsea_run_f32(const float* exprs, int64_t num_genes, int64_t num_samples,
+                 const uint8_t* labels, const int64_t* set_offsets,
+                 const int32_t* set_genes, int64_t num_sets, int64_t num_perms,
+                 int metric, int ascending, float* es_out, float* stats_out,
+                 const char* dump_prefix);
+int gsea_run_f64(const double* exprs, int64_t num_genes, int64_t num_samples,
+                 const uint8_t* labels, const int64_t* set_offsets,
+                 const int32_t* set_genes, int64_t num_sets, int64_t num_perms,
+                 int metric, int ascending, double* es_out, double* stats_out,
+                 const char* dump_prefix);
+
+/* ---- flat form of the C++ proxies gsea_single_proxy / gsea_double_proxy
+ * (src/cudaGSEA_wrapper.cuh:39-61) for callers without C++: gene symbols
+ * and gene-set symbols as C strings (unknown symbols ignored, duplicates
+ * collapse), sort_direction 1 = descending, swap_labels flips the classes.
+ * result_out receives 5*num_sets values of the chosen precision.        */
+int gsea_proxy_run(int precision, const void* exprs, int64_t num_genes, int64_t num_samples,
+                   const char* const* gene_symbols, const uint8_t* labels, int64_t num_sets,
+                   const int64_t* set_symbol_offsets, const char* const* set_symbols,
+                   const char* metric, int64_t num_perms, int sort_direction, int swap_labels,
+                   const char* dump_filename, void* result_out);
+
+/* ---- plan API: device-resident inputs, repeated execution --------------- */
+int gsea_plan_create(const gsea_config* cfg, gsea_plan* out);
+int gsea_plan_destroy(gsea_plan plan);
+/* copy inputs from host memory (synchronous) */
+int gsea_plan_set_inputs(gsea_plan plan, const void* exprs, const uint8_t* labels,
+                         const int64_t* set_offsets, const int32_t* set_genes);
+/* run permutation -> metric -> sort -> ES -> statistics on `stream`
+ * (a cudaStream_t, NULL = the plan's own stream); asynchronous */
+int gsea_plan_execute(gsea_plan plan, void* stream);
+/* one call = upload of all inputs from host + execute + download of the
+ * results to host, ordered on the plan's stream and synchronised at the end
+ * (the end-to-end path; pinned host buffers make the copies asynchronous) */
+int gsea_plan_run_host(gsea_plan plan, const void* exprs, const uint8_t* labels,
+                       const int64_t* set_offsets, const int32_t* set_genes,
+                       void* es_out, void* stats_out);
+/* wait for the plan's stream, then copy results to host (either may be NULL) */
+int gsea_plan_read(gsea_plan plan, void* es_out, void* stats_out);
+int gsea_plan_synchronize(gsea_plan plan);
+
+/* device buffers of a plan, for zero-copy consumers and parity tests.
+ * Per-permutation buffers hold the LAST permutation batch of the last
+ * execute (P_batch = the plan's batch size, see gsea_plan_info). */
+typedef enum {
+    GSEA_BUF_EXPRS = 0,       /* [S][G] T                                      */
+    GSEA_BUF_LABEL_MASKS = 1, /* [P_batch][W] uint32, bit s set = class A      */
+    GSEA_BUF_KEYS = 2,        /* [P_batch][G] T, metric per (perm, gene)       */
+    GSEA_BUF_RANKS = 3,       /* [P_batch][G] uint16 (G <= 65536) or uint32    */
+    GSEA_BUF_ORDER = 4,       /* [P_batch][G] uint32, gene at each position    */
+    GSEA_BUF_ES = 5,          /* [K][P] T                                      */
+    GSEA_BUF_STATS = 6,       /* [5][K] T                                      */
+    GSEA_BUF_SORTED = 7       /* [P_batch][G] T, |metric| at each position     */
+} gsea_buffer;
+int gsea_plan_buffer(gsea_plan plan, int which, void** dev_ptr, size_t* bytes);
+/* synchronise and copy min(bytes, buffer size) bytes of a plan buffer to host */
+int gsea_plan_read_buffer(gsea_plan plan, int which, void* host_dst, size_t bytes);
+/* permutations per device batch and whether ranks are stored as uint16 */
+int gsea_plan_info(gsea_plan plan, int64_t* perm_batch, int* ranks16);
+/* keep_intermediates != 0 also materialises GSEA_BUF_ORDER on execute */
+int gsea_plan_set_debug(gsea_plan plan, int keep_intermediates);
+/* kernel launches issued by the last execute */
+int gsea_plan_last_launches(gsea_plan plan, int64_t* launches);
+/* stage timing: with profiling on, execute records CUDA events between the
+ * stages on its stream (the reference's TIMERSTART/TIMERSTOP, cuda_helpers.cuh:
+ * 20-32); gsea_plan_stage_times waits for them and returns the device time of
+ * each stage of the last execute in milliseconds, summed over batches */
+typedef enum {
+    GSEA_STAGE_PERMUTE = 0, GSEA_STAGE_METRIC = 1, GSEA_STAGE_SORT = 2,
+    GSEA_STAGE_ES = 3, GSEA_STAGE_STATS = 4, GSEA_NUM_STAGES = 5
+} gsea_stage;
+int gsea_plan_set_profiling(gsea_plan plan, int on);
+int gsea_plan_stage_times(gsea_plan plan, double* ms /* [GSEA_NUM_STAGES] */);
+
+/* pinned (page-locked) host memory for asynchronous copies */
+int gsea_host_alloc(size_t bytes, void** ptr);
+int gsea_host_free(void* ptr);
+
+/* ---- .es dump (src/include/dump_binary.cuh:10-30 and naming at
+ *      src/cudaGSEA_wrapper.cu:384-390) --------------------------------- */
+int gsea_write_es_dump(const char* prefix, const void* es, int64_t num_sets,
+                       int64_t num_perms, int precision, char* path_out,
+                       size_t path_len);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GSEA103_H */

@@ -51,7 +51,7 @@ def build(force: bool = False) -> str:
     """Compile gsea_oracle.cpp (g++, -ffp-contract=off, OpenMP)."""
     src = os.path.join(HERE, "gsea_oracle.cpp")
     os.makedirs(BUILD_DIR, exist_ok=True)
-    if (not force and os.path.exists(ORACLE_SO)
+    if (not force and os.path.exists(ORACLE_SO) and _elf_machine(ORACLE_SO) == platform.machine()
             and os.path.getmtime(ORACLE_SO) >= os.path.getmtime(src)):
         return ORACLE_SO
     tmp = ORACLE_SO + f".tmp{os.getpid()}"

@@ -1,0 +1,272 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle and with the
+reference's golden outputs.  Stage by stage:
+
+  permutations   label masks == oracle permutations (bit-exact)
+  metric         keys == oracle keys bit-exact (log2 metrics: <= 2 ulp);
+                 == the reference's keys (SHA-256 of the golden fixture)
+  sort           order == oracle's stable order of the GPU's own keys; ranks
+                 are its inverse; sorted weights == |keys| in that order
+  ES             within 1e-5 relative (fp32) / 1e-12 (fp64) of the oracle's
+                 dense Kahan running sum over the same order
+  statistics     bit-identical to the oracle's final_statistics + FDR for
+                 the GPU's own ES
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from cudagsea_gb300 import api, synthetic
+from cudagsea_gb300 import _native as N
+from tests import helpers as H
+from tests.golden import make_golden as MG
+
+pytestmark = pytest.mark.gpu
+
+
+def run_plan(d, metric, double=False, P=None, perm_offset=0, perm_batch=0, ascending=False, debug=True):
+    P = P or d.num_perms
+    plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, P, metric, precision=64 if double else 32,
+                    ascending=ascending, perm_offset=perm_offset, perm_batch=perm_batch)
+    if debug:
+        plan.set_debug(True)
+    plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+    plan.execute()
+    es, st = plan.read()
+    out = {"es": es, "stats": st, "plan": plan}
+    if debug:
+        pb, G = plan.perm_batch, d.num_genes
+        dt = plan.dtype
+        out["keys"] = plan.read_buffer(N.BUF_KEYS, dt, (pb, G))
+        out["order"] = plan.read_buffer(N.BUF_ORDER, np.uint32, (pb, G))
+        out["ranks"] = plan.read_buffer(N.BUF_RANKS, np.uint16 if plan.ranks16 else np.uint32, (pb, G))
+        out["sorted"] = plan.read_buffer(N.BUF_SORTED, dt, (pb, G))
+        words = (d.num_samples + 31) // 32
+        out["masks"] = plan.read_buffer(N.BUF_LABEL_MASKS, np.uint32, (pb, words))
+    return out
+
+
+def decode_masks(masks, S):
+    bits = np.unpackbits(masks.view(np.uint8), bitorder="little").reshape(masks.shape[0], -1)[:, :S]
+    return np.where(bits == 1, 0, 1).astype(np.uint8)  # bit set = class A = label 0
+
+
+def check_sort(keys, order, ranks, sorted_abs, ascending=False):
+    sk, ref_order = oracle.sort(keys, ascending=ascending)
+    np.testing.assert_array_equal(order, ref_order)
+    P, G = keys.shape
+    inv = np.empty_like(order)
+    inv[np.arange(P)[:, None], order] = np.arange(G, dtype=order.dtype)[None, :]
+    np.testing.assert_array_equal(ranks.astype(np.uint32), inv)
+    np.testing.assert_array_equal(sorted_abs, np.where(sk < 0, -sk, sk))
+    return sk, ref_order
+
+
+def test_permutation_masks(gpu):
+    g = H.load("perm_labels.npz")
+    labels = g["labels"]
+    S = labels.size
+    d = synthetic.make(64, S, 2, 17, seed=5, n_class_b=int(labels.sum()))
+    d.labels = labels
+    r = run_plan(d, "naive_diff_of_classes")
+    np.testing.assert_array_equal(decode_masks(r["masks"], S), g["perm_labels"])
+    # counter-based stream: a shifted plan reproduces the same global permutations
+    r2 = run_plan(d, "naive_diff_of_classes", P=8, perm_offset=1000)
+    np.testing.assert_array_equal(decode_masks(r2["masks"], S), oracle.perm_labels(labels, 8, shift=1000))
+
+
+@pytest.mark.parametrize("double", [False, True], ids=["f32", "f64"])
+def test_all_metrics_stagewise(gpu, double):
+    g = H.load(f"metrics_{'f64' if double else 'f32'}.npz")
+    d = MG.metrics_case()
+    for m in range(14):
+        name = api.METRICS[m]
+        r = run_plan(d, m, double=double)
+        ok = oracle.metric(m, d.exprs, d.labels, d.num_perms, double=double)
+        if m in H.LOG_METRICS:
+            assert H.ulp_diff(r["keys"], ok).max() <= 2, name
+        else:
+            np.testing.assert_array_equal(r["keys"].view(np.uint8), ok.view(np.uint8), err_msg=name)
+            assert H.sha(r["keys"]) == str(g[f"keys_sha_{m}"]), name
+        sk, order = check_sort(r["keys"], r["order"], r["ranks"], r["sorted"])
+        es_o = oracle.es(sk, order, d.set_offsets, d.set_genes)
+        assert H.es_close(r["es"], es_o, double).all(), (name, np.nanmax(np.abs(r["es"] - es_o)))
+        st_o = oracle.stats(r["es"])
+        np.testing.assert_array_equal(r["stats"].view(np.uint8), st_o.view(np.uint8), err_msg=name)
+        # against the reference's own ES: equal within tolerance unless a tie
+        # explains the difference (the reference CPU sort is unstable)
+        ref_es = g[f"es_{m}"]
+        for kk, p in np.argwhere(~H.es_close(r["es"], ref_es, double)):
+            members = d.set_genes[d.set_offsets[kk]:d.set_offsets[kk + 1]]
+            if m in H.LOG_METRICS:
+                continue  # near-tie rank flips are allowed for the log metrics
+            assert H.tie_explained(sk[p], order[p], members), (name, kk, p)
+
+
+@pytest.mark.parametrize("double", [False, True], ids=["f32", "f64"])
+def test_config1_vs_reference(gpu, double):
+    """2,000 x 40, 50 sets, 1,024 permutations, twopass_signal2noise."""
+    g = H.load(f"small_{'f64' if double else 'f32'}.npz")
+    d = synthetic.small()
+    es, st = api.gsea(d.exprs, d.labels, d.set_offsets, d.set_genes, d.num_perms, "twopass_signal2noise",
+                      precision=64 if double else 32)
+    K = d.num_sets
+    assert H.es_close(es[:, :128], g["es_head"], double).mean() > 0.999
+    ref = g["stats"]
+    assert H.es_close(st[:K], ref[:K], double).all()          # ES
+    assert H.es_close(st[K:2 * K], ref[K:2 * K], double).all()  # NES
+    np.testing.assert_allclose(st[2 * K:4 * K], ref[2 * K:4 * K], atol=2.0 / d.num_perms)  # NP, FWER
+    # the oracle on the GPU's ES reproduces the GPU's statistics bit for bit
+    np.testing.assert_array_equal(oracle.stats(es).view(np.uint8), st.view(np.uint8))
+
+
+@pytest.mark.parametrize("double", [False, True], ids=["f32", "f64"])
+def test_tie_heavy_data(gpu, double):
+    g = H.load(f"ties_{'f64' if double else 'f32'}.npz")
+    d = MG.ties_case()
+    for m in (0, 8):
+        r = run_plan(d, m, double=double)
+        assert H.sha(r["keys"]) == str(g[f"keys_sha_{m}"])
+        sk, order = check_sort(r["keys"], r["order"], r["ranks"], r["sorted"])
+        es_o = oracle.es(sk, order, d.set_offsets, d.set_genes)
+        assert H.es_close(r["es"], es_o, double).all()
+
+
+def test_tiny_shapes_all_metrics(gpu):
+    d = synthetic.tiny()
+    for double in (False, True):
+        for m in range(14):
+            r = run_plan(d, m, double=double)
+            ok = oracle.metric(m, d.exprs, d.labels, d.num_perms, double=double)
+            assert H.ulp_diff(r["keys"], ok).max() <= (2 if m in H.LOG_METRICS else 0)
+            sk, order = check_sort(r["keys"], r["order"], r["ranks"], r["sorted"])
+            es_o = oracle.es(sk, order, d.set_offsets, d.set_genes)
+            assert H.es_close(r["es"], es_o, double).all(), (m, double)
+
+
+@pytest.mark.parametrize("G", [1, 31, 4097, 20480, 20481, 30000])
+@pytest.mark.parametrize("double", [False, True], ids=["f32", "f64"])
+def test_sort_sizes(gpu, G, double):
+    """Register-resident sort up to 20,480 genes (fp32), tiled sort beyond and for fp64."""
+    d = synthetic.make(G, 12, 3, 5, seed=G, n_class_b=6, n_shift=min(10, G), set_min=1, set_max=min(40, G))
+    r = run_plan(d, "twopass_signal2noise", double=double)
+    sk, order = check_sort(r["keys"], r["order"], r["ranks"], r["sorted"])
+    es_o = oracle.es(sk, order, d.set_offsets, d.set_genes)
+    assert H.es_close(r["es"], es_o, double).all()
+
+
+def test_ascending_order(gpu):
+    d = MG.metrics_case()
+    r = run_plan(d, "twopass_t_test", ascending=True)
+    sk, order = check_sort(r["keys"], r["order"], r["ranks"], r["sorted"], ascending=True)
+    es_o = oracle.es(sk, order, d.set_offsets, d.set_genes)
+    assert H.es_close(r["es"], es_o, False).all()
+
+
+def test_edge_sets(gpu):
+    """Empty overlap, all genes, duplicates, out-of-range ids, single-gene sets."""
+    d = synthetic.make(200, 10, 1, 16, seed=11, n_class_b=5)
+    G = d.num_genes
+    sets = [np.array([], np.int32), np.arange(G, dtype=np.int32), np.array([3, 3, 3, 7, 7], np.int32),
+            np.array([-5, 10**6, 4], np.int32), np.array([0], np.int32), np.array([G - 1], np.int32)]
+    d.set_offsets = np.r_[0, np.cumsum([s.size for s in sets])].astype(np.int64)
+    d.set_genes = np.concatenate(sets).astype(np.int32)
+    for double in (False, True):
+        r = run_plan(d, "twopass_signal2noise", double=double)
+        sk, order = check_sort(r["keys"], r["order"], r["ranks"], r["sorted"])
+        es_o = oracle.es(sk, order, d.set_offsets, d.set_genes)
+        assert H.es_close(r["es"], es_o, double).all(), (r["es"], es_o)
+        np.testing.assert_array_equal(oracle.stats(r["es"]).view(np.uint8), r["stats"].view(np.uint8))
+
+
+def test_nonfinite_keys(gpu):
+    """Zeros in class means make the ratio metrics produce inf/NaN keys."""
+    d = synthetic.make(300, 8, 6, 16, seed=3, n_class_b=4, set_min=5, set_max=60)
+    d.exprs[:, :40] = 0.0
+    d.exprs[:4, 40:60] = 0.0
+    for m in (1, 2, 4):
+        for double in (False, True):
+            r = run_plan(d, m, double=double)
+            ok = oracle.metric(m, d.exprs, d.labels, d.num_perms, double=double)
+            assert H.ulp_diff(r["keys"], ok).max() <= (2 if m in H.LOG_METRICS else 0)
+            sk, order = check_sort(r["keys"], r["order"], r["ranks"], r["sorted"])
+            es_o = oracle.es(sk, order, d.set_offsets, d.set_genes)
+            assert H.es_close(r["es"], es_o, double).all(), (m, double)
+
+
+def test_perm_batches_and_shards_agree(gpu):
+    d = MG.metrics_case()
+    full = run_plan(d, "twopass_signal2noise", P=64, debug=False)
+    batched = run_plan(d, "twopass_signal2noise", P=64, perm_batch=7, debug=False)
+    np.testing.assert_array_equal(full["es"], batched["es"])
+    np.testing.assert_array_equal(full["stats"], batched["stats"])
+    a = run_plan(d, "twopass_signal2noise", P=40, debug=False)
+    b = run_plan(d, "twopass_signal2noise", P=24, perm_offset=40, debug=False)
+    np.testing.assert_array_equal(np.concatenate([a["es"], b["es"]], axis=1), full["es"])
+
+
+def test_proxy_symbol_mapping(gpu, tmp_path):
+    """GSEA() through gsea_proxy_run: unknown symbols dropped, duplicates collapse."""
+    d = MG.metrics_case()
+    genes = [f"G{g}" for g in range(d.num_genes)]
+    table = api.ExpressionTable(d.exprs.T.astype(np.float64), genes, [f"p{s}" for s in range(d.num_samples)])
+    sets = {}
+    for k in range(d.num_sets):
+        mem = [genes[g] for g in d.set_genes[d.set_offsets[k]:d.set_offsets[k + 1]]]
+        sets[f"set{k}"] = mem + mem[:2] + ["NOT_A_GENE", "ALSO_MISSING"]
+    prefix = str(tmp_path / "dump")
+    res = api.GSEA(table, d.labels.tolist(), sets, d.num_perms, "twopass_signal2noise", dumpFileName=prefix)
+    es, st = api.gsea(d.exprs, d.labels, d.set_offsets, d.set_genes, d.num_perms, "twopass_signal2noise")
+    K = d.num_sets
+    np.testing.assert_array_equal(res.ES, st[:K])
+    np.testing.assert_array_equal(res.NES, st[K:2 * K])
+    np.testing.assert_array_equal(res.FWER, st[3 * K:4 * K])
+    dumped = np.fromfile(f"{prefix}_{K}_{d.num_perms}_32.es", np.float32).reshape(K, -1)
+    np.testing.assert_array_equal(dumped, es)
+    with pytest.raises(N.GseaError) as e:
+        api.GSEA(table, d.labels.tolist(), sets, 8, "no_such_metric")
+    assert e.value.status == 2
+
+
+def test_injected_launch_failure_keeps_context(gpu, monkeypatch):
+    d = synthetic.tiny()
+    plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, d.num_perms, "twopass_signal2noise")
+    plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+    monkeypatch.setenv("GSEA_FAULT", "launch")
+    with pytest.raises(N.GseaError) as e:
+        plan.execute()
+    assert e.value.status == 8
+    monkeypatch.delenv("GSEA_FAULT")
+    plan.execute()
+    es, st = plan.read()
+    es2, st2 = api.gsea(d.exprs, d.labels, d.set_offsets, d.set_genes, d.num_perms, "twopass_signal2noise")
+    np.testing.assert_array_equal(es, es2)
+
+
+def test_full_size_properties(gpu):
+    """20,000 x 200, 1,000 sets, 1,000 permutations (fp32): size-independent checks."""
+    d = synthetic.full()
+    plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, d.num_perms, "twopass_signal2noise")
+    plan.set_debug(True)
+    plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+    plan.execute()
+    es, st = plan.read()
+    assert np.isfinite(es).all() and (np.abs(es) <= 1.0 + 1e-6).all()
+    keys = plan.read_buffer(N.BUF_KEYS, np.float32, (plan.perm_batch, d.num_genes))
+    order = plan.read_buffer(N.BUF_ORDER, np.uint32, (plan.perm_batch, d.num_genes))
+    # spot-check permutations against the oracle: keys, order, ES
+    perms = [0, 1, 499, d.num_perms - 1]
+    for p in perms:
+        k1 = oracle.metric(8, d.exprs, d.labels, 1, shift=p)
+        np.testing.assert_array_equal(keys[p], k1[0])
+        sk, o = oracle.sort(k1)
+        np.testing.assert_array_equal(order[p], o[0])
+        e1 = oracle.es(sk, o, d.set_offsets, d.set_genes)
+        assert H.es_close(es[:, p], e1[:, 0], False).all()
+    np.testing.assert_array_equal(oracle.stats(es).view(np.uint8), st.view(np.uint8))
+    # a sharded plan reproduces the columns
+    tail = api.Plan(d.num_genes, d.num_samples, d.num_sets, 100, "twopass_signal2noise", perm_offset=900)
+    tail.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+    tail.execute()
+    np.testing.assert_array_equal(tail.read()[0], es[:, 900:])
