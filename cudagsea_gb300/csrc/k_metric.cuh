@@ -52,6 +52,15 @@ __device__ __forceinline__ T combine(T mA, T vA, T nA, T mB, T vB, T nB) {
     return E::div(E::sub(mA, mB), E::sqrt(E::add(E::div(wA, nA), E::div(wB, nB))));
 }
 
+// NaN keys (0/0 in the ratio metrics, log of a negative mean, ...) are
+// written as the positive all-ones NaN, whatever payload the arithmetic gave:
+// the radix order then ranks every NaN first (descending) in gene order, the
+// order CUDA's canonical NaN gets from the reference's GPU sort, on any host.
+__device__ __forceinline__ float canonical_nan(float v) { return v != v ? __uint_as_float(0x7fffffffu) : v; }
+__device__ __forceinline__ double canonical_nan(double v) {
+    return v != v ? __longlong_as_double(0x7fffffffffffffffll) : v;
+}
+
 template <int ACC, int COMB, class T, int PB>
 __global__ void __launch_bounds__(128)
 metric_kernel(const T* __restrict__ X, int G, int S, const uint32_t* __restrict__ masks, int words,
@@ -177,7 +186,7 @@ metric_kernel(const T* __restrict__ X, int G, int S, const uint32_t* __restrict_
 #pragma unroll
     for (int j = 0; j < PB; j++) {
         if (p0 + j < num_perms)
-            keys[(int64_t)(p0 + j) * G + g] = combine<T, COMB>(mA[j], vA[j], nA, mB[j], vB[j], nB);
+            keys[(int64_t)(p0 + j) * G + g] = canonical_nan(combine<T, COMB>(mA[j], vA[j], nA, mB[j], vB[j], nB));
     }
 }
 

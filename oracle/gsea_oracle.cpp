@@ -228,6 +228,20 @@ T metric_one(const MetricSpec& ms, const T* table, size_t G, size_t g, const uin
     return 0;
 }
 
+// NaN keys are written as the positive all-ones NaN: the platform's default
+// NaN differs (x86 produces a negative one, Arm and CUDA positive ones), and
+// its sign decides where NaNs rank.  Canonical NaNs rank first when
+// descending, in gene order, as CUDA's canonical NaN does in the reference's
+// GPU sort.
+inline float canonical_nan(float v) {
+    if (v == v) return v;
+    uint32_t u = 0x7fffffffu; float f; std::memcpy(&f, &u, 4); return f;
+}
+inline double canonical_nan(double v) {
+    if (v == v) return v;
+    uint64_t u = 0x7fffffffffffffffull; double f; std::memcpy(&f, &u, 8); return f;
+}
+
 template <class T>
 int metric_all(int metric, const T* table, const uint8_t* labels, size_t G, size_t S, size_t P,
                size_t shift, uint32_t seed, T* keys) {
@@ -240,7 +254,7 @@ int metric_all(int metric, const T* table, const uint8_t* labels, size_t G, size
         std::vector<uint8_t> lab(S);
         permuted_labels(labels, S, (size_t)p + shift, seed, lab.data());
         for (size_t g = 0; g < G; g++)
-            keys[(size_t)p * G + g] = metric_one<T>(ms, table, G, g, lab.data(), S, nA, nB);
+            keys[(size_t)p * G + g] = canonical_nan(metric_one<T>(ms, table, G, g, lab.data(), S, nA, nB));
     }
     return 0;
 }
