@@ -87,6 +87,7 @@ SIGNATURES = [
     ("gsea_plan_last_launches", ctypes.c_int, [_p, ctypes.POINTER(_i64)]),
     ("gsea_plan_set_profiling", ctypes.c_int, [_p, ctypes.c_int]),
     ("gsea_plan_stage_times", ctypes.c_int, [_p, ctypes.POINTER(ctypes.c_double)]),
+    ("gsea_stats_device_noalloc", ctypes.c_int, [_p, _i64, _i64, ctypes.c_int, _p, _p]),
     ("gsea_host_alloc", ctypes.c_int, [_sz, ctypes.POINTER(_p)]),
     ("gsea_host_free", ctypes.c_int, [_p]),
     ("gsea_write_es_dump", ctypes.c_int, [ctypes.c_char_p, _p, _i64, _i64, ctypes.c_int, ctypes.c_char_p, _sz]),

@@ -193,6 +193,20 @@ typedef enum {
 int gsea_plan_set_profiling(gsea_plan plan, int on);
 int gsea_plan_stage_times(gsea_plan plan, double* ms /* [GSEA_NUM_STAGES] */);
 
+/* Final statistics of a device ES matrix [K][P] into a device buffer of 5*K
+ * values, allocating no device memory at all.  No counterpart in the
+ * reference.  For hosts that cannot let a library allocate (an application
+ * that gives all device memory to its own pool, or a loop that must not call
+ * cudaMalloc/cudaFree because they can synchronise the device).  The working
+ * memory is a fixed 4 MiB array inside the library, held by every GPU that
+ * loads it; sizes whose scratch (sizeof(T)*(K+2P) + 8*(3K+8) + 256 bytes)
+ * exceeds it are rejected with GSEA_ERR_INVALID_ARGUMENT.  The first call on
+ * a device looks the array up for that device (make it before any stream
+ * capture); calls share the array, so calls that overlap on the GPU race.
+ * `stream` is a cudaStream_t (NULL = default stream); asynchronous.        */
+int gsea_stats_device_noalloc(const void* es, int64_t num_sets, int64_t num_perms, int precision,
+                              void* stats, void* stream);
+
 /* pinned (page-locked) host memory for asynchronous copies */
 int gsea_host_alloc(size_t bytes, void** ptr);
 int gsea_host_free(void* ptr);
