@@ -10,6 +10,7 @@
 //   * the statistics run on the device;
 //   * errors are returned as status codes with a per-thread message instead of
 //     exit().
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
 #include <cstdlib>
@@ -91,7 +92,11 @@ struct gsea_plan_s {
     uint8_t* labels = nullptr;
     int64_t* set_off = nullptr;
     int32_t* set_genes = nullptr;
+    int32_t* set_order = nullptr;      // sets by decreasing size, for the ES kernel
+    std::vector<int32_t> h_set_order;  // host staging of set_order
     uint32_t* masks = nullptr;
+    int* fast_ok = nullptr;            // expression values allow the packed metric form
+    void* decay = nullptr;             // [G+1] T: miss step per hit count
     void* keys = nullptr;
     void* ranks = nullptr;
     void* sorted = nullptr;
@@ -148,14 +153,17 @@ int mark(gsea_plan_s* p, int stage, cudaStream_t st) {
 }
 
 void free_plan_buffers(gsea_plan_s* p) {
-    void* bufs[] = {p->exprs, p->labels, p->set_off, p->set_genes, p->masks, p->keys, p->ranks,
-                    p->sorted, p->order, p->sort_scratch, p->es, p->stats, p->stats_scratch};
+    void* bufs[] = {p->exprs, p->labels, p->set_off, p->set_genes, p->set_order, p->masks, p->fast_ok, p->decay, p->keys,
+                    p->ranks, p->sorted, p->order, p->sort_scratch, p->es, p->stats, p->stats_scratch};
     for (void* b : bufs)
         if (b) cudaFree(b);
     p->exprs = p->labels = nullptr;
     p->set_off = nullptr;
     p->set_genes = nullptr;
+    p->set_order = nullptr;
     p->masks = nullptr;
+    p->fast_ok = nullptr;
+    p->decay = nullptr;
     p->keys = p->ranks = p->sorted = nullptr;
     p->order = nullptr;
     p->sort_scratch = p->es = p->stats = p->stats_scratch = nullptr;
@@ -199,10 +207,19 @@ int upload_sets(gsea_plan_s* p, const int64_t* off, const int32_t* genes, cudaSt
         p->nnz_cap = nnz;
     }
     p->nnz = nnz;
+    // largest sets first: the ES kernel's warps take sets in this order
+    p->h_set_order.resize((size_t)K);
+    for (int64_t k = 0; k < K; k++) p->h_set_order[k] = (int32_t)k;
+    std::stable_sort(p->h_set_order.begin(), p->h_set_order.end(),
+                     [off](int32_t x, int32_t y) { return off[x + 1] - off[x] > off[y + 1] - off[y]; });
     if (async) {
+        GSEA_CUDA(cudaMemcpyAsync(p->set_order, p->h_set_order.data(), sizeof(int32_t) * K, cudaMemcpyHostToDevice, st),
+                  "copy set order");
         GSEA_CUDA(cudaMemcpyAsync(p->set_off, off, sizeof(int64_t) * (K + 1), cudaMemcpyHostToDevice, st), "copy set offsets");
         if (nnz) GSEA_CUDA(cudaMemcpyAsync(p->set_genes, genes, sizeof(int32_t) * nnz, cudaMemcpyHostToDevice, st), "copy set genes");
     } else {
+        GSEA_CUDA(cudaMemcpy(p->set_order, p->h_set_order.data(), sizeof(int32_t) * K, cudaMemcpyHostToDevice),
+                  "copy set order");
         GSEA_CUDA(cudaMemcpy(p->set_off, off, sizeof(int64_t) * (K + 1), cudaMemcpyHostToDevice), "copy set offsets");
         if (nnz) GSEA_CUDA(cudaMemcpy(p->set_genes, genes, sizeof(int32_t) * nnz, cudaMemcpyHostToDevice), "copy set genes");
     }
@@ -219,6 +236,16 @@ int count_labels(gsea_plan_s* p, const uint8_t* labels) {
     if (a == 0 || b == 0) return fail(GSEA_ERR_INVALID_INPUT, "both classes need at least one sample");
     p->nA = a;
     p->nB = b;
+    return GSEA_OK;
+}
+
+// device-side check of the expression table (sets p->fast_ok), on `st`
+int check_inputs(gsea_plan_s* p, cudaStream_t st) {
+    const int64_t n = p->cfg.num_genes * p->cfg.num_samples;
+    cudaError_t e = p->cfg.precision == 64
+                        ? gsea::launch_finite_check<double>(static_cast<const double*>(p->exprs), n, p->fast_ok, st)
+                        : gsea::launch_finite_check<float>(static_cast<const float*>(p->exprs), n, p->fast_ok, st);
+    if (e != cudaSuccess) return cuda_fail(e, "input check kernel");
     return GSEA_OK;
 }
 
@@ -245,14 +272,15 @@ int execute_t(gsea_plan_s* p, cudaStream_t st) {
                   "permute kernel");
         if ((rc = mark(p, 0, st))) return rc;
         GSEA_CUDA(gsea::launch_metric<T>(c.metric, static_cast<const T*>(p->exprs), G, S, p->masks, p->words,
-                                         nb, p->nA, p->nB, static_cast<T*>(p->keys), st),
+                                         nb, p->nA, p->nB, static_cast<T*>(p->keys), p->fast_ok, st),
                   "metric kernel");
         if ((rc = mark(p, 1, st))) return rc;
         GSEA_CUDA(gsea::launch_sort<T>(static_cast<const T*>(p->keys), G, nb, c.ascending != 0, sb, st),
                   "sort kernel");
         if ((rc = mark(p, 2, st))) return rc;
         GSEA_CUDA(gsea::launch_es<T>(p->ranks, p->ranks16, static_cast<const T*>(p->sorted), G, nb, p->set_off,
-                                     p->set_genes, K, static_cast<T*>(p->es), P, b0, st),
+                                     p->set_genes, p->set_order, static_cast<const T*>(p->decay), K,
+                                     static_cast<T*>(p->es), P, b0, st),
                   "enrichment kernel");
         if ((rc = mark(p, 3, st))) return rc;
     }
@@ -406,7 +434,10 @@ int gsea_plan_create(const gsea_config* cfg, gsea_plan* out) {
     if ((rc = dev_alloc(&p->exprs, T * G * S, "expression table")) ||
         (rc = dev_alloc(&p->labels, (size_t)S, "labels")) ||
         (rc = dev_alloc(&p->set_off, sizeof(int64_t) * (K + 1), "set offsets")) ||
+        (rc = dev_alloc(&p->set_order, sizeof(int32_t) * K, "set order")) ||
         (rc = dev_alloc(&p->masks, 4 * (size_t)p->words * pb, "label masks")) ||
+        (rc = dev_alloc(&p->fast_ok, sizeof(int), "input flags")) ||
+        (rc = dev_alloc(&p->decay, T * ((size_t)G + 1), "decay table")) ||
         (rc = dev_alloc(&p->keys, T * (size_t)G * pb, "metric keys")) ||
         (rc = dev_alloc(&p->ranks, (p->ranks16 ? 2 : 4) * (size_t)G * pb, "ranks")) ||
         (rc = dev_alloc(&p->sorted, T * (size_t)G * pb, "sorted weights")) ||
@@ -427,6 +458,16 @@ int gsea_plan_create(const gsea_config* cfg, gsea_plan* out) {
         cudaStreamDestroy(p->stream);
         delete p;
         return rc;
+    }
+    cudaError_t de = cfg->precision == 64
+                         ? gsea::launch_decay_table<double>((int)G, static_cast<double*>(p->decay), p->stream)
+                         : gsea::launch_decay_table<float>((int)G, static_cast<float*>(p->decay), p->stream);
+    if (de == cudaSuccess) de = cudaStreamSynchronize(p->stream);
+    if (de != cudaSuccess) {
+        free_plan_buffers(p);
+        cudaStreamDestroy(p->stream);
+        delete p;
+        return cuda_fail(de, "decay table");
     }
     *out = p;
     return GSEA_OK;
@@ -454,6 +495,8 @@ int gsea_plan_set_inputs(gsea_plan p, const void* exprs, const uint8_t* labels, 
     GSEA_CUDA(cudaMemcpy(p->exprs, exprs, xbytes, cudaMemcpyHostToDevice), "copy expression table");
     GSEA_CUDA(cudaMemcpy(p->labels, labels, (size_t)p->cfg.num_samples, cudaMemcpyHostToDevice), "copy labels");
     if ((rc = upload_sets(p, set_offsets, set_genes, p->stream, false))) return rc;
+    if ((rc = check_inputs(p, p->stream))) return rc;
+    GSEA_CUDA(cudaStreamSynchronize(p->stream), "stream sync");
     p->inputs_set = true;
     return GSEA_OK;
 }
@@ -504,6 +547,7 @@ int gsea_plan_run_host(gsea_plan p, const void* exprs, const uint8_t* labels, co
     GSEA_CUDA(cudaMemcpyAsync(p->exprs, exprs, xbytes, cudaMemcpyHostToDevice, st), "copy expression table");
     GSEA_CUDA(cudaMemcpyAsync(p->labels, labels, (size_t)p->cfg.num_samples, cudaMemcpyHostToDevice, st), "copy labels");
     if ((rc = upload_sets(p, set_offsets, set_genes, st, true))) return rc;
+    if ((rc = check_inputs(p, st))) return rc;
     p->inputs_set = true;
     rc = p->cfg.precision == 64 ? execute_t<double>(p, st) : execute_t<float>(p, st);
     if (rc) return rc;

@@ -19,15 +19,26 @@
 // propagate the same way (the reference's Res stays NaN after the first NaN
 // step, and so does every later candidate here).
 //
-// Per permutation one CTA stages the gene ranks and the rank-ordered weights
-// in shared memory; a warp per set marks the members' ranks in a bitmap,
-// enumerates hits in rank order from it (each lane a contiguous word range),
-// scans hit counts and weight sums across lanes and evaluates the candidates.
-// Work per (set, permutation) is O(G/32 + n) instead of O(G).
+// Work per (set, permutation) is O(G/32 + n) instead of O(G):
+//   * one CTA per permutation stages the rank of every gene and the weight at
+//     every position in shared memory;
+//   * a warp takes the next set from a CTA-wide counter (largest sets first)
+//     and marks its members' ranks in a per-warp bitmap (duplicates collapse);
+//   * the hits are compacted into a rank-ordered list: each lane loads its
+//     own range of bitmap words into registers, a warp scan of their
+//     popcounts places each lane's hits, and the list overwrites the bitmap;
+//   * every lane then takes an equal contiguous slice of the list: it sums the
+//     slice's weights, one warp scan gives each slice its prefix and N_R, and
+//     a second walk over the slice evaluates the candidates exactly.  No lane
+//     idles while another walks a long run of hits.
+//   Sets larger than twice the bitmap's word count (or very large G) take a
+//   general path in which each lane walks its own word range.
 //
-// Rounding: the fp32 path accumulates weights as float-float pairs, so its
-// ES differ from the reference's Kahan running sum by a few ulp; the fp64
-// path is double throughout.
+// Rounding: fp32 sums are compensated (Kahan in a lane, float-float across
+// lanes), so the fp32 ES stay within a few ulp of the reference's Kahan
+// running sum; the fp64 path is double throughout.
+#include <climits>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -38,53 +49,59 @@ namespace {
 template <class T> struct Acc;
 template <> struct Acc<float> {
     float hi = 0.f, lo = 0.f;
+    // Kahan step (the running sum of one lane grows monotonically)
     __device__ __forceinline__ void add(float b) {
-        const float s = __fadd_rn(hi, b);
-        const float bb = __fsub_rn(s, hi);
-        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-        hi = s;
-        lo = __fadd_rn(lo, err);
+        const float y = __fsub_rn(b, lo);
+        const float t = __fadd_rn(hi, y);
+        lo = __fsub_rn(__fsub_rn(t, hi), y);
+        hi = t;
     }
-    __device__ __forceinline__ void add(const Acc& o) { add(o.hi); lo = __fadd_rn(lo, o.lo); }
-    __device__ __forceinline__ float scaled(float inv) const { return fmaf(hi, inv, lo * inv); }
-    __device__ __forceinline__ float total() const { return __fadd_rn(hi, lo); }
+    // merge another accumulator: two-sum of the main terms, the rounding
+    // error folded into the (negated) compensation
+    __device__ __forceinline__ void merge(const Acc& o) {
+        const float s = __fadd_rn(hi, o.hi);
+        const float bb = __fsub_rn(s, hi);
+        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(o.hi, bb));
+        hi = s;
+        lo = __fsub_rn(__fadd_rn(lo, o.lo), err);
+    }
+    __device__ __forceinline__ float value() const { return __fsub_rn(hi, lo); }
+    // (hi - lo) * inv + c, with one rounding of the product's main term
+    __device__ __forceinline__ float scaled_plus(float inv, float c) const {
+        return fmaf(hi, inv, fmaf(-lo, inv, c));
+    }
     __device__ __forceinline__ Acc shfl_up(int o) const {
         Acc r;
         r.hi = __shfl_up_sync(kFullMask, hi, o);
         r.lo = __shfl_up_sync(kFullMask, lo, o);
         return r;
     }
-    __device__ __forceinline__ Acc shfl(int src) const {
+    __device__ __forceinline__ Acc shfl_xor(int o) const {
         Acc r;
-        r.hi = __shfl_sync(kFullMask, hi, src);
-        r.lo = __shfl_sync(kFullMask, lo, src);
+        r.hi = __shfl_xor_sync(kFullMask, hi, o);
+        r.lo = __shfl_xor_sync(kFullMask, lo, o);
         return r;
     }
 };
 template <> struct Acc<double> {
-    double v = 0.0;
-    __device__ __forceinline__ void add(double b) { v += b; }
-    __device__ __forceinline__ void add(const Acc& o) { v += o.v; }
-    __device__ __forceinline__ double scaled(double inv) const { return v * inv; }
-    __device__ __forceinline__ double total() const { return v; }
+    double hi = 0.0, lo = 0.0;  // lo unused
+    __device__ __forceinline__ void add(double b) { hi += b; }
+    __device__ __forceinline__ void merge(const Acc& o) { hi += o.hi; }
+    __device__ __forceinline__ double value() const { return hi; }
+    __device__ __forceinline__ double scaled_plus(double inv, double c) const { return fma(hi, inv, c); }
     __device__ __forceinline__ Acc shfl_up(int o) const {
         Acc r;
-        r.v = __shfl_up_sync(kFullMask, v, o);
+        r.hi = __shfl_up_sync(kFullMask, hi, o);
         return r;
     }
-    __device__ __forceinline__ Acc shfl(int src) const {
+    __device__ __forceinline__ Acc shfl_xor(int o) const {
         Acc r;
-        r.v = __shfl_sync(kFullMask, v, src);
+        r.hi = __shfl_xor_sync(kFullMask, hi, o);
         return r;
     }
 };
 
-template <class T>
-__device__ __forceinline__ T fma_t(T a, T b, T c);
-template <> __device__ __forceinline__ float fma_t<float>(float a, float b, float c) { return fmaf(a, b, c); }
-template <> __device__ __forceinline__ double fma_t<double>(double a, double b, double c) { return fma(a, b, c); }
-
-// candidate (val, pos) replaces (best, bpos) when |val| > |best| or equal
+// candidate (val, pos) replaces (best, bpos) when |val| > |best|, or equal
 // magnitude at an earlier position; NaN never replaces
 template <class T>
 __device__ __forceinline__ void consider(T val, int pos, T& best, int& bpos) {
@@ -95,166 +112,375 @@ __device__ __forceinline__ void consider(T val, int pos, T& best, int& bpos) {
     }
 }
 
-template <class T, class RankT, int WARPS, bool STAGE>
+// ---------------------------------------------------------------------------
+// Per-set procedures.  Both run on one warp with the set's member ranks marked
+// in the warp's bitmap `bm` (G bits) and leave the bitmap all zero.
+
+// Fast procedure: the lane's bitmap words (at most WPL, a multiple of 4,
+// loaded as 16-byte vectors) are held in registers, the hits are compacted
+// into a rank-ordered list of positions that overwrites the start of the
+// bitmap (needs n <= 2*words), then every lane processes an equal contiguous
+// slice of the list -- no lane waits for another's hits.  The slice length is
+// odd so that the lanes' list reads fall into different banks; the first
+// CACHE weights of a slice stay in registers between the two walks.
+// `w0` = lane*WPL: the lane's first word, 16-byte aligned inside the warp's
+// region of WPL*32 words (bits at positions >= G are never set).
+template <class T, int WPL, int CACHE>
+__device__ __forceinline__ T set_score_list(uint32_t* bm, int w0, const T* wt, const T* __restrict__ decay, int G,
+                                            int lane) {
+    uint32_t wr[WPL];
+    int cnt = 0;
+#pragma unroll
+    for (int i = 0; i < WPL; i += 4) {
+        const uint4 v = *reinterpret_cast<const uint4*>(bm + w0 + i);  // words padded to WPL*32
+        wr[i] = v.x; wr[i + 1] = v.y; wr[i + 2] = v.z; wr[i + 3] = v.w;
+        cnt += __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
+    }
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(kFullMask, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const int n = __shfl_sync(kFullMask, incl, 31);
+    __syncwarp();  // every lane holds its words: the bitmap may be overwritten
+#pragma unroll
+    for (int i = 0; i < WPL; i += 4) {
+        if (wr[i] | wr[i + 1] | wr[i + 2] | wr[i + 3])
+            *reinterpret_cast<uint4*>(bm + w0 + i) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    __syncwarp();
+    uint16_t* list = reinterpret_cast<uint16_t*>(bm);
+    int j = incl - cnt;
+#pragma unroll
+    for (int i = 0; i < WPL; i++) {
+        uint32_t word = wr[i];
+        while (word) {
+            const int bit = __ffs(word) - 1;
+            word &= word - 1;
+            list[j++] = (uint16_t)(((w0 + i) << 5) + bit);
+        }
+    }
+    __syncwarp();
+    // balanced slices of the rank-ordered hit list
+    int per = (n + 31) >> 5;
+    per |= 1;
+    const int j0 = min(n, lane * per), j1 = min(n, j0 + per);
+    Acc<T> Wl;
+    T wc[CACHE];
+#pragma unroll
+    for (int c = 0; c < CACHE; c++) {
+        wc[c] = j0 + c < j1 ? wt[list[j0 + c]] : T(0);
+        if (j0 + c < j1) Wl.add(wc[c]);
+    }
+    for (int k = j0 + CACHE; k < j1; k++) Wl.add(wt[list[k]]);
+    Acc<T> W_incl = Wl;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const Acc<T> y = W_incl.shfl_up(o);
+        if (lane >= o) W_incl.merge(y);
+    }
+    Acc<T> W = W_incl.shfl_up(1);  // weight of the hits before this slice
+    if (lane == 0) W = Acc<T>();
+    Acc<T> Wt;                      // weight of all hits
+    Wt.hi = __shfl_sync(kFullMask, W_incl.hi, 31);
+    Wt.lo = __shfl_sync(kFullMask, W_incl.lo, 31);
+    const T N_R = Wt.value();
+    const T inv = n > 0 ? T(1) / N_R : T(0);
+    const T d = decay[n];
+    // The largest value is always just after a hit and the smallest just
+    // before one (or at the end): track the two separately.
+    T mx = T(0), mn = T(0);
+    int pmx = -1, pmn = -1;
+#pragma unroll
+    for (int c = 0; c < CACHE; c++) {
+        const int k = j0 + c;
+        if (k < j1) {
+            const int r = list[k];
+            const T md = -(T)(r - k) * d;  // misses before hit k, times the decay
+            const T before = k > 0 ? W.scaled_plus(inv, md) : md;
+            W.add(wc[c]);
+            const T after = W.scaled_plus(inv, md);
+            if (before < mn) { mn = before; pmn = r - 1; }
+            if (after > mx) { mx = after; pmx = r; }
+        }
+    }
+    for (int k = j0 + CACHE; k < j1; k++) {
+        const int r = list[k];
+        const T md = -(T)(r - k) * d;
+        const T before = k > 0 ? W.scaled_plus(inv, md) : md;
+        W.add(wt[r]);
+        const T after = W.scaled_plus(inv, md);
+        if (before < mn) { mn = before; pmn = r - 1; }
+        if (after > mx) { mx = after; pmx = r; }
+    }
+    if (lane == 31) {  // end of the list, after the trailing misses
+        const T tail = -(T)(G - n) * d;
+        const T end = n > 0 ? Wt.scaled_plus(inv, tail) : tail;
+        if (end < mn) { mn = end; pmn = G - 1; }
+    }
+    T best = T(0);
+    int bpos = -1;
+    if (pmx >= 0) consider<T>(mx, pmx, best, bpos);
+    if (mn < T(0)) consider<T>(mn, pmn, best, bpos);
+    __syncwarp();
+    for (int k = lane; k < (n + 1) / 2; k += 32) bm[k] = 0u;  // the list's words
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        const T ob = __shfl_xor_sync(kFullMask, best, o);
+        const int op = __shfl_xor_sync(kFullMask, bpos, o);
+        consider<T>(ob, op, best, bpos);
+    }
+    return best;
+}
+
+// General procedure (any G, any set size): each lane walks its own word range
+// twice -- weights first, then candidates with the exact prefix from a scan.
+template <class T>
+__device__ __noinline__ T set_score_walk(uint32_t* bm, int w0, int w1, const T* wt, const T* __restrict__ decay,
+                                         int G, int lane) {
+    int h = 0;
+    Acc<T> Wl;
+    for (int w = w0; w < w1; w++) {
+        uint32_t word = bm[w];
+        h += __popc(word);
+        while (word) {
+            const int bit = __ffs(word) - 1;
+            word &= word - 1;
+            Wl.add(wt[(w << 5) + bit]);
+        }
+    }
+    int h_incl = h;
+    Acc<T> W_incl = Wl;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int hy = __shfl_up_sync(kFullMask, h_incl, o);
+        const Acc<T> wy = W_incl.shfl_up(o);
+        if (lane >= o) {
+            h_incl += hy;
+            W_incl.merge(wy);
+        }
+    }
+    const int n = __shfl_sync(kFullMask, h_incl, 31);
+    Acc<T> Wt;
+    Wt.hi = __shfl_sync(kFullMask, W_incl.hi, 31);
+    Wt.lo = __shfl_sync(kFullMask, W_incl.lo, 31);
+    const T N_R = Wt.value();
+    const T inv = n > 0 ? T(1) / N_R : T(0);
+    const T d = decay[n];
+    Acc<T> W = W_incl.shfl_up(1);
+    if (lane == 0) W = Acc<T>();
+    int j = h_incl - h;
+    T best = T(0);
+    int bpos = -1;
+    for (int w = w0; w < w1; w++) {
+        uint32_t word = bm[w];
+        if (!word) continue;
+        bm[w] = 0u;
+        while (word) {
+            const int bit = __ffs(word) - 1;
+            word &= word - 1;
+            const int r = (w << 5) + bit;
+            const T m = (T)(r - j);
+            const T before = j > 0 ? W.scaled_plus(inv, -m * d) : -m * d;
+            consider<T>(before, r - 1, best, bpos);
+            W.add(wt[r]);
+            j++;
+            consider<T>(W.scaled_plus(inv, -m * d), r, best, bpos);
+        }
+    }
+    if (lane == 31) {
+        const T tail = -(T)(G - n) * d;
+        consider<T>(n > 0 ? Wt.scaled_plus(inv, tail) : tail, G - 1, best, bpos);
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        const T ob = __shfl_xor_sync(kFullMask, best, o);
+        const int op = __shfl_xor_sync(kFullMask, bpos, o);
+        consider<T>(ob, op, best, bpos);
+    }
+    return best;
+}
+
+// WPL > 0: bitmap words per lane held in registers by the list procedure
+// (G <= 1024*WPL, ranks < 65536); WPL == 0: general procedure only.
+template <class T, class RankT, int WARPS, bool STAGE, int WPL>
 __global__ void __launch_bounds__(WARPS * 32)
 es_kernel(const RankT* __restrict__ ranks, const T* __restrict__ sorted_abs, int G, int num_perms,
-          const int64_t* __restrict__ set_off, const int32_t* __restrict__ set_genes, int K,
-          T* __restrict__ es, int64_t es_stride, int64_t col0) {
+          const int64_t* __restrict__ set_off, const int32_t* __restrict__ set_genes,
+          const int32_t* __restrict__ set_order, const T* __restrict__ decay, int K, T* __restrict__ es,
+          int64_t es_stride, int64_t col0) {
     extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int next_set;
     const int words = (G + 31) >> 5;
+    // per-warp bitmap region: WPL*32 words for the register procedure
+    const int region = WPL > 0 ? WPL * 32 : words;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    // layout: [T w[G]] [RankT rank[G]] (when staged), then per-warp bitmaps
     T* s_w = reinterpret_cast<T*>(smem);
     RankT* s_rank = reinterpret_cast<RankT*>(smem + (STAGE ? sizeof(T) * (size_t)G : 0));
     size_t bm_off = STAGE ? (sizeof(T) + sizeof(RankT)) * (size_t)G : 0;
     bm_off = (bm_off + 15) & ~(size_t)15;
-    uint32_t* bm = reinterpret_cast<uint32_t*>(smem + bm_off) + (size_t)warp * words;
-    for (int w = lane; w < words; w += 32) bm[w] = 0u;
+    uint32_t* bm = reinterpret_cast<uint32_t*>(smem + bm_off) + (size_t)warp * region;
+    for (int w = lane; w < region; w += 32) bm[w] = 0u;
 
-    const int wpl = (words + 31) >> 5;  // words per lane
+    const int wpl = WPL > 0 ? WPL : (words + 31) >> 5;  // bitmap words per lane
     const int w0 = min(lane * wpl, words), w1 = min(w0 + wpl, words);
 
     for (int p = blockIdx.x; p < num_perms; p += gridDim.x) {
         const RankT* rk = ranks + (int64_t)p * G;
         const T* wt = sorted_abs + (int64_t)p * G;
+        __syncthreads();  // previous permutation finished with the staging and the counter
+        if (tid == 0) next_set = 0;
         if (STAGE) {
-            __syncthreads();
             for (int i = tid; i < G; i += WARPS * 32) {
                 s_w[i] = wt[i];
                 s_rank[i] = rk[i];
             }
-            __syncthreads();
             rk = s_rank;
             wt = s_w;
         }
-        for (int k = warp; k < K; k += WARPS) {
+        __syncthreads();
+        while (true) {
+            int slot = 0;
+            if (lane == 0) slot = atomicAdd(&next_set, 1);
+            slot = __shfl_sync(kFullMask, slot, 0);
+            if (slot >= K) break;
+            const int k = set_order ? set_order[slot] : slot;
             const int64_t a = set_off[k], b = set_off[k + 1];
-            // A: mark member ranks
-            for (int64_t i = a + lane; i < b; i += 32) {
-                const int g = set_genes[i];
-                if (g >= 0 && g < G) {
-                    const uint32_t r = (uint32_t)rk[g];
-                    atomicOr(&bm[r >> 5], 1u << (r & 31));
+            // mark the members' ranks (duplicates and unknown ids fall away)
+            for (int64_t base = a; base < b; base += 128) {
+                int g[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const int64_t idx = base + lane + 32 * i;
+                    g[i] = idx < b ? __ldg(set_genes + idx) : -1;
+                }
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    if (g[i] >= 0 && g[i] < G) {
+                        const uint32_t r = (uint32_t)rk[g[i]];
+                        atomicOr(&bm[r >> 5], 1u << (r & 31));
+                    }
                 }
             }
             __syncwarp();
-            // B: hits and weight sums of this lane's word range
-            int h = 0;
-            Acc<T> W;
-            for (int w = w0; w < w1; w++) {
-                uint32_t word = bm[w];
-                h += __popc(word);
-                while (word) {
-                    const int bit = __ffs(word) - 1;
-                    word &= word - 1;
-                    W.add(wt[(w << 5) + bit]);
-                }
-            }
-            // C: exclusive scans across lanes
-            int h_incl = h;
-            Acc<T> W_incl = W;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int hy = __shfl_up_sync(kFullMask, h_incl, o);
-                const Acc<T> wy = W_incl.shfl_up(o);
-                if (lane >= o) {
-                    h_incl += hy;
-                    W_incl.add(wy);
-                }
-            }
-            const int n_hits = __shfl_sync(kFullMask, h_incl, 31);
-            const Acc<T> W_tot = W_incl.shfl(31);
-            int j = h_incl - h;               // hits before this lane's range
-            Acc<T> Wr = W_incl.shfl_up(1);    // weight before this lane's range
-            if (lane == 0) Wr = Acc<T>();
-            const T N_R = W_tot.total();
-            const T inv = n_hits > 0 ? T(1) / N_R : T(0);
-            const T d = n_hits < G ? (T)(1.0 / (double)(G - n_hits)) : T(0);
-            // D: candidates in rank order
-            T best = T(0);
-            int bpos = -1;
-            for (int w = w0; w < w1; w++) {
-                uint32_t word = bm[w];
-                if (word) bm[w] = 0u;
-                while (word) {
-                    const int bit = __ffs(word) - 1;
-                    word &= word - 1;
-                    const int r = (w << 5) + bit;
-                    const T miss = (T)(r - j);
-                    const T hit_before = j > 0 ? Wr.scaled(inv) : T(0);
-                    consider<T>(fma_t<T>(-miss, d, hit_before), r - 1, best, bpos);
-                    Wr.add(wt[r]);
-                    j++;
-                    consider<T>(fma_t<T>(-miss, d, Wr.scaled(inv)), r, best, bpos);
-                }
-            }
-            if (lane == 31) {
-                const T hits_end = n_hits > 0 ? W_tot.scaled(inv) : T(0);
-                consider<T>(fma_t<T>(-(T)(G - n_hits), d, hits_end), G - 1, best, bpos);
-            }
-            // E: reduce (largest magnitude, earliest position)
-#pragma unroll
-            for (int o = 16; o >= 1; o >>= 1) {
-                const T ob = __shfl_xor_sync(kFullMask, best, o);
-                const int op = __shfl_xor_sync(kFullMask, bpos, o);
-                consider<T>(ob, op, best, bpos);
-            }
-            if (lane == 0) es[(int64_t)k * es_stride + col0 + p] = best;
+            T score;
+            if (WPL > 0 && b - a <= 2 * (int64_t)words)  // the list fits in the bitmap region
+                score = set_score_list<T, (WPL > 0 ? WPL : 4), (sizeof(T) == 4 ? 10 : 6)>(bm, lane * WPL, wt, decay,
+                                                                                        G, lane);
+            else
+                score = set_score_walk<T>(bm, w0, w1, wt, decay, G, lane);
+            if (lane == 0) es[(int64_t)k * es_stride + col0 + p] = score;
             __syncwarp();
         }
     }
 }
 
-constexpr int kWarps32 = 16;
-constexpr int kWarps64 = 8;
+// words of a warp's bitmap region: WPL*32 for the register procedure
+inline int es_region_words(int G, int wpl) { return wpl > 0 ? wpl * 32 : (G + 31) >> 5; }
 
-template <class T, class RankT, int WARPS>
+inline int es_wpl(int G, bool ranks16) {
+    const int need = (((G + 31) >> 5) + 31) >> 5;
+    if (!ranks16) return 0;
+    for (int w : {4, 8, 12, 16, 20})
+        if (need <= w) return w;
+    return 0;
+}
+
+template <class T, class RankT, int WARPS, bool STAGE>
+size_t es_smem_bytes(int G) {
+    const int region = es_region_words(G, es_wpl(G, sizeof(RankT) == 2));
+    size_t s = STAGE ? (((sizeof(T) + sizeof(RankT)) * (size_t)G + 15) & ~(size_t)15) : 0;
+    return s + sizeof(uint32_t) * (size_t)region * WARPS;
+}
+
+template <class T, class RankT, int WARPS, bool STAGE, int WPL>
+cudaError_t launch_es_v(const RankT* ranks, const T* sorted_abs, int G, int P, const int64_t* off,
+                        const int32_t* genes, const int32_t* order, const T* decay, int K, T* es, int64_t stride,
+                        int64_t col0, int grid, cudaStream_t st) {
+    const size_t smem = es_smem_bytes<T, RankT, WARPS, STAGE>(G);
+    auto kern = es_kernel<T, RankT, WARPS, STAGE, WPL>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, WARPS * 32, smem, st>>>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0);
+    launches_add(1);
+    return cudaGetLastError();
+}
+
+template <class T, class RankT, int WARPS, bool STAGE>
+cudaError_t launch_es_w(const RankT* ranks, const T* sorted_abs, int G, int P, const int64_t* off,
+                        const int32_t* genes, const int32_t* order, const T* decay, int K, T* es, int64_t stride,
+                        int64_t col0, int grid, cudaStream_t st) {
+    // words per lane for the register-resident list procedure (u16 positions)
+    switch (es_wpl(G, sizeof(RankT) == 2)) {
+        case 4: return launch_es_v<T, RankT, WARPS, STAGE, 4>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+        case 8: return launch_es_v<T, RankT, WARPS, STAGE, 8>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+        case 12: return launch_es_v<T, RankT, WARPS, STAGE, 12>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+        case 16: return launch_es_v<T, RankT, WARPS, STAGE, 16>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+        case 20: return launch_es_v<T, RankT, WARPS, STAGE, 20>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+        default: break;
+    }
+    return launch_es_v<T, RankT, WARPS, STAGE, 0>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+}
+
+template <class T, class RankT>
 cudaError_t launch_es_t(const RankT* ranks, const T* sorted_abs, int G, int P, const int64_t* off,
-                        const int32_t* genes, int K, T* es, int64_t stride, int64_t col0,
-                        cudaStream_t st) {
+                        const int32_t* genes, const int32_t* order, const T* decay, int K, T* es, int64_t stride,
+                        int64_t col0, cudaStream_t st) {
     int dev = 0, max_smem = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int words = (G + 31) >> 5;
-    const size_t bm_bytes = sizeof(uint32_t) * (size_t)words * WARPS;
-    size_t staged = (((sizeof(T) + sizeof(RankT)) * (size_t)G + 15) & ~(size_t)15) + bm_bytes;
-    const int grid = P < 2 * sms ? P : 2 * sms;
-    if (staged <= (size_t)max_smem) {
-        auto kern = es_kernel<T, RankT, WARPS, true>;
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)staged);
-        if (e != cudaSuccess) return e;
-        kern<<<grid, WARPS * 32, staged, st>>>(ranks, sorted_abs, G, P, off, genes, K, es, stride, col0);
-    } else {
-        if (bm_bytes > (size_t)max_smem) return cudaErrorInvalidValue;
-        auto kern = es_kernel<T, RankT, WARPS, false>;
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bm_bytes);
-        if (e != cudaSuccess) return e;
-        kern<<<grid, WARPS * 32, bm_bytes, st>>>(ranks, sorted_abs, G, P, off, genes, K, es, stride, col0);
-    }
-    launches_add(1);
-    return cudaGetLastError();
+    const size_t cap = (size_t)max_smem - 64;  // static shared counter
+    const int grid = P < sms ? P : sms;
+    if (es_smem_bytes<T, RankT, 32, true>(G) <= cap)
+        return launch_es_w<T, RankT, 32, true>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+    if (es_smem_bytes<T, RankT, 16, true>(G) <= cap)
+        return launch_es_w<T, RankT, 16, true>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+    if (es_smem_bytes<T, RankT, 8, true>(G) <= cap)
+        return launch_es_w<T, RankT, 8, true>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+    if (es_smem_bytes<T, RankT, 32, false>(G) <= cap)
+        return launch_es_w<T, RankT, 32, false>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+    if (es_smem_bytes<T, RankT, 8, false>(G) <= cap)
+        return launch_es_w<T, RankT, 8, false>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace
 
 template <class T>
 cudaError_t launch_es(const void* ranks, bool ranks16, const T* sorted_abs, int G, int num_perms,
-                      const int64_t* set_offsets, const int32_t* set_genes, int K, T* es,
-                      int64_t es_stride, int64_t perm_col0, cudaStream_t st) {
+                      const int64_t* set_offsets, const int32_t* set_genes, const int32_t* set_order,
+                      const T* decay, int K, T* es, int64_t es_stride, int64_t perm_col0, cudaStream_t st) {
     if (num_perms <= 0 || K <= 0) return cudaSuccess;
-    constexpr int WARPS = sizeof(T) == 4 ? kWarps32 : kWarps64;
     if (ranks16)
-        return launch_es_t<T, uint16_t, WARPS>(static_cast<const uint16_t*>(ranks), sorted_abs, G,
-                                               num_perms, set_offsets, set_genes, K, es, es_stride,
-                                               perm_col0, st);
-    return launch_es_t<T, uint32_t, WARPS>(static_cast<const uint32_t*>(ranks), sorted_abs, G,
-                                           num_perms, set_offsets, set_genes, K, es, es_stride,
-                                           perm_col0, st);
+        return launch_es_t<T, uint16_t>(static_cast<const uint16_t*>(ranks), sorted_abs, G, num_perms, set_offsets,
+                                        set_genes, set_order, decay, K, es, es_stride, perm_col0, st);
+    return launch_es_t<T, uint32_t>(static_cast<const uint32_t*>(ranks), sorted_abs, G, num_perms, set_offsets,
+                                    set_genes, set_order, decay, K, es, es_stride, perm_col0, st);
 }
-template cudaError_t launch_es<float>(const void*, bool, const float*, int, int, const int64_t*,
-                                      const int32_t*, int, float*, int64_t, int64_t, cudaStream_t);
-template cudaError_t launch_es<double>(const void*, bool, const double*, int, int, const int64_t*,
-                                       const int32_t*, int, double*, int64_t, int64_t, cudaStream_t);
+
+// decay[n] = (T)(1.0 / (G - n)) for n < G, 0 for n = G: the miss step of a
+// set with n hits, rounded from double as the reference does
+// (enrichment_scores.cuh:178)
+template <class T>
+__global__ void decay_table_kernel(int G, T* decay) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n <= G) decay[n] = n < G ? (T)(1.0 / (double)(G - n)) : T(0);
+}
+
+template <class T>
+cudaError_t launch_decay_table(int G, T* decay, cudaStream_t st) {
+    decay_table_kernel<T><<<(G + 256) / 256, 256, 0, st>>>(G, decay);
+    launches_add(1);
+    return cudaGetLastError();
+}
+template cudaError_t launch_decay_table<float>(int, float*, cudaStream_t);
+template cudaError_t launch_decay_table<double>(int, double*, cudaStream_t);
+
+template cudaError_t launch_es<float>(const void*, bool, const float*, int, int, const int64_t*, const int32_t*,
+                                      const int32_t*, const float*, int, float*, int64_t, int64_t, cudaStream_t);
+template cudaError_t launch_es<double>(const void*, bool, const double*, int, int, const int64_t*, const int32_t*,
+                                       const int32_t*, const double*, int, double*, int64_t, int64_t, cudaStream_t);
 
 }  // namespace gsea

@@ -21,6 +21,8 @@
 // permutation is a warp-uniform bit of a shared-memory mask word, so the
 // class selection never diverges.
 #pragma once
+#include <type_traits>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -61,20 +63,14 @@ __device__ __forceinline__ double canonical_nan(double v) {
     return v != v ? __longlong_as_double(0x7fffffffffffffffll) : v;
 }
 
+// Exact, predicated form: every class update is a conditional operation, as
+// in the reference, so it is bit-exact for any input including inf / NaN.
+// Called by one thread per gene with the block's masks in shared memory.
 template <int ACC, int COMB, class T, int PB>
-__global__ void __launch_bounds__(128)
-metric_kernel(const T* __restrict__ X, int G, int S, const uint32_t* __restrict__ masks, int words,
-              int num_perms, T nA, T nB, T* __restrict__ keys) {
+__device__ __forceinline__ void metric_exact(const T* __restrict__ X, int G, int S, const uint32_t* sm_masks,
+                                             int words, int num_perms, int p0, T nA, T nB, T* __restrict__ keys,
+                                             int g) {
     using E = Exact<T>;
-    extern __shared__ uint32_t sm_masks[];  // [PB][words]
-    const int p0 = blockIdx.y * PB;
-    for (int i = threadIdx.x; i < PB * words; i += blockDim.x) {
-        const int j = i / words, w = i - j * words;
-        sm_masks[i] = (p0 + j < num_perms) ? masks[(int64_t)(p0 + j) * words + w] : 0u;
-    }
-    __syncthreads();
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= G) return;
     const T* xg = X + g;
 
     T mA[PB], mB[PB], vA[PB], vB[PB], cA[PB], cB[PB];
@@ -190,6 +186,202 @@ metric_kernel(const T* __restrict__ X, int G, int S, const uint32_t* __restrict_
     }
 }
 
+template <int ACC, int COMB, class T, int PB>
+__global__ void __launch_bounds__(128)
+metric_kernel(const T* __restrict__ X, int G, int S, const uint32_t* __restrict__ masks, int words,
+              int num_perms, T nA, T nB, T* __restrict__ keys) {
+    extern __shared__ uint32_t sm_masks[];  // [PB][words]
+    const int p0 = blockIdx.y * PB;
+    for (int i = threadIdx.x; i < PB * words; i += blockDim.x) {
+        const int j = i / words, w = i - j * words;
+        sm_masks[i] = (p0 + j < num_perms) ? masks[(int64_t)(p0 + j) * words + w] : 0u;
+    }
+    __syncthreads();
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= G) return;
+    metric_exact<ACC, COMB, T, PB>(X, G, S, sm_masks, words, num_perms, p0, nA, nB, keys, g);
+}
+
+// ---------------------------------------------------------------------------
+// Packed fast form (fp32, naive / onepass / twopass accumulators).
+//
+// With a class weight l in {0, 1}, fma(l, v, acc) rounds exactly like the
+// reference's conditional `acc + v` when v is finite (l = 1: one rounding of
+// acc + v; l = 0: acc unchanged), and the naive accumulator's literal
+// `acc + l*v` for any v.  Blackwell's paired-FP32 instructions (fma / add /
+// mul .rn.f32x2) then update two permutations per instruction with no
+// predication: pass 1 is one packed FMA per class and permutation pair, pass 2
+// selects the class mean as lA*mA + lB*mB (exact: one product is zero) and
+// adds the squared deviation with the class weights.  The expression table is
+// checked once per upload (gsea::launch_finite_check): any value that is not
+// finite or has |x| >= 2^60 (whose square could overflow) sends the kernel to
+// the exact predicated form instead.
+__device__ __forceinline__ unsigned long long f2_pack(float a, float b) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(unsigned long long v, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b, unsigned long long c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b) {
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ unsigned long long f2_mul(unsigned long long a, unsigned long long b) {
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
+template <int ACC, int COMB, int PB>
+__global__ void __launch_bounds__(128, 8)
+metric_fast_kernel(const float* __restrict__ X, int G, int S, const uint32_t* __restrict__ masks, int words,
+                   int num_perms, float nA, float nB, float* __restrict__ keys, const int* __restrict__ fast_ok) {
+    static_assert(PB % 2 == 0, "permutations are processed in pairs");
+    constexpr int PAIRS = PB / 2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ulonglong2* lab = reinterpret_cast<ulonglong2*>(smem_raw);                       // [S][PAIRS]
+    uint32_t* sm_masks = reinterpret_cast<uint32_t*>(lab + (size_t)S * PAIRS);        // [PB][words]
+    const int p0 = blockIdx.y * PB;
+    for (int i = threadIdx.x; i < PB * words; i += blockDim.x) {
+        const int j = i / words, w = i - j * words;
+        sm_masks[i] = (p0 + j < num_perms) ? masks[(int64_t)(p0 + j) * words + w] : 0u;
+    }
+    __syncthreads();
+    const bool fast = ACC == ACC_NAIVE || *fast_ok != 0;
+    if (fast) {
+        for (int i = threadIdx.x; i < S * PAIRS; i += blockDim.x) {
+            const int sidx = i / PAIRS, q = i - sidx * PAIRS;
+            const int w = sidx >> 5, t = sidx & 31;
+            const float a0 = (float)((sm_masks[(2 * q) * words + w] >> t) & 1u);
+            const float a1 = (float)((sm_masks[(2 * q + 1) * words + w] >> t) & 1u);
+            lab[i] = make_ulonglong2(f2_pack(a0, a1), f2_pack(1.f - a0, 1.f - a1));
+        }
+    }
+    __syncthreads();
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= G) return;
+    if (!fast) {
+        metric_exact<ACC, COMB, float, PB>(X, G, S, sm_masks, words, num_perms, p0, nA, nB, keys, g);
+        return;
+    }
+    const float* xg = X + g;
+    unsigned long long mA[PAIRS], mB[PAIRS], vA[PAIRS], vB[PAIRS];
+#pragma unroll
+    for (int q = 0; q < PAIRS; q++) mA[q] = mB[q] = vA[q] = vB[q] = 0ull;
+    // pass 1: class sums (and sums of squares for onepass)
+#pragma unroll 2
+    for (int sidx = 0; sidx < S; sidx++) {
+        const float x = __ldg(xg + (int64_t)sidx * G);
+        const unsigned long long xx = f2_pack(x, x);
+        unsigned long long sq = 0ull;
+        if (ACC == ACC_ONEPASS) {
+            const float x2 = __fmul_rn(x, x);
+            sq = f2_pack(x2, x2);
+        }
+        const ulonglong2* ls = lab + (size_t)sidx * PAIRS;
+#pragma unroll
+        for (int q = 0; q < PAIRS; q++) {
+            const ulonglong2 l = ls[q];
+            mA[q] = f2_fma(l.x, xx, mA[q]);
+            mB[q] = f2_fma(l.y, xx, mB[q]);
+            if (ACC == ACC_ONEPASS) {
+                vA[q] = f2_fma(l.x, sq, vA[q]);
+                vB[q] = f2_fma(l.y, sq, vB[q]);
+            }
+        }
+    }
+    float fmA[PB], fmB[PB];
+#pragma unroll
+    for (int q = 0; q < PAIRS; q++) {
+        f2_unpack(mA[q], fmA[2 * q], fmA[2 * q + 1]);
+        f2_unpack(mB[q], fmB[2 * q], fmB[2 * q + 1]);
+    }
+#pragma unroll
+    for (int j = 0; j < PB; j++) {
+        fmA[j] = __fdiv_rn(fmA[j], nA);
+        fmB[j] = __fdiv_rn(fmB[j], nB);
+    }
+    float fvA[PB], fvB[PB];
+#pragma unroll
+    for (int j = 0; j < PB; j++) fvA[j] = fvB[j] = 0.f;
+    if (ACC == ACC_ONEPASS) {
+#pragma unroll
+        for (int q = 0; q < PAIRS; q++) {
+            f2_unpack(vA[q], fvA[2 * q], fvA[2 * q + 1]);
+            f2_unpack(vB[q], fvB[2 * q], fvB[2 * q + 1]);
+        }
+#pragma unroll
+        for (int j = 0; j < PB; j++) {
+            fvA[j] = __fsub_rn(__fdiv_rn(fvA[j], nA), __fmul_rn(fmA[j], fmA[j]));
+            fvB[j] = __fsub_rn(__fdiv_rn(fvB[j], nB), __fmul_rn(fmB[j], fmB[j]));
+        }
+    }
+    if (ACC == ACC_TWOPASS) {
+        // pass 2: squared deviations from the own class mean
+#pragma unroll
+        for (int q = 0; q < PAIRS; q++) {
+            mA[q] = f2_pack(fmA[2 * q], fmA[2 * q + 1]);
+            mB[q] = f2_pack(fmB[2 * q], fmB[2 * q + 1]);
+        }
+#pragma unroll 2
+        for (int sidx = 0; sidx < S; sidx++) {
+            const float x = __ldg(xg + (int64_t)sidx * G);
+            const unsigned long long xx = f2_pack(x, x);
+            const ulonglong2* ls = lab + (size_t)sidx * PAIRS;
+#pragma unroll
+            for (int q = 0; q < PAIRS; q++) {
+                const ulonglong2 l = ls[q];
+                const unsigned long long m = f2_fma(l.x, mA[q], f2_mul(l.y, mB[q]));  // own class mean
+                const unsigned long long dv = f2_sub(xx, m);
+                const unsigned long long dd = f2_mul(dv, dv);
+                vA[q] = f2_fma(l.x, dd, vA[q]);
+                vB[q] = f2_fma(l.y, dd, vB[q]);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < PAIRS; q++) {
+            f2_unpack(vA[q], fvA[2 * q], fvA[2 * q + 1]);
+            f2_unpack(vB[q], fvB[2 * q], fvB[2 * q + 1]);
+        }
+#pragma unroll
+        for (int j = 0; j < PB; j++) {
+            fvA[j] = __fdiv_rn(fvA[j], nA);
+            fvB[j] = __fdiv_rn(fvB[j], nB);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < PB; j++) {
+        if (p0 + j < num_perms)
+            keys[(int64_t)(p0 + j) * G + g] =
+                canonical_nan(combine<float, COMB>(fmA[j], fvA[j], nA, fmB[j], fvB[j], nB));
+    }
+}
+
+template <int ACC, int COMB>
+cudaError_t launch_metric_fast(const float* X, int G, int S, const uint32_t* masks, int words, int num_perms,
+                               int64_t nA, int64_t nB, float* keys, const int* fast_ok, cudaStream_t st) {
+    constexpr int PB = 8;
+    const int threads = 128;
+    dim3 grid((G + threads - 1) / threads, (num_perms + PB - 1) / PB);
+    const size_t smem = sizeof(ulonglong2) * (size_t)S * (PB / 2) + sizeof(uint32_t) * PB * words;
+    auto kern = metric_fast_kernel<ACC, COMB, PB>;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    kern<<<grid, threads, smem, st>>>(X, G, S, masks, words, num_perms, (float)nA, (float)nB, keys, fast_ok);
+    launches_add(1);
+    return cudaGetLastError();
+}
+
 template <int ACC, int COMB, class T>
 cudaError_t launch_metric_t(const T* X, int G, int S, const uint32_t* masks, int words,
                             int num_perms, int64_t nA, int64_t nB, T* keys, cudaStream_t st) {
@@ -206,8 +398,24 @@ cudaError_t launch_metric_t(const T* X, int G, int S, const uint32_t* masks, int
 template <class T>
 cudaError_t launch_metric_impl(int metric, const T* X, int G, int S, const uint32_t* masks,
                                int words, int num_perms, int64_t nA, int64_t nB, T* keys,
-                               cudaStream_t st) {
+                               const int* fast_ok, cudaStream_t st) {
     if (num_perms <= 0) return cudaSuccess;
+    if constexpr (std::is_same<T, float>::value) {
+      if (fast_ok && (size_t)S * 4 * 16 + 32 * (size_t)words <= 100 * 1024) {
+        const float* Xf = X;
+        float* kf = keys;
+        switch (metric) {
+            case 0: return launch_metric_fast<ACC_NAIVE, COMB_DIFF>(Xf, G, S, masks, words, num_perms, nA, nB, kf, fast_ok, st);
+            case 1: return launch_metric_fast<ACC_NAIVE, COMB_RATIO>(Xf, G, S, masks, words, num_perms, nA, nB, kf, fast_ok, st);
+            case 2: return launch_metric_fast<ACC_NAIVE, COMB_LOG2>(Xf, G, S, masks, words, num_perms, nA, nB, kf, fast_ok, st);
+            case 6: return launch_metric_fast<ACC_ONEPASS, COMB_S2N>(Xf, G, S, masks, words, num_perms, nA, nB, kf, fast_ok, st);
+            case 7: return launch_metric_fast<ACC_ONEPASS, COMB_TTEST>(Xf, G, S, masks, words, num_perms, nA, nB, kf, fast_ok, st);
+            case 8: return launch_metric_fast<ACC_TWOPASS, COMB_S2N>(Xf, G, S, masks, words, num_perms, nA, nB, kf, fast_ok, st);
+            case 9: return launch_metric_fast<ACC_TWOPASS, COMB_TTEST>(Xf, G, S, masks, words, num_perms, nA, nB, kf, fast_ok, st);
+            default: break;
+        }
+      }
+    }
 #define GSEA_M(ID, A, C)                                                                        \
     case ID:                                                                                   \
         return launch_metric_t<A, C, T>(X, G, S, masks, words, num_perms, nA, nB, keys, st);

@@ -88,7 +88,33 @@ permute_kernel(const uint8_t* __restrict__ labels, int S, int64_t num_perms, int
     }
 }
 
+// fast_ok stays 1 unless some value is not finite or has |x| >= 2^60
+template <class T>
+__global__ void finite_check_kernel(const T* __restrict__ x, int64_t n, int* __restrict__ fast_ok) {
+    bool ok = true;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const T v = x[i];
+        ok &= (v == v) && fabs(v) < T(1.152921504606846976e18);  // 2^60
+    }
+    if (!__all_sync(kFullMask, ok) && (threadIdx.x & 31) == 0) atomicExch(fast_ok, 0);
+}
+
 }  // namespace
+
+template <class T>
+cudaError_t launch_finite_check(const T* exprs, int64_t n, int* fast_ok, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(fast_ok, 1, sizeof(int), st);  // non-zero = packed form allowed
+    if (e != cudaSuccess) return e;
+    const int threads = 256;
+    int64_t blocks = (n + threads - 1) / threads;
+    if (blocks > 4096) blocks = 4096;
+    if (blocks < 1) blocks = 1;
+    finite_check_kernel<T><<<(unsigned)blocks, threads, 0, st>>>(exprs, n, fast_ok);
+    launches_add(1);
+    return cudaGetLastError();
+}
+template cudaError_t launch_finite_check<float>(const float*, int64_t, int*, cudaStream_t);
+template cudaError_t launch_finite_check<double>(const double*, int64_t, int*, cudaStream_t);
 
 cudaError_t launch_permute(const uint8_t* labels, int S, int64_t num_perms, int64_t perm_offset,
                            uint32_t seed, uint32_t* masks, int words, cudaStream_t st) {

@@ -7,9 +7,10 @@
 //
 //   * stable, so tied metrics keep ascending gene order (CUB's semantics);
 //   * -0.0 ranks below +0.0 and NaNs sit at the two ends, as with CUB;
-//   * digit ranks inside a warp come from __match_any_sync (warp-uniform,
-//     deterministic), ranks across warps from a digit-major scan of per-warp
-//     counters in shared memory.
+//   * digit ranks inside a warp come from per-bit ballots (lanes with equal
+//     digits) and one shared-memory atomicAdd per digit group on the warp's
+//     counter; ranks across warps from a digit-major scan of the per-warp
+//     counters.
 //
 // Two variants:
 //   sort_regs_kernel   the whole segment lives in registers (1024 threads x
@@ -34,6 +35,20 @@ constexpr int kWarps = kThreads / 32;
 template <class U>
 __device__ __forceinline__ uint32_t digit_of(U key, int shift) {
     return (uint32_t)(key >> shift) & 0xFFu;
+}
+
+// lanes holding the same 8-bit digit (BITS significant bits), from one
+// ballot per bit: cheaper than the general match instruction
+template <int BITS>
+__device__ __forceinline__ uint32_t match_digit(uint32_t dig) {
+    uint32_t peers = kFullMask;
+#pragma unroll
+    for (int b = 0; b < BITS; b++) {
+        const bool set = (dig >> b) & 1u;
+        const uint32_t vote = __ballot_sync(kFullMask, set);
+        peers &= set ? vote : ~vote;
+    }
+    return peers;
 }
 
 // inverse of RadixKey<T>::from
@@ -141,15 +156,19 @@ sort_regs_kernel(const T* __restrict__ keys, int G, int num_perms, bool descendi
         for (int shift = 0; shift < 8 * (int)sizeof(U); shift += 8) {
             for (int d = lane; d < 256; d += 32) cnt[warp][d] = 0;
             __syncwarp();
+            // rank within the warp: the lowest lane of each digit group adds
+            // the group's size to the warp's digit counter; the atomics of
+            // successive items retire in program order, so ranks follow the
+            // logical item order (stable)
 #pragma unroll
             for (int i = 0; i < ITEMS; i++) {
                 const uint32_t dig = digit_of(key[i], shift);
-                const uint32_t peers = __match_any_sync(kFullMask, dig);
-                const uint32_t before = cnt[warp][dig];
+                const uint32_t peers = match_digit<8>(dig);
+                const int leader = __ffs(peers) - 1;
+                uint32_t before = 0;
+                if (lane == leader) before = atomicAdd(&cnt[warp][dig], (uint32_t)__popc(peers));
+                before = __shfl_sync(kFullMask, before, leader);
                 dst16[my0 + 32 * i] = (uint16_t)(before + __popc(peers & lt));
-                __syncwarp();
-                if ((peers & lt) == 0) cnt[warp][dig] = before + __popc(peers);
-                __syncwarp();
             }
             __syncthreads();
             scan_counters(cnt, tot, nullptr, warp_sums);
@@ -269,13 +288,12 @@ sort_tiled_kernel(const T* __restrict__ keys, int G, int num_perms, bool descend
                     k[i] = valid ? kA[pos] : U(0);
                     v[i] = valid ? vA[pos] : 0u;
                     dg[i] = valid ? digit_of(k[i], shift) : 256u;
-                    const uint32_t peers = __match_any_sync(kFullMask, dg[i]);
+                    const uint32_t peers = match_digit<9>(dg[i]);
+                    const int leader = __ffs(peers) - 1;
                     uint32_t before = 0;
-                    if (valid) before = cnt[warp][dg[i]];
+                    if (valid && lane == leader) before = atomicAdd(&cnt[warp][dg[i]], (uint32_t)__popc(peers));
+                    before = __shfl_sync(kFullMask, before, leader);
                     r[i] = before + __popc(peers & lt);
-                    __syncwarp();
-                    if (valid && (peers & lt) == 0) cnt[warp][dg[i]] = before + __popc(peers);
-                    __syncwarp();
                 }
                 __syncthreads();
                 scan_counters(cnt, tot, base, warp_sums);

@@ -24,9 +24,10 @@ namespace gsea {
 namespace {
 
 struct StatsScratch {
-    // laid out in the scratch buffer
+    // fac[K] mx[P] mn[P] (T) | cnt_obs[K] lcount[K] (u64) | sorted_pos[K]
+    // sorted_neg[K] (T) | hpos[K+2] hneg[K+2] totals[8] (u64)
     static size_t bytes(int K, int64_t P, size_t tsize) {
-        return tsize * ((size_t)K + 2 * (size_t)P) + sizeof(unsigned long long) * (3 * (size_t)K + 8);
+        return tsize * ((size_t)3 * K + 2 * (size_t)P) + sizeof(unsigned long long) * (4 * (size_t)K + 12) + 64;
     }
 };
 
@@ -64,105 +65,203 @@ __global__ void stats_set_kernel(const T* __restrict__ es, int K, int64_t P, T* 
     }
 }
 
-// one thread per permutation column: extrema of normalised scores
+// extrema of the normalised scores per permutation column.  Each thread folds
+// a chunk of sets for one column and merges it with an atomic max / min on
+// the order-preserving radix image of the value (NaN skipped, as the
+// reference's `<` / `>` updates skip it).  Radix image 0 ("empty" for the
+// max) and all-ones ("empty" for the min) belong only to NaN bit patterns.
+constexpr int kExtremaSets = 16;
 template <class T>
-__global__ void stats_extrema_kernel(const T* __restrict__ es, int K, int64_t P,
-                                     const T* __restrict__ fac, T* __restrict__ mx, T* __restrict__ mn) {
+__global__ void stats_extrema_kernel(const T* __restrict__ es, int K, int64_t P, const T* __restrict__ fac,
+                                     typename RadixKey<T>::U* __restrict__ mx,
+                                     typename RadixKey<T>::U* __restrict__ mn) {
+    using U = typename RadixKey<T>::U;
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P) return;
+    const int k0 = blockIdx.y * kExtremaSets, k1 = min(K, k0 + kExtremaSets);
     T hi = -INFINITY, lo = INFINITY;
-    for (int k = 0; k < K; k++) {
+    for (int k = k0; k < k1; k++) {
         const T v = Exact<T>::mul(es[(int64_t)k * P + p], fac[k]);
         hi = hi < v ? v : hi;
         lo = lo > v ? v : lo;
     }
-    mx[p] = hi;
-    mn[p] = lo;
+    atomicMax(&mx[p], (U)RadixKey<T>::from(hi, false));
+    atomicMin(&mn[p], (U)RadixKey<T>::from(lo, false));
 }
 
-// one warp per set: FWER; also the observed-side totals for FDR
 template <class T>
-__global__ void stats_fwer_kernel(int K, int64_t P, const T* __restrict__ mx, const T* __restrict__ mn,
-                                  T* __restrict__ out, unsigned long long* __restrict__ totals) {
+__device__ __forceinline__ T radix_value(typename RadixKey<T>::U u);
+template <>
+__device__ __forceinline__ float radix_value<float>(uint32_t u) {
+    u = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    return __uint_as_float(u);
+}
+template <>
+__device__ __forceinline__ double radix_value<double>(unsigned long long u) {
+    u = (u & 0x8000000000000000ull) ? (u & 0x7fffffffffffffffull) : ~u;
+    return __longlong_as_double((long long)u);
+}
+
+// one warp per set: FWER
+template <class T>
+__global__ void stats_fwer_kernel(int K, int64_t P, const typename RadixKey<T>::U* __restrict__ mx,
+                                  const typename RadixKey<T>::U* __restrict__ mn, T* __restrict__ out) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= K) return;
     const T score = out[K + warp];
     unsigned long long c = 0;
     if (score > T(0)) {
-        for (int64_t p = lane; p < P; p += 32) c += mx[p] >= score;
+        for (int64_t p = lane; p < P; p += 32) c += radix_value<T>(mx[p]) >= score;
     } else {
-        for (int64_t p = lane; p < P; p += 32) c += mn[p] <= score;
+        for (int64_t p = lane; p < P; p += 32) c += radix_value<T>(mn[p]) <= score;
     }
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) c += __shfl_xor_sync(kFullMask, c, o);
-    if (lane == 0) {
-        out[3 * K + warp] = Exact<T>::div((T)c, (T)P);
-        if (score >= T(0)) atomicAdd(&totals[2], 1ull);   // observed >= 0
-        if (score <= T(0)) atomicAdd(&totals[3], 1ull);   // observed <= 0
-    }
+    if (lane == 0) out[3 * K + warp] = Exact<T>::div((T)c, (T)P);
 }
 
-// FDR counts: each block takes a chunk of null scores (all sets, perms >= 1)
-// into shared memory; each thread owns sets and counts the chunk's scores
-// beyond its set's NES.  Also counts the null scores on each side.
-constexpr int kFdrChunk = 4096;
-template <class T>
-__global__ void stats_fdr_count_kernel(const T* __restrict__ es, int K, int64_t P,
-                                       const T* __restrict__ fac, const T* __restrict__ out,
-                                       unsigned long long* __restrict__ cnt_null,
-                                       unsigned long long* __restrict__ totals) {
-    __shared__ T chunk[kFdrChunk];
-    const int64_t total = (int64_t)K * (P - 1);
-    const int64_t c0 = (int64_t)blockIdx.x * kFdrChunk;
-    const int n = (int)(total - c0 < kFdrChunk ? total - c0 : kFdrChunk);
-    unsigned long long pos = 0, neg = 0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const int64_t q = c0 + i;
-        const int64_t k = q / (P - 1), p = 1 + q % (P - 1);
-        const T v = Exact<T>::mul(es[k * P + p], fac[k]);
-        chunk[i] = v;
-        pos += v >= T(0);
-        neg += v <= T(0);
-    }
-    __syncthreads();
-    for (int o = 16; o >= 1; o >>= 1) {
-        pos += __shfl_xor_sync(kFullMask, pos, o);
-        neg += __shfl_xor_sync(kFullMask, neg, o);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        if (pos) atomicAdd(&totals[0], pos);
-        if (neg) atomicAdd(&totals[1], neg);
-    }
-    for (int k = threadIdx.x; k < K; k += blockDim.x) {
-        const T s = out[K + k];
-        unsigned long long c = 0;
-        if (s > T(0)) {
-            for (int i = 0; i < n; i++) c += chunk[i] >= s;
-        } else {
-            for (int i = 0; i < n; i++) c += chunk[i] <= s;
-        }
-        if (c) atomicAdd(&cnt_null[k], c);
-    }
-}
+// ---------------------------------------------------------------------------
+// FDR counts, exact and O(K*P*log K).  Each side is handled as "key >= key*":
+// positive side keys are the scores themselves (observed NES >= 0, null
+// scores >= 0), negative side keys their negations (scores <= 0); a zero is on
+// both sides, NaN on neither.
+//   1. stats_fdr_obs_kernel: for every set, L = #{same-side observed keys <
+//      its key} and the observed count #{>= key}; the observed keys are
+//      scattered into ascending order at L + (#equal keys of lower index).
+//   2. stats_fdr_hist_kernel: every null score is binary-searched into the
+//      sorted observed keys of its side: t = #{observed keys <= it}, H[t]++.
+//   3. stats_fdr_suffix_kernel: S[i] = sum_{t >= i} H[t].
+//   4. stats_fdr_final_kernel: #{null keys >= key*} = S[L + 1] (a null key v
+//      satisfies v >= key* exactly when t(v) >= L + 1).
+// Layout of the FDR part of the scratch (unsigned long long):
+//   cnt_obs[K] | L[K] | sorted_pos[K] (T) | sorted_neg[K] (T) |
+//   H_pos[K+2] | H_neg[K+2] | totals[8]
 
-// observed counts: #{observed NES beyond NES*} on the same side
 template <class T>
-__global__ void stats_fdr_obs_kernel(int K, const T* __restrict__ out, unsigned long long* __restrict__ cnt_obs) {
+__device__ __forceinline__ int side_of(T s) { return s > T(0) ? 0 : (s <= T(0) ? 1 : -1); }
+
+template <class T>
+__global__ void stats_fdr_obs_kernel(int K, const T* __restrict__ out, unsigned long long* __restrict__ cnt_obs,
+                                     unsigned long long* __restrict__ lcount, T* __restrict__ sorted_pos,
+                                     T* __restrict__ sorted_neg, unsigned long long* __restrict__ totals) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= K) return;
     const T s = out[K + k];
-    unsigned long long co = 0;
-    if (s > T(0)) {
-        for (int j = 0; j < K; j++) co += out[K + j] >= s;
-    } else {
-        for (int j = 0; j < K; j++) co += out[K + j] <= s;
+    // membership in the two sorted arrays: o >= 0 (positive), o <= 0 (negative)
+    for (int side = 0; side < 2; side++) {
+        const bool in = side == 0 ? (s >= T(0)) : (s <= T(0));
+        if (!in) continue;
+        const T key = side == 0 ? s : -s;
+        unsigned long long less = 0, eq_before = 0;
+        for (int j = 0; j < K; j++) {
+            const T o = out[K + j];
+            const bool jin = side == 0 ? (o >= T(0)) : (o <= T(0));
+            if (!jin) continue;
+            const T oj = side == 0 ? o : -o;
+            less += oj < key;
+            eq_before += (oj == key) && (j < k);
+        }
+        (side == 0 ? sorted_pos : sorted_neg)[less + eq_before] = key;
+        atomicAdd(&totals[2 + side], 1ull);
+        if (side_of(s) == side) {
+            // observed count on the set's own side: #{keys >= key} = m - less
+            lcount[k] = less;
+        }
     }
-    cnt_obs[k] = co;
+    const int sd = side_of(s);
+    if (sd >= 0) {
+        const T key = sd == 0 ? s : -s;
+        unsigned long long ge = 0;
+        for (int j = 0; j < K; j++) {
+            const T o = out[K + j];
+            const bool jin = sd == 0 ? (o >= T(0)) : (o <= T(0));
+            ge += jin && ((sd == 0 ? o : -o) >= key);
+        }
+        cnt_obs[k] = ge;
+    }
 }
 
 template <class T>
-__global__ void stats_fdr_final_kernel(int K, const unsigned long long* __restrict__ cnt_null,
-                                       const unsigned long long* __restrict__ cnt_obs,
+__device__ __forceinline__ unsigned upper_bound_t(const T* a, unsigned n, T v) {
+    unsigned lo = 0, hi = n;
+    while (lo < hi) {
+        const unsigned mid = (lo + hi) >> 1;
+        if (a[mid] <= v) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+constexpr int kHistThreads = 256;
+template <class T>
+__global__ void __launch_bounds__(kHistThreads)
+stats_fdr_hist_kernel(const T* __restrict__ es, int K, int64_t P, const T* __restrict__ fac,
+                      const T* __restrict__ sorted_pos, const T* __restrict__ sorted_neg,
+                      unsigned long long* __restrict__ hpos, unsigned long long* __restrict__ hneg,
+                      unsigned long long* __restrict__ totals) {
+    const unsigned npos = (unsigned)totals[2], nneg = (unsigned)totals[3];
+    const int64_t total = (int64_t)K * (P - 1);
+    unsigned long long cpos = 0, cneg = 0;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k = q / (P - 1), p = 1 + q % (P - 1);
+        const T v = Exact<T>::mul(es[k * P + p], fac[k]);
+        if (v >= T(0)) {
+            cpos++;
+            atomicAdd(&hpos[upper_bound_t(sorted_pos, npos, v)], 1ull);
+        }
+        if (v <= T(0)) {
+            cneg++;
+            atomicAdd(&hneg[upper_bound_t(sorted_neg, nneg, -v)], 1ull);
+        }
+    }
+    for (int o = 16; o >= 1; o >>= 1) {
+        cpos += __shfl_xor_sync(kFullMask, cpos, o);
+        cneg += __shfl_xor_sync(kFullMask, cneg, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (cpos) atomicAdd(&totals[0], cpos);
+        if (cneg) atomicAdd(&totals[1], cneg);
+    }
+}
+
+// in-place suffix sums of the two histograms (one block each)
+__global__ void stats_fdr_suffix_kernel(unsigned long long* __restrict__ hpos, unsigned long long* __restrict__ hneg,
+                                        const unsigned long long* __restrict__ totals) {
+    unsigned long long* h = blockIdx.x == 0 ? hpos : hneg;
+    const unsigned n = (unsigned)totals[2 + blockIdx.x] + 1;  // bins 0..m
+    __shared__ unsigned long long carry;
+    __shared__ unsigned long long wsum[32];
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    // walk from the top bin down in chunks of blockDim.x
+    for (int64_t top = (int64_t)n - 1; top >= 0; top -= blockDim.x) {
+        const int64_t i = top - threadIdx.x;
+        unsigned long long v = i >= 0 ? h[i] : 0ull;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long y = __shfl_up_sync(kFullMask, v, o);
+            if (lane >= o) v += y;
+        }
+        if (lane == 31) wsum[warp] = v;
+        __syncthreads();
+        unsigned long long before = carry;
+        for (int w = 0; w < warp; w++) before += wsum[w];
+        if (i >= 0) h[i] = v + before;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long t = 0;
+            for (int w = 0; w < nw; w++) t += wsum[w];
+            carry += t;
+        }
+        __syncthreads();
+    }
+}
+
+template <class T>
+__global__ void stats_fdr_final_kernel(int K, const unsigned long long* __restrict__ cnt_obs,
+                                       const unsigned long long* __restrict__ lcount,
+                                       const unsigned long long* __restrict__ spos,
+                                       const unsigned long long* __restrict__ sneg,
                                        const unsigned long long* __restrict__ totals, T* __restrict__ out) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= K) return;
@@ -172,9 +271,12 @@ __global__ void stats_fdr_final_kernel(int K, const unsigned long long* __restri
         q = s;
     } else {
         const bool up = s > T(0);
+        const unsigned long long L = lcount[k];
+        const unsigned long long m = up ? totals[2] : totals[3];
+        const unsigned long long c_null = L + 1 <= m ? (up ? spos : sneg)[L + 1] : 0ull;
         const double null_side = (double)(up ? totals[0] : totals[1]);
-        const double obs_side = (double)(up ? totals[2] : totals[3]);
-        const double fn = null_side > 0 ? (double)cnt_null[k] / null_side : 0.0;
+        const double obs_side = (double)m;
+        const double fn = null_side > 0 ? (double)c_null / null_side : 0.0;
         const double fo = (double)cnt_obs[k] / obs_side;
         const double r = fn / fo;
         q = (T)(r < 1.0 ? r : 1.0);
@@ -195,28 +297,40 @@ template <class T>
 cudaError_t launch_stats(const T* es, int K, int64_t P, T* stats, void* scratch, cudaStream_t st) {
     if (K <= 0 || P <= 0) return cudaSuccess;
     unsigned char* s = static_cast<unsigned char*>(scratch);
-    T* fac = reinterpret_cast<T*>(s);
-    T* mx = fac + K;
-    T* mn = mx + P;
-    size_t off = sizeof(T) * ((size_t)K + 2 * (size_t)P);
-    off = (off + 15) & ~(size_t)15;
-    unsigned long long* cnt_null = reinterpret_cast<unsigned long long*>(s + off);
-    unsigned long long* cnt_obs = cnt_null + K;
-    unsigned long long* totals = cnt_obs + K;
-    cudaError_t e = cudaMemsetAsync(cnt_null, 0, sizeof(unsigned long long) * (2 * (size_t)K + 8), st);
+    auto align16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
+    size_t off = 0;
+    using U = typename RadixKey<T>::U;
+    T* fac = reinterpret_cast<T*>(s + off);
+    U* mx = reinterpret_cast<U*>(fac + K);
+    U* mn = mx + P;
+    off = align16(sizeof(T) * ((size_t)K + 2 * (size_t)P));
+    unsigned long long* cnt_obs = reinterpret_cast<unsigned long long*>(s + off);
+    unsigned long long* lcount = cnt_obs + K;
+    off = align16(off + sizeof(unsigned long long) * 2 * (size_t)K);
+    T* sorted_pos = reinterpret_cast<T*>(s + off);
+    T* sorted_neg = sorted_pos + K;
+    off = align16(off + sizeof(T) * 2 * (size_t)K);
+    unsigned long long* hpos = reinterpret_cast<unsigned long long*>(s + off);
+    unsigned long long* hneg = hpos + (K + 2);
+    unsigned long long* totals = hneg + (K + 2);
+    cudaError_t e = cudaMemsetAsync(hpos, 0, sizeof(unsigned long long) * (2 * ((size_t)K + 2) + 8), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(mx, 0x00, sizeof(U) * (size_t)P, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(mn, 0xff, sizeof(U) * (size_t)P, st);
     if (e != cudaSuccess) return e;
     const int wpb = 8;  // warps per block
     stats_set_kernel<T><<<(K + wpb - 1) / wpb, wpb * 32, 0, st>>>(es, K, P, stats, fac);
-    stats_extrema_kernel<T><<<(unsigned)((P + 255) / 256), 256, 0, st>>>(es, K, P, fac, mx, mn);
-    stats_fwer_kernel<T><<<(K + wpb - 1) / wpb, wpb * 32, 0, st>>>(K, P, mx, mn, stats, totals);
-    int launches = 4;
-    const int64_t total = P > 1 ? (int64_t)K * (P - 1) : 0;
-    const unsigned blocks = total > 0 ? (unsigned)((total + kFdrChunk - 1) / kFdrChunk) : 1u;
-    stats_fdr_count_kernel<T><<<blocks, 256, 0, st>>>(es, K, P, fac, stats, cnt_null, totals);
-    stats_fdr_obs_kernel<T><<<(K + 255) / 256, 256, 0, st>>>(K, stats, cnt_obs);
-    launches++;
-    stats_fdr_final_kernel<T><<<(K + 255) / 256, 256, 0, st>>>(K, cnt_null, cnt_obs, totals, stats);
-    launches_add(launches + 1);
+    stats_extrema_kernel<T><<<dim3((unsigned)((P + 127) / 128), (K + kExtremaSets - 1) / kExtremaSets), 128, 0, st>>>(
+        es, K, P, fac, mx, mn);
+    stats_fwer_kernel<T><<<(K + wpb - 1) / wpb, wpb * 32, 0, st>>>(K, P, mx, mn, stats);
+    stats_fdr_obs_kernel<T><<<(K + 127) / 128, 128, 0, st>>>(K, stats, cnt_obs, lcount, sorted_pos, sorted_neg,
+                                                              totals);
+    const int64_t nnull = (int64_t)K * (P - 1);
+    const unsigned hblocks = nnull > 0 ? (unsigned)((nnull + kHistThreads * 8 - 1) / (kHistThreads * 8)) : 1u;
+    stats_fdr_hist_kernel<T><<<hblocks, kHistThreads, 0, st>>>(es, K, P, fac, sorted_pos, sorted_neg, hpos, hneg,
+                                                               totals);
+    stats_fdr_suffix_kernel<<<2, 1024, 0, st>>>(hpos, hneg, totals);
+    stats_fdr_final_kernel<T><<<(K + 255) / 256, 256, 0, st>>>(K, cnt_obs, lcount, hpos, hneg, totals, stats);
+    launches_add(7);
     return cudaGetLastError();
 }
 template cudaError_t launch_stats<float>(const float*, int, int64_t, float*, void*, cudaStream_t);

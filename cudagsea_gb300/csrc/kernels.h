@@ -12,10 +12,16 @@ cudaError_t launch_permute(const uint8_t* labels, int S, int64_t num_perms, int6
                            uint32_t seed, uint32_t* masks, int words, cudaStream_t st);
 
 // Plain-form class statistics + metric: keys[p][g] for p < num_perms.
+// fast_ok (device int, may be null): set by launch_finite_check; non-zero lets
+// the fp32 kernels use the packed form (bit-identical for finite inputs).
 template <class T>
 cudaError_t launch_metric(int metric, const T* exprs, int G, int S, const uint32_t* masks,
                           int words, int num_perms, int64_t nA, int64_t nB, T* keys,
-                          cudaStream_t st);
+                          const int* fast_ok, cudaStream_t st);
+
+// fast_ok = 1 if every expression value is finite with |x| < 2^60, else 0
+template <class T>
+cudaError_t launch_finite_check(const T* exprs, int64_t n, int* fast_ok, cudaStream_t st);
 
 // Per-permutation stable sort of keys (descending unless ascending):
 //   ranks[p][g]   position of gene g (uint16 when G <= 65536, else uint32)
@@ -37,10 +43,15 @@ cudaError_t launch_sort(const T* keys, int G, int num_perms, bool ascending, con
 
 // Enrichment scores es[k][perm_col0 + p] (row stride es_stride) from ranks and
 // sorted |keys| of num_perms permutations.
+// set_order (optional) lists the sets in the order warps should take them
+// (largest first balances the warps of a CTA).
+// decay (G+1 entries, from launch_decay_table) holds the miss step per hit count.
 template <class T>
 cudaError_t launch_es(const void* ranks, bool ranks16, const T* sorted_abs, int G, int num_perms,
-                      const int64_t* set_offsets, const int32_t* set_genes, int K, T* es,
-                      int64_t es_stride, int64_t perm_col0, cudaStream_t st);
+                      const int64_t* set_offsets, const int32_t* set_genes, const int32_t* set_order,
+                      const T* decay, int K, T* es, int64_t es_stride, int64_t perm_col0, cudaStream_t st);
+template <class T>
+cudaError_t launch_decay_table(int G, T* decay, cudaStream_t st);
 
 // Final statistics (ES, NES, NP, FWER, FDR) from es[K][P]; scratch sized by
 // stats_scratch_bytes.

@@ -199,7 +199,7 @@ int gsea_plan_stage_times(gsea_plan plan, double* ms /* [GSEA_NUM_STAGES] */);
  * that gives all device memory to its own pool, or a loop that must not call
  * cudaMalloc/cudaFree because they can synchronise the device).  The working
  * memory is a fixed 4 MiB array inside the library, held by every GPU that
- * loads it; sizes whose scratch (sizeof(T)*(K+2P) + 8*(3K+8) + 256 bytes)
+ * loads it; sizes whose scratch (sizeof(T)*(3K+2P) + 8*(4K+12) + 320 bytes)
  * exceeds it are rejected with GSEA_ERR_INVALID_ARGUMENT.  The first call on
  * a device looks the array up for that device (make it before any stream
  * capture); calls share the array, so calls that overlap on the GPU race.

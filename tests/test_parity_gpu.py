@@ -270,3 +270,20 @@ def test_full_size_properties(gpu):
     tail.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
     tail.execute()
     np.testing.assert_array_equal(tail.read()[0], es[:, 900:])
+
+
+@pytest.mark.parametrize("value", [np.inf, -np.inf, np.nan, 3e18], ids=["inf", "-inf", "nan", "huge"])
+def test_packed_metric_falls_back_on_special_inputs(gpu, value):
+    """Inputs the packed fp32 form cannot reproduce send the kernel to the
+    exact predicated form: keys stay bit-identical to the oracle."""
+    d = MG.metrics_case()
+    d.exprs = d.exprs.copy()
+    d.exprs[3, 17] = value
+    d.exprs[10, 400] = value
+    for m in (6, 8, 9, 0):
+        r = run_plan(d, m)
+        ok = oracle.metric(m, d.exprs, d.labels, d.num_perms)
+        np.testing.assert_array_equal(r["keys"].view(np.uint32), ok.view(np.uint32), err_msg=str(m))
+        sk, order = check_sort(r["keys"], r["order"], r["ranks"], r["sorted"])
+        es_o = oracle.es(sk, order, d.set_offsets, d.set_genes)
+        assert H.es_close(r["es"], es_o, False).all()
