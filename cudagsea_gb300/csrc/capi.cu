@@ -97,6 +97,14 @@ struct gsea_plan_s {
     uint32_t* masks = nullptr;
     int* fast_ok = nullptr;            // expression values allow the packed metric form
     void* decay = nullptr;             // [G+1] T: miss step per hit count
+    // chosen form (tensor-core class statistics)
+    float* gene_mu = nullptr;
+    double* gene_t1 = nullptr;
+    double* gene_t2 = nullptr;
+    unsigned char* opA1 = nullptr;
+    unsigned char* opA2 = nullptr;
+    unsigned char* opB = nullptr;
+    int* dev_error = nullptr;          // set by kernels whose bounded waits expired
     void* keys = nullptr;
     void* ranks = nullptr;
     void* sorted = nullptr;
@@ -153,7 +161,8 @@ int mark(gsea_plan_s* p, int stage, cudaStream_t st) {
 }
 
 void free_plan_buffers(gsea_plan_s* p) {
-    void* bufs[] = {p->exprs, p->labels, p->set_off, p->set_genes, p->set_order, p->masks, p->fast_ok, p->decay, p->keys,
+    void* bufs[] = {p->exprs, p->labels, p->set_off, p->set_genes, p->set_order, p->masks, p->fast_ok, p->decay, p->gene_mu,
+                    p->gene_t1, p->gene_t2, p->opA1, p->opA2, p->opB, p->dev_error, p->keys,
                     p->ranks, p->sorted, p->order, p->sort_scratch, p->es, p->stats, p->stats_scratch};
     for (void* b : bufs)
         if (b) cudaFree(b);
@@ -164,6 +173,10 @@ void free_plan_buffers(gsea_plan_s* p) {
     p->masks = nullptr;
     p->fast_ok = nullptr;
     p->decay = nullptr;
+    p->gene_mu = nullptr;
+    p->gene_t1 = p->gene_t2 = nullptr;
+    p->opA1 = p->opA2 = p->opB = nullptr;
+    p->dev_error = nullptr;
     p->keys = p->ranks = p->sorted = nullptr;
     p->order = nullptr;
     p->sort_scratch = p->es = p->stats = p->stats_scratch = nullptr;
@@ -239,13 +252,32 @@ int count_labels(gsea_plan_s* p, const uint8_t* labels) {
     return GSEA_OK;
 }
 
-// device-side check of the expression table (sets p->fast_ok), on `st`
+// device-side preparation of freshly uploaded inputs, on `st`: the check of
+// the expression table (sets p->fast_ok) and, for the chosen form, the split
+// tensor-core operands
 int check_inputs(gsea_plan_s* p, cudaStream_t st) {
     const int64_t n = p->cfg.num_genes * p->cfg.num_samples;
     cudaError_t e = p->cfg.precision == 64
                         ? gsea::launch_finite_check<double>(static_cast<const double*>(p->exprs), n, p->fast_ok, st)
                         : gsea::launch_finite_check<float>(static_cast<const float*>(p->exprs), n, p->fast_ok, st);
     if (e != cudaSuccess) return cuda_fail(e, "input check kernel");
+    if (p->cfg.form == GSEA_FORM_CHOSEN) {
+        e = gsea::launch_chosen_prepare<float>(static_cast<const float*>(p->exprs), (int)p->cfg.num_genes,
+                                               (int)p->cfg.num_samples, p->gene_mu, p->gene_t1, p->gene_t2, p->opA1,
+                                               p->opA2, st);
+        if (e != cudaSuccess) return cuda_fail(e, "tensor operand preparation");
+    }
+    return GSEA_OK;
+}
+
+// error flag raised by a kernel whose bounded wait expired (after a sync)
+int check_device_error(gsea_plan_s* p) {
+    int flag = 0;
+    GSEA_CUDA(cudaMemcpy(&flag, p->dev_error, sizeof(int), cudaMemcpyDeviceToHost), "read error flag");
+    if (flag) {
+        cudaMemset(p->dev_error, 0, sizeof(int));
+        return fail(GSEA_ERR_CUDA, "a tensor-core kernel gave up waiting for its data (bounded wait expired)");
+    }
     return GSEA_OK;
 }
 
@@ -271,9 +303,16 @@ int execute_t(gsea_plan_s* p, cudaStream_t st) {
         GSEA_CUDA(gsea::launch_permute(p->labels, S, nb, c.perm_offset + b0, c.seed, p->masks, p->words, st),
                   "permute kernel");
         if ((rc = mark(p, 0, st))) return rc;
-        GSEA_CUDA(gsea::launch_metric<T>(c.metric, static_cast<const T*>(p->exprs), G, S, p->masks, p->words,
-                                         nb, p->nA, p->nB, static_cast<T*>(p->keys), p->fast_ok, st),
-                  "metric kernel");
+        if (c.form == GSEA_FORM_CHOSEN) {
+            GSEA_CUDA(gsea::launch_chosen_metric(c.metric, p->masks, p->words, G, S, nb, p->nA, p->nB, p->gene_mu,
+                                                 p->gene_t1, p->gene_t2, p->opA1, p->opA2, p->opB,
+                                                 static_cast<float*>(p->keys), p->dev_error, st),
+                      "tensor-core class statistics");
+        } else {
+            GSEA_CUDA(gsea::launch_metric<T>(c.metric, static_cast<const T*>(p->exprs), G, S, p->masks, p->words,
+                                             nb, p->nA, p->nB, static_cast<T*>(p->keys), p->fast_ok, st),
+                      "metric kernel");
+        }
         if ((rc = mark(p, 1, st))) return rc;
         GSEA_CUDA(gsea::launch_sort<T>(static_cast<const T*>(p->keys), G, nb, c.ascending != 0, sb, st),
                   "sort kernel");
@@ -408,8 +447,8 @@ int gsea_plan_create(const gsea_config* cfg, gsea_plan* out) {
     int rc = validate_config(cfg);
     if (rc) return rc;
     if (injected("alloc")) return fail(GSEA_ERR_INJECTED, "injected allocation failure: plan");
-    if (cfg->form == GSEA_FORM_CHOSEN)
-        return fail(GSEA_ERR_UNSUPPORTED, "the tensor-core form is not available in this build");
+    if (cfg->form == GSEA_FORM_CHOSEN && cfg->precision != 32)
+        return fail(GSEA_ERR_UNSUPPORTED, "the tensor-core form computes from fp32 inputs (precision 32)");
     gsea_plan_s* p = new (std::nothrow) gsea_plan_s();
     if (!p) return fail(GSEA_ERR_OUT_OF_MEMORY, "host allocation");
     p->cfg = *cfg;
@@ -438,6 +477,7 @@ int gsea_plan_create(const gsea_config* cfg, gsea_plan* out) {
         (rc = dev_alloc(&p->masks, 4 * (size_t)p->words * pb, "label masks")) ||
         (rc = dev_alloc(&p->fast_ok, sizeof(int), "input flags")) ||
         (rc = dev_alloc(&p->decay, T * ((size_t)G + 1), "decay table")) ||
+        (rc = dev_alloc(&p->dev_error, sizeof(int), "error flag")) ||
         (rc = dev_alloc(&p->keys, T * (size_t)G * pb, "metric keys")) ||
         (rc = dev_alloc(&p->ranks, (p->ranks16 ? 2 : 4) * (size_t)G * pb, "ranks")) ||
         (rc = dev_alloc(&p->sorted, T * (size_t)G * pb, "sorted weights")) ||
@@ -452,6 +492,18 @@ int gsea_plan_create(const gsea_config* cfg, gsea_plan* out) {
                                                  : gsea::sort_scratch_bytes<float>((int)G, (int)pb);
     p->stats_scratch_bytes = cfg->precision == 64 ? gsea::stats_scratch_bytes<double>((int)K, P)
                                                   : gsea::stats_scratch_bytes<float>((int)K, P);
+    if (cfg->form == GSEA_FORM_CHOSEN &&
+        ((rc = dev_alloc(&p->gene_mu, sizeof(float) * (size_t)G, "gene means")) ||
+         (rc = dev_alloc(&p->gene_t1, sizeof(double) * (size_t)G, "gene totals")) ||
+         (rc = dev_alloc(&p->gene_t2, sizeof(double) * (size_t)G, "gene totals")) ||
+         (rc = dev_alloc(&p->opA1, gsea::chosen_a_bytes((int)G, (int)S), "tensor operand A")) ||
+         (rc = dev_alloc(&p->opA2, gsea::chosen_a_bytes((int)G, (int)S), "tensor operand A2")) ||
+         (rc = dev_alloc(&p->opB, gsea::chosen_b_bytes((int)pb, (int)S), "tensor operand B")))) {
+        free_plan_buffers(p);
+        cudaStreamDestroy(p->stream);
+        delete p;
+        return rc;
+    }
     if ((p->sort_scratch_bytes && (rc = dev_alloc(&p->sort_scratch, p->sort_scratch_bytes, "sort scratch"))) ||
         (rc = dev_alloc(&p->stats_scratch, p->stats_scratch_bytes, "statistics scratch"))) {
         free_plan_buffers(p);
@@ -462,6 +514,7 @@ int gsea_plan_create(const gsea_config* cfg, gsea_plan* out) {
     cudaError_t de = cfg->precision == 64
                          ? gsea::launch_decay_table<double>((int)G, static_cast<double*>(p->decay), p->stream)
                          : gsea::launch_decay_table<float>((int)G, static_cast<float*>(p->decay), p->stream);
+    if (de == cudaSuccess) de = cudaMemsetAsync(p->dev_error, 0, sizeof(int), p->stream);
     if (de == cudaSuccess) de = cudaStreamSynchronize(p->stream);
     if (de != cudaSuccess) {
         free_plan_buffers(p);
@@ -516,7 +569,7 @@ int gsea_plan_synchronize(gsea_plan p) {
     if (rc) return rc;
     GSEA_CUDA(cudaStreamSynchronize(p->stream), "stream sync");
     GSEA_CUDA(cudaDeviceSynchronize(), "device sync");
-    return GSEA_OK;
+    return check_device_error(p);
 }
 
 int gsea_plan_read(gsea_plan p, void* es_out, void* stats_out) {
@@ -524,6 +577,7 @@ int gsea_plan_read(gsea_plan p, void* es_out, void* stats_out) {
     int rc = use_device(p);
     if (rc) return rc;
     GSEA_CUDA(cudaDeviceSynchronize(), "device sync");
+    if ((rc = check_device_error(p))) return rc;
     if (injected("d2h")) return fail(GSEA_ERR_INJECTED, "injected device-to-host failure");
     const size_t T = p->tsize;
     if (es_out)
@@ -559,7 +613,7 @@ int gsea_plan_run_host(gsea_plan p, const void* exprs, const uint8_t* labels, co
         GSEA_CUDA(cudaMemcpyAsync(stats_out, p->stats, T * 5 * (size_t)p->cfg.num_sets, cudaMemcpyDeviceToHost, st),
                   "copy statistics");
     GSEA_CUDA(cudaStreamSynchronize(st), "stream sync");
-    return GSEA_OK;
+    return p->cfg.form == GSEA_FORM_CHOSEN ? check_device_error(p) : GSEA_OK;
 }
 
 int gsea_plan_buffer(gsea_plan p, int which, void** dev_ptr, size_t* bytes) {

@@ -1,0 +1,415 @@
+// k_chosen.cu -- class statistics on the tcgen05 tensor cores (chosen form).
+//
+// For every permutation p and gene g the reference sums class-A values and
+// squares over the samples (src/include/functors.cuh:87-433).  With the
+// permuted labels as a 0/1 matrix L[s][p] (class A = 1) these sums are the
+// contractions
+//     SA [g][p] = sum_s x'[s][g]   * L[s][p]
+//     SA2[g][p] = sum_s x'[s][g]^2 * L[s][p]
+// over centred values x' = x - mean_g (the gene mean over all samples, FP64);
+// class B follows from the per-gene totals (T1 - SA, T2 - SA2).
+//
+// Operands: x' and x'^2 are split into three BF16 parts each (hi + mid + lo
+// carries ~24 significant bits) stacked along K, the labels are exact 0/1 in
+// BF16 and repeated for each part, so one BF16 x BF16 -> FP32 GEMM of depth
+// 3*S gives each sum.  A CTA owns 128 genes x 256 permutations:
+//   * two FP32 accumulators in tensor memory (columns 0-255: SA,
+//     256-511: SA2), allocated with tcgen05.alloc;
+//   * the operands are pre-arranged in the canonical no-swizzle K-major
+//     layout (8x8 core matrices of 128 bytes), 64 K-elements per chunk, so a
+//     chunk of A (16 KB), A2 (16 KB) and B (32 KB) is one contiguous 1-D TMA
+//     bulk copy each (cp.async.bulk) completing on an mbarrier; two stages;
+//   * one thread issues tcgen05.mma (M=128, N=256, K=16) with shared-memory
+//     descriptors and tcgen05.commit to the stage's mbarrier;
+//   * four warps read the accumulators with tcgen05.ld (32 lanes x 16
+//     columns at a time), finalise the metric and store the keys.
+// Every mbarrier wait is bounded (about one second of clock); on expiry the
+// kernel records an error flag, waits a bounded time for its own copies and
+// MMAs, frees its tensor memory and returns -- no wait can hang the GPU.
+//
+// Finalisation: means and the mean-square-minus-squared-mean variances are
+// formed from the FP32 sums with the subtraction in FP64; the metric itself
+// (difference, ratio, log2 ratio, signal-to-noise, T test, with the
+// reference's fixlow floors) is then evaluated in FP32 on centred
+// differences.  The result is the metric of the FP32 inputs to ~1e-6
+// relative, not the reference's operation order: near-tied genes may swap.
+#include <cuda_bf16.h>
+
+#include <cstdint>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace gsea {
+namespace chosen {
+
+constexpr int BM = 128;          // genes per CTA (TMEM lanes)
+constexpr int BN = 256;          // permutations per CTA
+constexpr int BK = 64;           // K elements per chunk
+constexpr int A_CHUNK = BM * BK * 2;   // 16 KB
+constexpr int B_CHUNK = BN * BK * 2;   // 32 KB
+constexpr int STAGE_BYTES = 2 * A_CHUNK + B_CHUNK;
+constexpr int STAGES = 2;
+constexpr int THREADS = 128;
+constexpr long long kWaitCycles = 2000000000ll;  // ~1 s at 2 GHz
+
+// byte offset of element (row, k) inside a chunk laid out as 8x8 core
+// matrices: core (row/8, k/8) at ((row/8)*8 + k/8)*128, row-major inside
+__host__ __device__ __forceinline__ uint32_t core_offset(int row, int k) {
+    return (uint32_t)((((row >> 3) * (BK / 8) + (k >> 3)) << 7) + ((row & 7) << 4) + ((k & 7) << 1));
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// shared-memory matrix descriptor, no swizzle, K-major
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;  // descriptor version for tcgen05
+    // base offset 0, lbo mode 0, layout type 0 (no swizzle)
+    return d;
+}
+
+// instruction descriptor: kind::f16, BF16 x BF16 -> F32, K-major A and B
+__host__ __device__ constexpr uint32_t make_idesc(int m, int n) {
+    return (1u << 4)                       // D format F32
+           | (1u << 7)                     // A format BF16
+           | (1u << 10)                    // B format BF16
+           | ((uint32_t)(n >> 3) << 17)    // N / 8
+           | ((uint32_t)(m >> 4) << 24);   // M / 16
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait; false after ~1 s
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (!mbar_try(bar, parity)) {
+        if (clock64() - t0 > kWaitCycles) return false;
+    }
+    return true;
+}
+__device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
+            tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+          "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(taddr)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// metric from centred class statistics (see the file comment)
+template <int COMB>
+__device__ __forceinline__ float finalize(float mAc, float mBc, float mu, float vA, float vB, float nA, float nB) {
+    const float diff = mAc - mBc;
+    const float mA = mu + mAc, mB = mu + mBc;
+    if (COMB == 0) return diff;
+    if (COMB == 1) return mA / mB;
+    if (COMB == 2) return logf(mA / mB) * 1.44269504089f;
+    if (COMB == 3) {
+        float sA = sqrtf(vA), sB = sqrtf(vB);
+        const float lowA = 0.2f * fabsf(mA), lowB = 0.2f * fabsf(mB);
+        sA = lowA < sA ? sA : lowA;
+        sB = lowB < sB ? sB : lowB;
+        return diff / (sA + sB);
+    }
+    float wA = vA, wB = vB;
+    const float lowA = 0.04f * fabsf(mA), lowB = 0.04f * fabsf(mB);
+    wA = lowA < wA ? wA : lowA;
+    wB = lowB < wB ? wB : lowB;
+    return diff / sqrtf(wA / nA + wB / nB);
+}
+
+__device__ __forceinline__ float canonical_nan_f(float v) { return v != v ? __uint_as_float(0x7fffffffu) : v; }
+
+template <int COMB>
+__global__ void __launch_bounds__(THREADS, 1)
+class_stats_kernel(const unsigned char* __restrict__ A1, const unsigned char* __restrict__ A2,
+                   const unsigned char* __restrict__ B, int chunks, int G, int num_perms,
+                   const float* __restrict__ gene_mu, const double* __restrict__ gene_t1,
+                   const double* __restrict__ gene_t2, float nA, float nB, float* __restrict__ keys,
+                   int* __restrict__ error_flag) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bar_full[STAGES];
+    __shared__ __align__(8) uint64_t bar_done[STAGES];
+    __shared__ uint32_t tmem_slot;
+    __shared__ int failed;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int gt = blockIdx.x, pt = blockIdx.y;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(&tmem_slot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < STAGES; s++) {
+            mbar_init(smem_u32(&bar_full[s]), 1);
+            mbar_init(smem_u32(&bar_done[s]), 1);
+        }
+        failed = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = tmem_slot;
+
+    if (tid == 0) {
+        const uint32_t idesc = make_idesc(BM, BN);
+        uint32_t ph_full[STAGES] = {0, 0}, ph_done[STAGES] = {0, 0};
+        int issued = 0;  // chunks whose MMAs were committed
+        bool ok = true;
+        for (int c = 0; c < chunks && ok; c++) {
+            const int s = c & 1;
+            if (c >= STAGES) {  // the MMAs that read this stage are done
+                ok = mbar_wait(smem_u32(&bar_done[s]), ph_done[s]);
+                ph_done[s] ^= 1;
+                if (!ok) break;
+            }
+            unsigned char* st = smem + s * STAGE_BYTES;
+            const uint32_t bar = smem_u32(&bar_full[s]);
+            mbar_expect_tx(bar, STAGE_BYTES);
+            bulk_copy(smem_u32(st), A1 + ((size_t)gt * chunks + c) * A_CHUNK, A_CHUNK, bar);
+            bulk_copy(smem_u32(st + A_CHUNK), A2 + ((size_t)gt * chunks + c) * A_CHUNK, A_CHUNK, bar);
+            bulk_copy(smem_u32(st + 2 * A_CHUNK), B + ((size_t)pt * chunks + c) * B_CHUNK, B_CHUNK, bar);
+            ok = mbar_wait(bar, ph_full[s]);
+            ph_full[s] ^= 1;
+            if (!ok) break;
+            fence_after();
+            const uint32_t a1 = smem_u32(st), a2 = a1 + A_CHUNK, b = a1 + 2 * A_CHUNK;
+#pragma unroll
+            for (int kk = 0; kk < BK / 16; kk++) {
+                // K = 16 spans two core matrices along K: LBO = 128 B apart,
+                // row groups SBO = (BK/8)*128 B apart
+                const uint32_t koff = kk * 256;
+                const uint64_t da1 = make_desc(a1 + koff, 128, (BK / 8) * 128);
+                const uint64_t da2 = make_desc(a2 + koff, 128, (BK / 8) * 128);
+                const uint64_t db = make_desc(b + koff, 128, (BK / 8) * 128);
+                const uint32_t acc = (c > 0 || kk > 0) ? 1u : 0u;
+                mma_bf16(tmem, da1, db, idesc, acc);
+                mma_bf16(tmem + BN, da2, db, idesc, acc);
+            }
+            mma_commit(smem_u32(&bar_done[s]));
+            issued = c + 1;
+        }
+        // wait for the last commit of every stage in use
+        for (int c = (issued > STAGES ? issued - STAGES : 0); c < issued; c++) {
+            const int s = c & 1;
+            if (!mbar_wait(smem_u32(&bar_done[s]), ph_done[s])) ok = false;
+            ph_done[s] ^= 1;
+        }
+        if (!ok) {
+            failed = 1;
+            atomicExch(error_flag, 1);
+        }
+        fence_before();
+    }
+    __syncthreads();
+    fence_after();
+
+    if (!failed) {
+        const int row = warp * 32 + lane;  // TMEM lane = gene within the tile
+        const int g = gt * BM + row;
+        const bool gv = g < G;
+        const float mu = gv ? gene_mu[g] : 0.f;
+        const float t1 = gv ? (float)gene_t1[g] : 0.f, t2 = gv ? (float)gene_t2[g] : 0.f;
+        const float inA = 1.f / nA, inB = 1.f / nB;
+        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+        for (int cb = 0; cb < BN / 16; cb++) {
+            uint32_t va[16], vq[16];
+            tmem_ld16(tmem + lane_base + cb * 16, va);
+            tmem_ld16(tmem + lane_base + BN + cb * 16, vq);
+            tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+                const int p = pt * BN + cb * 16 + j;
+                const float sA = __uint_as_float(va[j]), sA2 = __uint_as_float(vq[j]);
+                // class means and mean squares (centred); B from the totals
+                const float mAc = sA * inA;
+                const float mBc = (t1 - sA) * inB;
+                const float eA = sA2 * inA;
+                const float eB = (t2 - sA2) * inB;
+                // variance = mean square - squared mean, subtracted in FP64
+                const float vA = (float)fma(-(double)mAc, (double)mAc, (double)eA);
+                const float vB = (float)fma(-(double)mBc, (double)mBc, (double)eB);
+                const float key = finalize<COMB>(mAc, mBc, mu, vA, vB, nA, nB);
+                if (gv && p < num_perms) keys[(size_t)p * G + g] = canonical_nan_f(key);
+            }
+        }
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+    }
+}
+
+// ---------------------------------------------------------------------------
+// operand preparation
+
+// per gene: mean over all samples and the centred totals (FP64)
+template <class T>
+__global__ void gene_moments_kernel(const T* __restrict__ X, int G, int S, float* __restrict__ mu_f,
+                                    double* __restrict__ t1, double* __restrict__ t2) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= G) return;
+    double s = 0.0;
+    for (int i = 0; i < S; i++) s += (double)X[(size_t)i * G + g];
+    const double mu = s / S;
+    double a = 0.0, b = 0.0;
+    for (int i = 0; i < S; i++) {
+        const double d = (double)X[(size_t)i * G + g] - mu;
+        a += d;
+        b += d * d;
+    }
+    mu_f[g] = (float)mu;
+    t1[g] = a;
+    t2[g] = b;
+}
+
+__device__ __forceinline__ void split3(double v, __nv_bfloat16& hi, __nv_bfloat16& mid, __nv_bfloat16& lo) {
+    hi = __double2bfloat16(v);
+    const double r1 = v - (double)__bfloat162float(hi);
+    mid = __double2bfloat16(r1);
+    const double r2 = r1 - (double)__bfloat162float(mid);
+    lo = __double2bfloat16(r2);
+}
+
+// A1 (x') and A2 (x'^2) in chunked core-matrix layout; K index = part*S + s.
+// One thread per (gene, sample); the buffers are zeroed beforehand.
+template <class T>
+__global__ void split_operands_kernel(const T* __restrict__ X, int G, int S, int chunks,
+                                      const float* __restrict__ mu_f, unsigned char* __restrict__ A1,
+                                      unsigned char* __restrict__ A2) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = blockIdx.y;
+    if (g >= G) return;
+    const double d = (double)X[(size_t)s * G + g] - (double)mu_f[g];
+    __nv_bfloat16 p[3], q[3];
+    split3(d, p[0], p[1], p[2]);
+    split3(d * d, q[0], q[1], q[2]);
+    const int gt = g / BM, row = g % BM;
+    for (int part = 0; part < 3; part++) {
+        const int k = part * S + s;
+        const int c = k / BK, kk = k % BK;
+        const size_t off = ((size_t)gt * chunks + c) * A_CHUNK + core_offset(row, kk);
+        *reinterpret_cast<__nv_bfloat16*>(A1 + off) = p[part];
+        *reinterpret_cast<__nv_bfloat16*>(A2 + off) = q[part];
+    }
+}
+
+// B: class-A indicator of every (permutation, sample), repeated for the three
+// parts; one thread per (permutation, sample); the buffer is zeroed before.
+__global__ void label_operand_kernel(const uint32_t* __restrict__ masks, int words, int S, int num_perms,
+                                     int chunks, unsigned char* __restrict__ Bm) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = blockIdx.y;
+    if (p >= num_perms) return;
+    const bool a = (masks[(size_t)p * words + (s >> 5)] >> (s & 31)) & 1u;
+    const __nv_bfloat16 v = __float2bfloat16(a ? 1.f : 0.f);
+    const int pt = p / BN, row = p % BN;
+    for (int part = 0; part < 3; part++) {
+        const int k = part * S + s;
+        const int c = k / BK, kk = k % BK;
+        *reinterpret_cast<__nv_bfloat16*>(Bm + ((size_t)pt * chunks + c) * B_CHUNK + core_offset(row, kk)) = v;
+    }
+}
+
+}  // namespace chosen
+
+int chosen_chunks(int S) { return (3 * S + chosen::BK - 1) / chosen::BK; }
+size_t chosen_a_bytes(int G, int S) {
+    return (size_t)((G + chosen::BM - 1) / chosen::BM) * chosen_chunks(S) * chosen::A_CHUNK;
+}
+size_t chosen_b_bytes(int P, int S) {
+    return (size_t)((P + chosen::BN - 1) / chosen::BN) * chosen_chunks(S) * chosen::B_CHUNK;
+}
+
+template <class T>
+cudaError_t launch_chosen_prepare(const T* X, int G, int S, float* mu, double* t1, double* t2, unsigned char* A1,
+                                  unsigned char* A2, cudaStream_t st) {
+    const size_t ab = chosen_a_bytes(G, S);
+    cudaError_t e = cudaMemsetAsync(A1, 0, ab, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(A2, 0, ab, st);
+    if (e != cudaSuccess) return e;
+    chosen::gene_moments_kernel<T><<<(G + 127) / 128, 128, 0, st>>>(X, G, S, mu, t1, t2);
+    chosen::split_operands_kernel<T><<<dim3((G + 127) / 128, S), 128, 0, st>>>(X, G, S, chosen_chunks(S), mu, A1, A2);
+    launches_add(2);
+    return cudaGetLastError();
+}
+template cudaError_t launch_chosen_prepare<float>(const float*, int, int, float*, double*, double*, unsigned char*,
+                                                  unsigned char*, cudaStream_t);
+
+cudaError_t launch_chosen_metric(int metric, const uint32_t* masks, int words, int G, int S, int num_perms,
+                                 int64_t nA, int64_t nB, const float* mu, const double* t1, const double* t2,
+                                 const unsigned char* A1, const unsigned char* A2, unsigned char* Bm, float* keys,
+                                 int* error_flag, cudaStream_t st) {
+    using namespace chosen;
+    const int chunks = chosen_chunks(S);
+    cudaError_t e = cudaMemsetAsync(Bm, 0, chosen_b_bytes(num_perms, S), st);
+    if (e != cudaSuccess) return e;
+    label_operand_kernel<<<dim3((num_perms + 127) / 128, S), 128, 0, st>>>(masks, words, S, num_perms, chunks, Bm);
+    const int comb = metric == 0 || metric == 3 ? 0 : metric == 1 || metric == 4 ? 1 : metric == 2 || metric == 5 ? 2
+                   : (metric == 6 || metric == 8 || metric == 10 || metric == 12) ? 3 : 4;
+    const dim3 grid((G + BM - 1) / BM, (num_perms + BN - 1) / BN);
+    const size_t smem = (size_t)STAGES * STAGE_BYTES;
+#define GSEA_CHOSEN(C)                                                                                        \
+    {                                                                                                         \
+        auto kern = class_stats_kernel<C>;                                                                    \
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);               \
+        if (e != cudaSuccess) return e;                                                                       \
+        kern<<<grid, THREADS, smem, st>>>(A1, A2, Bm, chunks, G, num_perms, mu, t1, t2, (float)nA, (float)nB, \
+                                          keys, error_flag);                                                  \
+    }
+    switch (comb) {
+        case 0: GSEA_CHOSEN(0) break;
+        case 1: GSEA_CHOSEN(1) break;
+        case 2: GSEA_CHOSEN(2) break;
+        case 3: GSEA_CHOSEN(3) break;
+        default: GSEA_CHOSEN(4) break;
+    }
+#undef GSEA_CHOSEN
+    launches_add(2);
+    return cudaGetLastError();
+}
+
+}  // namespace gsea

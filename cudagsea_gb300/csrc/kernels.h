@@ -60,6 +60,22 @@ size_t stats_scratch_bytes(int K, int64_t P);
 template <class T>
 cudaError_t launch_stats(const T* es, int K, int64_t P, T* stats, void* scratch, cudaStream_t st);
 
+// Chosen form (tcgen05 class statistics, fp32 inputs).  Operand buffers:
+// A1/A2 chosen_a_bytes(G, S) each, B chosen_b_bytes(P_batch, S).
+int chosen_chunks(int S);
+size_t chosen_a_bytes(int G, int S);
+size_t chosen_b_bytes(int P, int S);
+// once per upload: gene means / centred totals and the split operands
+template <class T>
+cudaError_t launch_chosen_prepare(const T* X, int G, int S, float* mu, double* t1, double* t2,
+                                  unsigned char* A1, unsigned char* A2, cudaStream_t st);
+// per permutation batch: label operand + GEMM + metric epilogue -> keys[p][g];
+// error_flag is set if a bounded wait expired
+cudaError_t launch_chosen_metric(int metric, const uint32_t* masks, int words, int G, int S, int num_perms,
+                                 int64_t nA, int64_t nB, const float* mu, const double* t1, const double* t2,
+                                 const unsigned char* A1, const unsigned char* A2, unsigned char* Bm,
+                                 float* keys, int* error_flag, cudaStream_t st);
+
 // number of kernel launches issued by the launchers above since the last reset
 int64_t launches_take();
 void launches_add(int64_t n);
