@@ -23,7 +23,7 @@ STATUS = {
 }
 
 BUF_EXPRS, BUF_LABEL_MASKS, BUF_KEYS, BUF_RANKS, BUF_ORDER, BUF_ES, BUF_STATS, BUF_SORTED = range(8)
-FORM_PLAIN, FORM_CHOSEN = 0, 1
+FORM_PLAIN, FORM_CHOSEN, FORM_CHOSEN_FP64 = 0, 1, 2
 STAGES = ("permute", "metric", "sort", "es", "stats")
 
 

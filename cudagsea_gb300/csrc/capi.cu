@@ -139,7 +139,7 @@ int validate_config(const gsea_config* c) {
         return fail(GSEA_ERR_UNKNOWN_METRIC, "unknown metric id");
     if (c->precision != 32 && c->precision != 64)
         return fail(GSEA_ERR_INVALID_ARGUMENT, "precision must be 32 or 64");
-    if (c->form != GSEA_FORM_PLAIN && c->form != GSEA_FORM_CHOSEN)
+    if (c->form != GSEA_FORM_PLAIN && c->form != GSEA_FORM_CHOSEN && c->form != GSEA_FORM_CHOSEN_FP64)
         return fail(GSEA_ERR_INVALID_ARGUMENT, "unknown form");
     if (c->perm_offset < 0 || c->perm_batch < 0)
         return fail(GSEA_ERR_INVALID_ARGUMENT, "negative perm_offset / perm_batch");
@@ -261,7 +261,7 @@ int check_inputs(gsea_plan_s* p, cudaStream_t st) {
                         ? gsea::launch_finite_check<double>(static_cast<const double*>(p->exprs), n, p->fast_ok, st)
                         : gsea::launch_finite_check<float>(static_cast<const float*>(p->exprs), n, p->fast_ok, st);
     if (e != cudaSuccess) return cuda_fail(e, "input check kernel");
-    if (p->cfg.form == GSEA_FORM_CHOSEN) {
+    if (p->cfg.form != GSEA_FORM_PLAIN) {
         e = gsea::launch_chosen_prepare<float>(static_cast<const float*>(p->exprs), (int)p->cfg.num_genes,
                                                (int)p->cfg.num_samples, p->gene_mu, p->gene_t1, p->gene_t2, p->opA1,
                                                p->opA2, st);
@@ -303,8 +303,9 @@ int execute_t(gsea_plan_s* p, cudaStream_t st) {
         GSEA_CUDA(gsea::launch_permute(p->labels, S, nb, c.perm_offset + b0, c.seed, p->masks, p->words, st),
                   "permute kernel");
         if ((rc = mark(p, 0, st))) return rc;
-        if (c.form == GSEA_FORM_CHOSEN) {
-            GSEA_CUDA(gsea::launch_chosen_metric(c.metric, p->masks, p->words, G, S, nb, p->nA, p->nB, p->gene_mu,
+        if (c.form != GSEA_FORM_PLAIN) {
+            GSEA_CUDA(gsea::launch_chosen_metric(c.metric, c.form == GSEA_FORM_CHOSEN_FP64, p->masks, p->words, G, S,
+                                                 nb, p->nA, p->nB, p->gene_mu,
                                                  p->gene_t1, p->gene_t2, p->opA1, p->opA2, p->opB,
                                                  static_cast<float*>(p->keys), p->dev_error, st),
                       "tensor-core class statistics");
@@ -447,7 +448,7 @@ int gsea_plan_create(const gsea_config* cfg, gsea_plan* out) {
     int rc = validate_config(cfg);
     if (rc) return rc;
     if (injected("alloc")) return fail(GSEA_ERR_INJECTED, "injected allocation failure: plan");
-    if (cfg->form == GSEA_FORM_CHOSEN && cfg->precision != 32)
+    if (cfg->form != GSEA_FORM_PLAIN && cfg->precision != 32)
         return fail(GSEA_ERR_UNSUPPORTED, "the tensor-core form computes from fp32 inputs (precision 32)");
     gsea_plan_s* p = new (std::nothrow) gsea_plan_s();
     if (!p) return fail(GSEA_ERR_OUT_OF_MEMORY, "host allocation");
@@ -492,7 +493,7 @@ int gsea_plan_create(const gsea_config* cfg, gsea_plan* out) {
                                                  : gsea::sort_scratch_bytes<float>((int)G, (int)pb);
     p->stats_scratch_bytes = cfg->precision == 64 ? gsea::stats_scratch_bytes<double>((int)K, P)
                                                   : gsea::stats_scratch_bytes<float>((int)K, P);
-    if (cfg->form == GSEA_FORM_CHOSEN &&
+    if (cfg->form != GSEA_FORM_PLAIN &&
         ((rc = dev_alloc(&p->gene_mu, sizeof(float) * (size_t)G, "gene means")) ||
          (rc = dev_alloc(&p->gene_t1, sizeof(double) * (size_t)G, "gene totals")) ||
          (rc = dev_alloc(&p->gene_t2, sizeof(double) * (size_t)G, "gene totals")) ||
@@ -613,7 +614,7 @@ int gsea_plan_run_host(gsea_plan p, const void* exprs, const uint8_t* labels, co
         GSEA_CUDA(cudaMemcpyAsync(stats_out, p->stats, T * 5 * (size_t)p->cfg.num_sets, cudaMemcpyDeviceToHost, st),
                   "copy statistics");
     GSEA_CUDA(cudaStreamSynchronize(st), "stream sync");
-    return p->cfg.form == GSEA_FORM_CHOSEN ? check_device_error(p) : GSEA_OK;
+    return p->cfg.form != GSEA_FORM_PLAIN ? check_device_error(p) : GSEA_OK;
 }
 
 int gsea_plan_buffer(gsea_plan p, int which, void** dev_ptr, size_t* bytes) {

@@ -18,17 +18,21 @@
 //   * the operands are pre-arranged in the canonical no-swizzle K-major
 //     layout (8x8 core matrices of 128 bytes), 64 K-elements per chunk, so a
 //     chunk of A (16 KB), A2 (16 KB) and B (32 KB) is one contiguous 1-D TMA
-//     bulk copy each (cp.async.bulk) completing on an mbarrier; two stages;
+//     bulk copy each (cp.async.bulk) completing on an mbarrier; three stages
+//     in flight, a stage refilled as soon as the MMAs of its chunk retired;
 //   * one thread issues tcgen05.mma (M=128, N=256, K=16) with shared-memory
 //     descriptors and tcgen05.commit to the stage's mbarrier;
-//   * four warps read the accumulators with tcgen05.ld (32 lanes x 16
-//     columns at a time), finalise the metric and store the keys.
+//   * eight warps read the accumulators with tcgen05.ld (a warp reads its
+//     lane quarter, 32 lanes x 16 columns at a time, over half of the
+//     columns), finalise the metric and store the keys.
 // Every mbarrier wait is bounded (about one second of clock); on expiry the
 // kernel records an error flag, waits a bounded time for its own copies and
 // MMAs, frees its tensor memory and returns -- no wait can hang the GPU.
 //
 // Finalisation: means and the mean-square-minus-squared-mean variances are
-// formed from the FP32 sums with the subtraction in FP64; the metric itself
+// formed from the FP32 sums, the subtraction either in FP64
+// (GSEA_FORM_CHOSEN_FP64) or as an error-free FP32 transformation
+// (GSEA_FORM_CHOSEN, see variance()); the metric itself
 // (difference, ratio, log2 ratio, signal-to-noise, T test, with the
 // reference's fixlow floors) is then evaluated in FP32 on centred
 // differences.  The result is the metric of the FP32 inputs to ~1e-6
@@ -49,8 +53,8 @@ constexpr int BK = 64;           // K elements per chunk
 constexpr int A_CHUNK = BM * BK * 2;   // 16 KB
 constexpr int B_CHUNK = BN * BK * 2;   // 32 KB
 constexpr int STAGE_BYTES = 2 * A_CHUNK + B_CHUNK;
-constexpr int STAGES = 2;
-constexpr int THREADS = 128;
+constexpr int STAGES = 3;
+constexpr int THREADS = 256;     // 8 warps: two per TMEM lane quarter in the epilogue
 constexpr long long kWaitCycles = 2000000000ll;  // ~1 s at 2 GHz
 
 // byte offset of element (row, k) inside a chunk laid out as 8x8 core
@@ -159,7 +163,21 @@ __device__ __forceinline__ float finalize(float mAc, float mBc, float mu, float 
 
 __device__ __forceinline__ float canonical_nan_f(float v) { return v != v ? __uint_as_float(0x7fffffffu) : v; }
 
-template <int COMB>
+// variance = mean square - squared mean
+//   FP64SUB:  the subtraction in FP64 (the squared mean is exact in FP64)
+//   else:     error-free FP32 transformation -- p = m*m rounded, e = fma(m, m,
+//             -p) its exact rounding error, v = (ms - p) - e -- which agrees
+//             with the FP64 form to about one ulp at FP32 speed (GB300's FP64
+//             rate is a small fraction of its FP32 rate)
+template <bool FP64SUB>
+__device__ __forceinline__ float variance(float ms, float m) {
+    if (FP64SUB) return (float)fma(-(double)m, (double)m, (double)ms);
+    const float p = m * m;
+    const float e = fmaf(m, m, -p);
+    return (ms - p) - e;
+}
+
+template <int COMB, bool FP64SUB>
 __global__ void __launch_bounds__(THREADS, 1)
 class_stats_kernel(const unsigned char* __restrict__ A1, const unsigned char* __restrict__ A2,
                    const unsigned char* __restrict__ B, int chunks, int G, int num_perms,
@@ -194,27 +212,29 @@ class_stats_kernel(const unsigned char* __restrict__ A1, const unsigned char* __
 
     if (tid == 0) {
         const uint32_t idesc = make_idesc(BM, BN);
-        uint32_t ph_full[STAGES] = {0, 0}, ph_done[STAGES] = {0, 0};
-        int issued = 0;  // chunks whose MMAs were committed
+        uint32_t ph_full[STAGES] = {}, ph_done[STAGES] = {};
         bool ok = true;
-        for (int c = 0; c < chunks && ok; c++) {
-            const int s = c & 1;
-            if (c >= STAGES) {  // the MMAs that read this stage are done
-                ok = mbar_wait(smem_u32(&bar_done[s]), ph_done[s]);
-                ph_done[s] ^= 1;
-                if (!ok) break;
-            }
+        // stage s holds chunk c with c % STAGES == s
+        auto load = [&](int c) {
+            const int s = c % STAGES;
             unsigned char* st = smem + s * STAGE_BYTES;
             const uint32_t bar = smem_u32(&bar_full[s]);
             mbar_expect_tx(bar, STAGE_BYTES);
             bulk_copy(smem_u32(st), A1 + ((size_t)gt * chunks + c) * A_CHUNK, A_CHUNK, bar);
             bulk_copy(smem_u32(st + A_CHUNK), A2 + ((size_t)gt * chunks + c) * A_CHUNK, A_CHUNK, bar);
             bulk_copy(smem_u32(st + 2 * A_CHUNK), B + ((size_t)pt * chunks + c) * B_CHUNK, B_CHUNK, bar);
-            ok = mbar_wait(bar, ph_full[s]);
+        };
+        const int pre = chunks < STAGES ? chunks : STAGES;
+        for (int c = 0; c < pre; c++) load(c);
+        int committed = 0;  // chunks whose MMAs were committed
+        int loaded = pre;   // chunks whose loads were issued
+        for (int c = 0; c < chunks && ok; c++) {
+            const int s = c % STAGES;
+            ok = mbar_wait(smem_u32(&bar_full[s]), ph_full[s]);
             ph_full[s] ^= 1;
             if (!ok) break;
             fence_after();
-            const uint32_t a1 = smem_u32(st), a2 = a1 + A_CHUNK, b = a1 + 2 * A_CHUNK;
+            const uint32_t a1 = smem_u32(smem + s * STAGE_BYTES), a2 = a1 + A_CHUNK, b = a1 + 2 * A_CHUNK;
 #pragma unroll
             for (int kk = 0; kk < BK / 16; kk++) {
                 // K = 16 spans two core matrices along K: LBO = 128 B apart,
@@ -228,13 +248,26 @@ class_stats_kernel(const unsigned char* __restrict__ A1, const unsigned char* __
                 mma_bf16(tmem + BN, da2, db, idesc, acc);
             }
             mma_commit(smem_u32(&bar_done[s]));
-            issued = c + 1;
+            committed = c + 1;
+            // refill the stage of the previous chunk once its MMAs have read it
+            if (c >= 1 && loaded < chunks) {
+                const int sp = (c - 1) % STAGES;
+                ok = mbar_wait(smem_u32(&bar_done[sp]), ph_done[sp]);
+                ph_done[sp] ^= 1;
+                if (!ok) break;
+                load(loaded++);
+            }
         }
-        // wait for the last commit of every stage in use
-        for (int c = (issued > STAGES ? issued - STAGES : 0); c < issued; c++) {
-            const int s = c & 1;
-            if (!mbar_wait(smem_u32(&bar_done[s]), ph_done[s])) ok = false;
-            ph_done[s] ^= 1;
+        // wait for every commit not yet waited for
+        {
+            int waited_upto = 0;  // chunks c < waited_upto had their done-barrier consumed
+            // the refill waits consumed the done phases of chunks 0 .. loaded-STAGES-1
+            waited_upto = loaded - pre;
+            for (int c = waited_upto; c < committed; c++) {
+                const int sd = c % STAGES;
+                if (!mbar_wait(smem_u32(&bar_done[sd]), ph_done[sd])) ok = false;
+                ph_done[sd] ^= 1;
+            }
         }
         if (!ok) {
             failed = 1;
@@ -246,14 +279,16 @@ class_stats_kernel(const unsigned char* __restrict__ A1, const unsigned char* __
     fence_after();
 
     if (!failed) {
-        const int row = warp * 32 + lane;  // TMEM lane = gene within the tile
+        const int quarter = warp & 3;          // TMEM lanes 32*quarter .. +31
+        const int half = warp >> 2;            // column half handled by this warp
+        const int row = quarter * 32 + lane;   // TMEM lane = gene within the tile
         const int g = gt * BM + row;
         const bool gv = g < G;
         const float mu = gv ? gene_mu[g] : 0.f;
         const float t1 = gv ? (float)gene_t1[g] : 0.f, t2 = gv ? (float)gene_t2[g] : 0.f;
         const float inA = 1.f / nA, inB = 1.f / nB;
-        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-        for (int cb = 0; cb < BN / 16; cb++) {
+        const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+        for (int cb = half * (BN / 32); cb < (half + 1) * (BN / 32); cb++) {
             uint32_t va[16], vq[16];
             tmem_ld16(tmem + lane_base + cb * 16, va);
             tmem_ld16(tmem + lane_base + BN + cb * 16, vq);
@@ -267,9 +302,8 @@ class_stats_kernel(const unsigned char* __restrict__ A1, const unsigned char* __
                 const float mBc = (t1 - sA) * inB;
                 const float eA = sA2 * inA;
                 const float eB = (t2 - sA2) * inB;
-                // variance = mean square - squared mean, subtracted in FP64
-                const float vA = (float)fma(-(double)mAc, (double)mAc, (double)eA);
-                const float vB = (float)fma(-(double)mBc, (double)mBc, (double)eB);
+                const float vA = variance<FP64SUB>(eA, mAc);
+                const float vB = variance<FP64SUB>(eB, mBc);
                 const float key = finalize<COMB>(mAc, mBc, mu, vA, vB, nA, nB);
                 if (gv && p < num_perms) keys[(size_t)p * G + g] = canonical_nan_f(key);
             }
@@ -379,10 +413,10 @@ cudaError_t launch_chosen_prepare(const T* X, int G, int S, float* mu, double* t
 template cudaError_t launch_chosen_prepare<float>(const float*, int, int, float*, double*, double*, unsigned char*,
                                                   unsigned char*, cudaStream_t);
 
-cudaError_t launch_chosen_metric(int metric, const uint32_t* masks, int words, int G, int S, int num_perms,
-                                 int64_t nA, int64_t nB, const float* mu, const double* t1, const double* t2,
-                                 const unsigned char* A1, const unsigned char* A2, unsigned char* Bm, float* keys,
-                                 int* error_flag, cudaStream_t st) {
+cudaError_t launch_chosen_metric(int metric, bool fp64_variance, const uint32_t* masks, int words, int G, int S,
+                                 int num_perms, int64_t nA, int64_t nB, const float* mu, const double* t1,
+                                 const double* t2, const unsigned char* A1, const unsigned char* A2,
+                                 unsigned char* Bm, float* keys, int* error_flag, cudaStream_t st) {
     using namespace chosen;
     const int chunks = chosen_chunks(S);
     cudaError_t e = cudaMemsetAsync(Bm, 0, chosen_b_bytes(num_perms, S), st);
@@ -394,7 +428,7 @@ cudaError_t launch_chosen_metric(int metric, const uint32_t* masks, int words, i
     const size_t smem = (size_t)STAGES * STAGE_BYTES;
 #define GSEA_CHOSEN(C)                                                                                        \
     {                                                                                                         \
-        auto kern = class_stats_kernel<C>;                                                                    \
+        auto kern = fp64_variance ? class_stats_kernel<C, true> : class_stats_kernel<C, false>;              \
         e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);               \
         if (e != cudaSuccess) return e;                                                                       \
         kern<<<grid, THREADS, smem, st>>>(A1, A2, Bm, chunks, G, num_perms, mu, t1, t2, (float)nA, (float)nB, \

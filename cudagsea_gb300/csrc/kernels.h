@@ -71,10 +71,10 @@ cudaError_t launch_chosen_prepare(const T* X, int G, int S, float* mu, double* t
                                   unsigned char* A1, unsigned char* A2, cudaStream_t st);
 // per permutation batch: label operand + GEMM + metric epilogue -> keys[p][g];
 // error_flag is set if a bounded wait expired
-cudaError_t launch_chosen_metric(int metric, const uint32_t* masks, int words, int G, int S, int num_perms,
-                                 int64_t nA, int64_t nB, const float* mu, const double* t1, const double* t2,
-                                 const unsigned char* A1, const unsigned char* A2, unsigned char* Bm,
-                                 float* keys, int* error_flag, cudaStream_t st);
+cudaError_t launch_chosen_metric(int metric, bool fp64_variance, const uint32_t* masks, int words, int G, int S,
+                                 int num_perms, int64_t nA, int64_t nB, const float* mu, const double* t1,
+                                 const double* t2, const unsigned char* A1, const unsigned char* A2,
+                                 unsigned char* Bm, float* keys, int* error_flag, cudaStream_t st);
 
 // number of kernel launches issued by the launchers above since the last reset
 int64_t launches_take();

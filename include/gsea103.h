@@ -69,8 +69,10 @@ typedef enum {
 
 /* pipeline form */
 typedef enum {
-    GSEA_FORM_PLAIN = 0,   /* bit-exact SIMT class statistics in the reference's operation order */
-    GSEA_FORM_CHOSEN = 1   /* tensor-core (tcgen05) class statistics, FP64 finalisation          */
+    GSEA_FORM_PLAIN = 0,       /* bit-exact SIMT class statistics in the reference's operation order */
+    GSEA_FORM_CHOSEN = 1,      /* tensor-core (tcgen05) class statistics; variance subtraction as an
+                                  error-free FP32 transformation (FP32 inputs only)               */
+    GSEA_FORM_CHOSEN_FP64 = 2  /* tensor-core class statistics, variance subtraction in FP64      */
 } gsea_form;
 
 typedef struct {

@@ -19,9 +19,9 @@ KEY_RTOL = 1e-4
 NES_ATOL = 1e-4
 
 
-def chosen_run(d, metric, P=None, debug=True):
+def chosen_run(d, metric, P=None, debug=True, form=N.FORM_CHOSEN):
     P = P or d.num_perms
-    plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, P, metric, precision=32, form=N.FORM_CHOSEN)
+    plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, P, metric, precision=32, form=form)
     if debug:
         plan.set_debug(True)
     plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
@@ -59,10 +59,11 @@ def flips_are_near_ties(keys64, order_a, order_b, rel=1e-4):
     return bad
 
 
+@pytest.mark.parametrize("form", [N.FORM_CHOSEN, N.FORM_CHOSEN_FP64], ids=["fp32eft", "fp64"])
 @pytest.mark.parametrize("metric", [0, 1, 2, 6, 8, 9, 12])
-def test_chosen_keys_match_fp64(gpu, metric):
+def test_chosen_keys_match_fp64(gpu, metric, form):
     d = MG.metrics_case()
-    r = chosen_run(d, metric)
+    r = chosen_run(d, metric, form=form)
     k64 = oracle.metric(metric, d.exprs.astype(np.float64), d.labels, d.num_perms, double=True)
     ok = key_close(r["keys"], k64)
     assert ok.all(), (metric, np.abs(r["keys"] - k64)[~ok][:5])
@@ -79,10 +80,11 @@ def test_chosen_sizes(gpu, shape):
     assert flips_are_near_ties(k64, r["order"], o64) == 0
 
 
-def test_chosen_pipeline_vs_fp64_oracle(gpu):
+@pytest.mark.parametrize("form", [N.FORM_CHOSEN, N.FORM_CHOSEN_FP64], ids=["fp32eft", "fp64"])
+def test_chosen_pipeline_vs_fp64_oracle(gpu, form):
     """2,000 x 40, 50 sets, 1,024 permutations: |dNES| <= 1e-4 against FP64."""
     d = synthetic.small()
-    r = chosen_run(d, 8, debug=False)
+    r = chosen_run(d, 8, debug=False, form=form)
     es64, st64 = oracle.gsea(8, d.exprs.astype(np.float64), d.labels, d.set_offsets, d.set_genes, d.num_perms,
                              double=True)
     K = d.num_sets
