@@ -88,6 +88,13 @@ SIGNATURES = [
     ("gsea_plan_set_profiling", ctypes.c_int, [_p, ctypes.c_int]),
     ("gsea_plan_stage_times", ctypes.c_int, [_p, ctypes.POINTER(ctypes.c_double)]),
     ("gsea_stats_device_noalloc", ctypes.c_int, [_p, _i64, _i64, ctypes.c_int, _p, _p]),
+    ("gsea_dataset_load", ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(_p)]),
+    ("gsea_dataset_dims", ctypes.c_int, [_p, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_i64),
+                                         ctypes.POINTER(_i64)]),
+    ("gsea_dataset_arrays", ctypes.c_int, [_p, ctypes.c_int, _p, _p, _p, _p]),
+    ("gsea_dataset_gene", ctypes.c_char_p, [_p, _i64]),
+    ("gsea_dataset_set_name", ctypes.c_char_p, [_p, _i64]),
+    ("gsea_dataset_free", None, [_p]),
     ("gsea_host_alloc", ctypes.c_int, [_sz, ctypes.POINTER(_p)]),
     ("gsea_host_free", ctypes.c_int, [_p]),
     ("gsea_write_es_dump", ctypes.c_int, [ctypes.c_char_p, _p, _i64, _i64, ctypes.c_int, ctypes.c_char_p, _sz]),

@@ -21,6 +21,8 @@ CSRC = os.path.join(PKG, "csrc")
 OBJ = os.path.join(PKG, "_obj")
 LIB_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIB_DIR, "libgsea103.so")
+CLI = os.path.join(LIB_DIR, "gsea103")
+CLI_SRC = os.path.join(CSRC, "cli.cpp")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
@@ -81,6 +83,7 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
     os.makedirs(OBJ, exist_ok=True)
     os.makedirs(LIB_DIR, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
+    srcs = [s for s in srcs if s != CLI_SRC]
     newest_header = max([os.path.getmtime(h) for h in _headers()] + [0.0])
     todo = []
     objs = []
@@ -103,6 +106,16 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}")
         os.replace(tmp, LIB)
+    if (not os.path.exists(CLI) or _foreign(CLI) or os.path.getmtime(CLI) < os.path.getmtime(LIB)
+            or os.path.getmtime(CLI) < os.path.getmtime(CLI_SRC)):
+        tmp = CLI + f".tmp{os.getpid()}"
+        cmd = ["g++"] + CXX_FLAGS + ["-o", tmp, CLI_SRC, "-L" + LIB_DIR, "-lgsea103", "-Wl,-rpath,$ORIGIN"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"cli build failed:\n{r.stdout}")
+        os.replace(tmp, CLI)
     return LIB
 
 

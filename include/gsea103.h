@@ -209,6 +209,25 @@ int gsea_plan_stage_times(gsea_plan plan, double* ms /* [GSEA_NUM_STAGES] */);
 int gsea_stats_device_noalloc(const void* es, int64_t num_sets, int64_t num_perms, int precision,
                               void* stats, void* stream);
 
+/* ---- Broad files (replace read_gct / read_cls / read_gmt,
+ *      src/include/read_data_files.cuh:46-321, and the loader proxies
+ *      src/cudaGSEA_wrapper.cuh:15-25): parse a .gct / .cls / .gmt triple,
+ *      map gene-set symbols to gene indices (unknown dropped, duplicates
+ *      collapsed) and hand out the arrays gsea_run takes.  Parse errors return
+ *      GSEA_ERR_IO with the reference's message in gsea_last_error().       */
+typedef struct gsea_dataset_s* gsea_dataset;
+int gsea_dataset_load(const char* gct_path, const char* cls_path, const char* gmt_path, gsea_dataset* out);
+int gsea_dataset_dims(gsea_dataset ds, int64_t* num_genes, int64_t* num_samples, int64_t* num_sets,
+                      int64_t* num_members);
+/* exprs patient-major in the given precision (32: values parsed as float,
+ * like the reference's single-precision reader; 64: as double); any output
+ * may be NULL */
+int gsea_dataset_arrays(gsea_dataset ds, int precision, void* exprs_pm, uint8_t* labels,
+                        int64_t* set_offsets, int32_t* set_genes);
+const char* gsea_dataset_gene(gsea_dataset ds, int64_t gene);
+const char* gsea_dataset_set_name(gsea_dataset ds, int64_t set);
+void gsea_dataset_free(gsea_dataset ds);
+
 /* pinned (page-locked) host memory for asynchronous copies */
 int gsea_host_alloc(size_t bytes, void** ptr);
 int gsea_host_free(void* ptr);

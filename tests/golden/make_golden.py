@@ -21,6 +21,9 @@ Fixtures (compressed .npz):
   ties_<prec>.npz      integer-valued expressions (many tied metrics),
                        G=300, S=16, K=10, P=32, naive_diff and twopass_s2n
   tiny.npz             37 genes x 5 samples, 3 sets, 3 permutations
+  cli_result_*.txt     "RESULT:" lines of the reference CLI (-cpu) on .gct /
+                       .cls / .gmt files of the 2,000 x 40 workload (256
+                       permutations, twopass_signal2noise)
 """
 from __future__ import annotations
 
@@ -112,6 +115,20 @@ def main():
             out[f"es_{prec}_{m}"] = es
             out[f"stats_{prec}_{m}"] = st
     np.savez_compressed(os.path.join(HERE, "tiny.npz"), **out)
+    # --- the reference CLI on Broad files of the 2,000 x 40 workload (CPU mode)
+    import subprocess
+    import tempfile
+    from cudagsea_gb300 import broad
+    d = synthetic.small(num_perms=256)
+    with tempfile.TemporaryDirectory() as tmp:
+        gct, cls, gmt = broad.write_dataset(os.path.join(tmp, "small"), d)
+        for prec in ("single", "double"):
+            out = subprocess.run([os.path.join(oracle.REF_DIR, "cudaGSEA_cpu"), "-res", gct, "-cls", cls, "-gmx",
+                                  gmt, "-nperm", "256", "-metric", "twopass_signal2noise", "-precision", prec,
+                                  "-cpu"], capture_output=True, text=True, check=True).stdout
+            lines = [l for l in out.splitlines() if l.startswith("RESULT:")]
+            with open(os.path.join(HERE, f"cli_result_{prec}.txt"), "w") as f:
+                f.write("\n".join(lines) + "\n")
     print("golden fixtures written to", HERE)
 
 
