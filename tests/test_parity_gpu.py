@@ -287,3 +287,23 @@ def test_packed_metric_falls_back_on_special_inputs(gpu, value):
         sk, order = check_sort(r["keys"], r["order"], r["ranks"], r["sorted"])
         es_o = oracle.es(sk, order, d.set_offsets, d.set_genes)
         assert H.es_close(r["es"], es_o, False).all()
+
+
+def test_run_sharded_single_rank(gpu, tmp_path):
+    """The shard driver on a one-rank gloo group equals the plain run."""
+    import socket
+    import torch.distributed as dist
+    from cudagsea_gb300.shard import run_sharded
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=0, world_size=1)
+    try:
+        d = MG.metrics_case()
+        es, st = run_sharded(d, d.num_perms)
+        es2, st2 = api.gsea(d.exprs, d.labels, d.set_offsets, d.set_genes, d.num_perms)
+        np.testing.assert_array_equal(es, es2)
+        np.testing.assert_array_equal(st, st2)
+    finally:
+        dist.destroy_process_group()
