@@ -50,6 +50,33 @@ class Config(ctypes.Structure):
     ]
 
 
+class AdaptiveParams(ctypes.Structure):
+    _fields_ = [
+        ("pilot_perms", ctypes.c_int64),
+        ("growth", ctypes.c_double),
+        ("z", ctypes.c_double),
+        ("q_call", ctypes.c_double),
+        ("margin", ctypes.c_double),
+        ("p_floor", ctypes.c_double),
+        ("prior_cap", ctypes.c_double),
+        ("fallback_tol", ctypes.c_double),
+    ]
+
+
+class AdaptiveReport(ctypes.Structure):
+    _fields_ = [
+        ("rounds", ctypes.c_int64),
+        ("scores", ctypes.c_int64),
+        ("stopped_pilot", ctypes.c_int64),
+        ("full_sets", ctypes.c_int64),
+        ("stop_p", ctypes.c_double),
+        ("model_used", ctypes.c_int32),
+        ("model_mean_err", ctypes.c_double),
+    ]
+
+
+MODEL_INPUTS, MODEL_HIDDEN, MODEL_OUTPUTS, MODEL_PARAMS, MODEL_NORMS = 5, 64, 2, 4674, 15
+
 _lib: Optional[ctypes.CDLL] = None
 _p = ctypes.c_void_p
 _i64 = ctypes.c_int64
@@ -88,6 +115,21 @@ SIGNATURES = [
     ("gsea_plan_set_profiling", ctypes.c_int, [_p, ctypes.c_int]),
     ("gsea_plan_stage_times", ctypes.c_int, [_p, ctypes.POINTER(ctypes.c_double)]),
     ("gsea_stats_device_noalloc", ctypes.c_int, [_p, _i64, _i64, ctypes.c_int, _p, _p]),
+    ("gsea_model_create", ctypes.c_int, [ctypes.c_uint32, ctypes.c_int, ctypes.POINTER(_p)]),
+    ("gsea_model_destroy", ctypes.c_int, [_p]),
+    ("gsea_model_get", ctypes.c_int, [_p, _p, _p]),
+    ("gsea_model_set", ctypes.c_int, [_p, _p, _p]),
+    ("gsea_model_predict", ctypes.c_int, [_p, _p, _i64, _p, _p]),
+    ("gsea_model_loss_grad", ctypes.c_int, [_p, _p, _p, _i64, _p, _p, _p]),
+    ("gsea_model_train", ctypes.c_int, [_p, _p, _p, _i64, ctypes.c_int, ctypes.c_int, ctypes.c_float, _p]),
+    ("gsea_model_calibrate", ctypes.c_int, [_p, _p, _p, _i64]),
+    ("gsea_plan_model_samples", ctypes.c_int, [_p, ctypes.c_int, ctypes.c_int, _p, _p, ctypes.POINTER(_i64), _p, _p,
+                                               ctypes.POINTER(_i64)]),
+    ("gsea_adaptive_params_init", None, [ctypes.POINTER(AdaptiveParams)]),
+    ("gsea_plan_execute_adaptive", ctypes.c_int, [_p, _p, ctypes.POINTER(AdaptiveParams), _p,
+                                                  ctypes.POINTER(AdaptiveReport)]),
+    ("gsea_adaptive_decide", ctypes.c_int, [_i64, _p, _p, _p, _p, ctypes.c_double, ctypes.c_double, _p]),
+    ("gsea_stats_ragged", ctypes.c_int, [_p, _i64, _i64, _p, _i64, ctypes.c_int, _p, _p]),
     ("gsea_dataset_load", ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(_p)]),
     ("gsea_dataset_dims", ctypes.c_int, [_p, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_i64),
                                          ctypes.POINTER(_i64)]),

@@ -21,6 +21,7 @@
 
 #include "../../include/gsea103.h"
 #include "kernels.h"
+#include "plan.h"
 
 namespace gsea {
 static std::atomic<long long> g_launches{0};
@@ -31,25 +32,8 @@ void launches_add(int64_t n) { g_launches.fetch_add(n); }
 namespace {
 
 thread_local std::string t_error;
-
-int fail(int status, const std::string& msg) {
-    t_error = msg;
-    return status;
-}
-
-int cuda_fail(cudaError_t e, const char* what) {
-    if (e == cudaErrorMemoryAllocation)
-        return fail(GSEA_ERR_OUT_OF_MEMORY, std::string(what) + ": " + cudaGetErrorString(e));
-    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
-        return fail(GSEA_ERR_NO_DEVICE, std::string(what) + ": " + cudaGetErrorString(e));
-    return fail(GSEA_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
-}
-
-#define GSEA_CUDA(call, what)                        \
-    do {                                             \
-        cudaError_t e_ = (call);                     \
-        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
-    } while (0)
+using gsea::fail;
+using gsea::cuda_fail;
 
 // Host-side fault injection for the error paths: GSEA_FAULT=alloc|launch|d2h
 // makes the matching step of the next call fail with GSEA_ERR_INJECTED.  No
@@ -74,54 +58,6 @@ namespace gsea {
 void set_last_error(const char* msg) { t_error = msg ? msg : ""; }
 }  // namespace gsea
 
-struct gsea_plan_s {
-    gsea_config cfg;
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    size_t tsize = 4;
-    int words = 0;
-    int64_t pb = 0;  // permutations per batch
-    bool ranks16 = true;
-    bool debug = false;
-    bool inputs_set = false;
-    int64_t nA = 0, nB = 0;
-    int64_t nnz = 0, nnz_cap = 0;
-    int64_t last_launches = 0;
-    // device buffers
-    void* exprs = nullptr;
-    uint8_t* labels = nullptr;
-    int64_t* set_off = nullptr;
-    int32_t* set_genes = nullptr;
-    int32_t* set_order = nullptr;      // sets by decreasing size, for the ES kernel
-    std::vector<int32_t> h_set_order;  // host staging of set_order
-    uint32_t* masks = nullptr;
-    int* fast_ok = nullptr;            // expression values allow the packed metric form
-    void* decay = nullptr;             // [G+1] T: miss step per hit count
-    // chosen form (tensor-core class statistics)
-    float* gene_mu = nullptr;
-    double* gene_t1 = nullptr;
-    double* gene_t2 = nullptr;
-    unsigned char* opA1 = nullptr;
-    unsigned char* opA2 = nullptr;
-    unsigned char* opB = nullptr;
-    int* dev_error = nullptr;          // set by kernels whose bounded waits expired
-    void* keys = nullptr;
-    void* ranks = nullptr;
-    void* sorted = nullptr;
-    uint32_t* order = nullptr;
-    void* sort_scratch = nullptr;
-    size_t sort_scratch_bytes = 0;
-    void* es = nullptr;
-    void* stats = nullptr;
-    void* stats_scratch = nullptr;
-    size_t stats_scratch_bytes = 0;
-    // stage timing (gsea_plan_set_profiling): events recorded at every stage
-    // boundary of the last execute, tagged with the stage they close
-    bool profile = false;
-    std::vector<cudaEvent_t> events;
-    std::vector<int> event_stage;
-    size_t events_used = 0;
-};
 
 namespace {
 
@@ -163,7 +99,8 @@ int mark(gsea_plan_s* p, int stage, cudaStream_t st) {
 void free_plan_buffers(gsea_plan_s* p) {
     void* bufs[] = {p->exprs, p->labels, p->set_off, p->set_genes, p->set_order, p->masks, p->fast_ok, p->decay, p->gene_mu,
                     p->gene_t1, p->gene_t2, p->opA1, p->opA2, p->opB, p->dev_error, p->keys,
-                    p->ranks, p->sorted, p->order, p->sort_scratch, p->es, p->stats, p->stats_scratch};
+                    p->ranks, p->sorted, p->order, p->sort_scratch, p->es, p->stats, p->stats_scratch,
+                    p->moments, p->active, p->counts, p->exceed, p->sumabs, p->feat, p->pred};
     for (void* b : bufs)
         if (b) cudaFree(b);
     p->exprs = p->labels = nullptr;
@@ -180,6 +117,12 @@ void free_plan_buffers(gsea_plan_s* p) {
     p->keys = p->ranks = p->sorted = nullptr;
     p->order = nullptr;
     p->sort_scratch = p->es = p->stats = p->stats_scratch = nullptr;
+    p->moments = nullptr;
+    p->active = nullptr;
+    p->counts = nullptr;
+    p->exceed = nullptr;
+    p->sumabs = nullptr;
+    p->feat = p->pred = nullptr;
 }
 
 template <class Ptr>
@@ -222,7 +165,11 @@ int upload_sets(gsea_plan_s* p, const int64_t* off, const int32_t* genes, cudaSt
     p->nnz = nnz;
     // largest sets first: the ES kernel's warps take sets in this order
     p->h_set_order.resize((size_t)K);
-    for (int64_t k = 0; k < K; k++) p->h_set_order[k] = (int32_t)k;
+    p->h_set_size.resize((size_t)K);
+    for (int64_t k = 0; k < K; k++) {
+        p->h_set_order[k] = (int32_t)k;
+        p->h_set_size[k] = off[k + 1] - off[k];
+    }
     std::stable_sort(p->h_set_order.begin(), p->h_set_order.end(),
                      [off](int32_t x, int32_t y) { return off[x + 1] - off[x] > off[y + 1] - off[y]; });
     if (async) {
@@ -282,12 +229,10 @@ int check_device_error(gsea_plan_s* p) {
 }
 
 template <class T>
-int execute_t(gsea_plan_s* p, cudaStream_t st) {
+int run_range_t(gsea_plan_s* p, cudaStream_t st, int64_t lo, int64_t hi, const int32_t* set_list, int n_sets) {
     const gsea_config& c = p->cfg;
-    const int G = (int)c.num_genes, S = (int)c.num_samples, K = (int)c.num_sets;
+    const int G = (int)c.num_genes, S = (int)c.num_samples;
     const int64_t P = c.num_perms;
-    if (injected("launch")) return fail(GSEA_ERR_INJECTED, "injected launch failure");
-    gsea::launches_take();
     gsea::SortBuffers sb;
     sb.ranks = p->ranks;
     sb.ranks16 = p->ranks16;
@@ -295,11 +240,9 @@ int execute_t(gsea_plan_s* p, cudaStream_t st) {
     sb.order = p->debug ? p->order : nullptr;
     sb.scratch = p->sort_scratch;
     sb.scratch_bytes = p->sort_scratch_bytes;
-    p->events_used = 0;
-    int rc = mark(p, -1, st);
-    if (rc) return rc;
-    for (int64_t b0 = 0; b0 < P; b0 += p->pb) {
-        const int nb = (int)(P - b0 < p->pb ? P - b0 : p->pb);
+    int rc;
+    for (int64_t b0 = lo; b0 < hi; b0 += p->pb) {
+        const int nb = (int)(hi - b0 < p->pb ? hi - b0 : p->pb);
         GSEA_CUDA(gsea::launch_permute(p->labels, S, nb, c.perm_offset + b0, c.seed, p->masks, p->words, st),
                   "permute kernel");
         if ((rc = mark(p, 0, st))) return rc;
@@ -319,11 +262,25 @@ int execute_t(gsea_plan_s* p, cudaStream_t st) {
                   "sort kernel");
         if ((rc = mark(p, 2, st))) return rc;
         GSEA_CUDA(gsea::launch_es<T>(p->ranks, p->ranks16, static_cast<const T*>(p->sorted), G, nb, p->set_off,
-                                     p->set_genes, p->set_order, static_cast<const T*>(p->decay), K,
+                                     p->set_genes, set_list, static_cast<const T*>(p->decay), n_sets,
                                      static_cast<T*>(p->es), P, b0, st),
                   "enrichment kernel");
         if ((rc = mark(p, 3, st))) return rc;
     }
+    return GSEA_OK;
+}
+
+template <class T>
+int execute_t(gsea_plan_s* p, cudaStream_t st) {
+    const gsea_config& c = p->cfg;
+    const int K = (int)c.num_sets;
+    const int64_t P = c.num_perms;
+    if (injected("launch")) return fail(GSEA_ERR_INJECTED, "injected launch failure");
+    gsea::launches_take();
+    p->events_used = 0;
+    int rc = mark(p, -1, st);
+    if (rc) return rc;
+    if ((rc = run_range_t<T>(p, st, 0, P, p->set_order, K))) return rc;
     GSEA_CUDA(gsea::launch_stats<T>(static_cast<const T*>(p->es), K, P, static_cast<T*>(p->stats),
                                     p->stats_scratch, st),
               "statistics kernels");
@@ -351,6 +308,15 @@ int write_dump(const char* prefix, const void* es, int64_t K, int64_t P, int pre
 }
 
 }  // namespace
+
+namespace gsea {
+int plan_run_range(gsea_plan_s* p, cudaStream_t st, int64_t lo, int64_t hi, const int32_t* set_list, int n_sets) {
+    if (injected("launch")) return fail(GSEA_ERR_INJECTED, "injected launch failure");
+    return p->cfg.precision == 64 ? run_range_t<double>(p, st, lo, hi, set_list, n_sets)
+                                  : run_range_t<float>(p, st, lo, hi, set_list, n_sets);
+}
+int plan_dev_alloc(void** ptr, size_t bytes, const char* what) { return dev_alloc(ptr, bytes, what); }
+}  // namespace gsea
 
 extern "C" {
 

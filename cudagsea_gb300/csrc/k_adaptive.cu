@@ -1,0 +1,245 @@
+// k_adaptive.cu -- device helpers of the learned permutation allocator: metric
+// moments, per-set null statistics, training samples, features and the
+// exceedance counts of the sequential stopping rule.  No counterpart in the
+// reference.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace gsea {
+namespace {
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(kFullMask, v, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    double r = 0.0;
+    for (int w = 0; w < nw; w++) r += sh[w];
+    return r;
+}
+
+// moments[0..4] = mean, sd, skewness of the finite keys; mean and sd of |key|
+template <class T>
+__global__ void __launch_bounds__(1024) moments_kernel(const T* __restrict__ keys, int G, double* __restrict__ out) {
+    __shared__ double sh[32];
+    double n = 0, s1 = 0, a1 = 0;
+    for (int g = threadIdx.x; g < G; g += blockDim.x) {
+        const double v = (double)keys[g];
+        if (isfinite(v)) {
+            n += 1.0;
+            s1 += v;
+            a1 += fabs(v);
+        }
+    }
+    n = block_sum(n, sh);
+    s1 = block_sum(s1, sh);
+    a1 = block_sum(a1, sh);
+    const double mean = n > 0 ? s1 / n : 0.0, amean = n > 0 ? a1 / n : 0.0;
+    double c2 = 0, c3 = 0, d2 = 0;
+    for (int g = threadIdx.x; g < G; g += blockDim.x) {
+        const double v = (double)keys[g];
+        if (isfinite(v)) {
+            const double c = v - mean, d = fabs(v) - amean;
+            c2 += c * c;
+            c3 += c * c * c;
+            d2 += d * d;
+        }
+    }
+    c2 = block_sum(c2, sh);
+    c3 = block_sum(c3, sh);
+    d2 = block_sum(d2, sh);
+    if (threadIdx.x == 0) {
+        const double var = n > 0 ? c2 / n : 0.0, sd = sqrt(var);
+        out[0] = mean;
+        out[1] = sd;
+        out[2] = sd > 0 ? (c3 / n) / (var * sd) : 0.0;
+        out[3] = amean;
+        out[4] = n > 0 ? sqrt(d2 / n) : 0.0;
+    }
+}
+
+// mean |ES| of every set over columns [0, P)
+template <class T>
+__global__ void set_means_kernel(const T* __restrict__ es, int64_t ld, int64_t P, double* __restrict__ means) {
+    __shared__ double sh[32];
+    const int64_t k = blockIdx.x;
+    double a = 0.0;
+    for (int64_t p = threadIdx.x; p < P; p += blockDim.x) a += fabs((double)es[k * ld + p]);
+    a = block_sum(a, sh);
+    if (threadIdx.x == 0) means[k] = a / (double)P;
+}
+
+__device__ __forceinline__ void features(float* x, double nk, double u, const double* mom) {
+    const double n = nk > 1.0 ? nk : 1.0;
+    x[0] = (float)log(n);
+    x[1] = (float)(u * sqrt(n));
+    x[2] = (float)(mom[1] > 0 ? mom[0] / mom[1] : 0.0);
+    x[3] = (float)mom[2];
+    x[4] = (float)(mom[3] > 0 ? mom[4] / mom[3] : 0.0);
+}
+
+constexpr int kMaxQueries = 24;
+
+// Block per set with slot[k] != -1: queries thresholds u_j = m_k 0.25 1.25^j
+// and the observed |ES_k|; targets = fraction of the P columns with
+// |ES| >= u, log m_k.  slot[k] >= 0: sample rows slot[k] .. of (x, t);
+// slot[k] <= -2: rows -(slot[k] + 2) .. of (xv, tv).
+template <class T>
+__global__ void __launch_bounds__(256) model_samples_kernel(const T* __restrict__ es, int64_t ld, int64_t P,
+                                                            const int64_t* __restrict__ off,
+                                                            const double* __restrict__ mom,
+                                                            const double* __restrict__ means, int queries,
+                                                            const int64_t* __restrict__ slot, float* __restrict__ x,
+                                                            float* __restrict__ t, float* __restrict__ xv,
+                                                            float* __restrict__ tv) {
+    __shared__ unsigned cnt[kMaxQueries + 1];
+    const int64_t k = blockIdx.x;
+    const int64_t sl = slot[k];
+    if (sl == -1) return;
+    const double m = means[k];
+    const T* row = es + k * ld;
+    const double obs = fabs((double)row[0]);
+    double u[kMaxQueries + 1];
+    double f = 0.25;
+#pragma unroll
+    for (int j = 0; j < kMaxQueries; j++) {
+        u[j] = m * f;
+        f *= 1.25;
+    }
+    u[kMaxQueries] = obs;
+    unsigned c[kMaxQueries + 1];
+#pragma unroll
+    for (int j = 0; j <= kMaxQueries; j++) c[j] = 0;
+    if (threadIdx.x <= kMaxQueries) cnt[threadIdx.x] = 0;
+    __syncthreads();
+    for (int64_t p = threadIdx.x; p < P; p += blockDim.x) {
+        const double v = fabs((double)row[p]);
+#pragma unroll
+        for (int j = 0; j <= kMaxQueries; j++) c[j] += v >= u[j];
+    }
+#pragma unroll
+    for (int j = 0; j <= kMaxQueries; j++) {
+        unsigned v = c[j];
+        for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(kFullMask, v, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(&cnt[j], v);
+    }
+    __syncthreads();
+    const int nq = queries + 1;
+    if (threadIdx.x < nq) {
+        const int j = threadIdx.x < queries ? threadIdx.x : kMaxQueries;
+        const int64_t row_out = (sl >= 0 ? sl : -(sl + 2)) + threadIdx.x;
+        float* xo = (sl >= 0 ? x : xv) + row_out * 5;
+        float* to = (sl >= 0 ? t : tv) + row_out * 2;
+        features(xo, (double)(off[k + 1] - off[k]), u[j], mom);
+        to[0] = (float)((double)cnt[j] / (double)P);
+        to[1] = (float)log(m);
+    }
+}
+
+// features of every set at its observed score
+template <class T>
+__global__ void model_features_kernel(const T* __restrict__ es, int64_t ld, const int64_t* __restrict__ off, int K,
+                                      const double* __restrict__ mom, float* __restrict__ x) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= K) return;
+    features(x + (int64_t)k * 5, (double)(off[k + 1] - off[k]), fabs((double)es[(int64_t)k * ld]), mom);
+}
+
+// warp per listed set: exceed[k] += #{p in [lo, hi): |S_kp| >= |S_k0|},
+// sumabs[k] += sum |S_kp|
+template <class T>
+__global__ void exceed_kernel(const T* __restrict__ es, int64_t ld, const int32_t* __restrict__ list, int n_list,
+                              int64_t lo, int64_t hi, unsigned long long* __restrict__ exceed,
+                              double* __restrict__ sumabs) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= n_list) return;
+    const int64_t k = list ? list[warp] : warp;
+    const T* row = es + k * ld;
+    const T a0 = fabs(row[0]);
+    unsigned long long c = 0;
+    double s = 0.0;
+    for (int64_t p = lo + lane; p < hi; p += 32) {
+        const T a = fabs(row[p]);
+        c += a >= a0;
+        s += (double)a;
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        c += __shfl_xor_sync(kFullMask, c, o);
+        s += __shfl_xor_sync(kFullMask, s, o);
+    }
+    if (lane == 0) {
+        exceed[k] += c;
+        sumabs[k] += s;
+    }
+}
+
+}  // namespace
+
+template <class T>
+cudaError_t launch_moments(const T* keys, int G, double* moments, cudaStream_t st) {
+    moments_kernel<T><<<1, 1024, 0, st>>>(keys, G, moments);
+    launches_add(1);
+    return cudaGetLastError();
+}
+template cudaError_t launch_moments<float>(const float*, int, double*, cudaStream_t);
+template cudaError_t launch_moments<double>(const double*, int, double*, cudaStream_t);
+
+template <class T>
+cudaError_t launch_set_means(const T* es, int64_t ld, int64_t P, int K, double* means, cudaStream_t st) {
+    if (K <= 0) return cudaSuccess;
+    set_means_kernel<T><<<K, 256, 0, st>>>(es, ld, P, means);
+    launches_add(1);
+    return cudaGetLastError();
+}
+template cudaError_t launch_set_means<float>(const float*, int64_t, int64_t, int, double*, cudaStream_t);
+template cudaError_t launch_set_means<double>(const double*, int64_t, int64_t, int, double*, cudaStream_t);
+
+int model_max_queries() { return kMaxQueries; }
+
+template <class T>
+cudaError_t launch_model_samples(const T* es, int64_t ld, int64_t P, const int64_t* off, int K, const double* mom,
+                                 const double* means, int queries, const int64_t* slot, float* x, float* t,
+                                 float* xv, float* tv, cudaStream_t st) {
+    if (K <= 0) return cudaSuccess;
+    if (queries < 1 || queries > kMaxQueries) return cudaErrorInvalidValue;
+    model_samples_kernel<T><<<K, 256, 0, st>>>(es, ld, P, off, mom, means, queries, slot, x, t, xv, tv);
+    launches_add(1);
+    return cudaGetLastError();
+}
+template cudaError_t launch_model_samples<float>(const float*, int64_t, int64_t, const int64_t*, int, const double*,
+                                                 const double*, int, const int64_t*, float*, float*, float*, float*,
+                                                 cudaStream_t);
+template cudaError_t launch_model_samples<double>(const double*, int64_t, int64_t, const int64_t*, int, const double*,
+                                                  const double*, int, const int64_t*, float*, float*, float*, float*,
+                                                  cudaStream_t);
+
+template <class T>
+cudaError_t launch_model_features(const T* es, int64_t ld, const int64_t* off, int K, const double* mom, float* x,
+                                  cudaStream_t st) {
+    if (K <= 0) return cudaSuccess;
+    model_features_kernel<T><<<(K + 255) / 256, 256, 0, st>>>(es, ld, off, K, mom, x);
+    launches_add(1);
+    return cudaGetLastError();
+}
+template cudaError_t launch_model_features<float>(const float*, int64_t, const int64_t*, int, const double*, float*,
+                                                  cudaStream_t);
+template cudaError_t launch_model_features<double>(const double*, int64_t, const int64_t*, int, const double*, float*,
+                                                   cudaStream_t);
+
+template <class T>
+cudaError_t launch_exceed(const T* es, int64_t ld, const int32_t* list, int n_list, int64_t lo, int64_t hi,
+                          unsigned long long* exceed, double* sumabs, cudaStream_t st) {
+    if (n_list <= 0 || hi <= lo) return cudaSuccess;
+    exceed_kernel<T><<<(n_list + 7) / 8, 256, 0, st>>>(es, ld, list, n_list, lo, hi, exceed, sumabs);
+    launches_add(1);
+    return cudaGetLastError();
+}
+template cudaError_t launch_exceed<float>(const float*, int64_t, const int32_t*, int, int64_t, int64_t,
+                                          unsigned long long*, double*, cudaStream_t);
+template cudaError_t launch_exceed<double>(const double*, int64_t, const int32_t*, int, int64_t, int64_t,
+                                           unsigned long long*, double*, cudaStream_t);
+
+}  // namespace gsea

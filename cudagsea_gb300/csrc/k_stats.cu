@@ -17,6 +17,13 @@
 // against the null of permutations 1..P-1 of all sets, per sign side:
 //   NES* > 0: q = [#{null >= NES*} / #{null >= 0}] / [#{obs >= NES*} / #{obs >= 0}]
 //   NES* <= 0: mirrored with <=, capped at 1.
+//
+// Ragged form (adaptive permutation allocation): set k holds n_k scores in
+// row k of a matrix with row stride ld.  fac, NES and NP use the set's own
+// n_k columns; FWER uses the first p_fwer columns (those every set has);
+// in the FDR null every set carries the same total weight, each of its
+// n_k - 1 null scores counting (ld - 1) / (n_k - 1).  With n_k = ld for all
+// sets the weights are exactly 1 and the ragged form is the dense one.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -25,7 +32,7 @@ namespace {
 
 struct StatsScratch {
     // fac[K] mx[P] mn[P] (T) | cnt_obs[K] lcount[K] (u64) | sorted_pos[K]
-    // sorted_neg[K] (T) | hpos[K+2] hneg[K+2] totals[8] (u64)
+    // sorted_neg[K] (T) | hpos[K+2] hneg[K+2] (f64) | totals[8] (u64 / f64)
     static size_t bytes(int K, int64_t P, size_t tsize) {
         return tsize * ((size_t)3 * K + 2 * (size_t)P) + sizeof(unsigned long long) * (4 * (size_t)K + 12) + 64;
     }
@@ -33,11 +40,12 @@ struct StatsScratch {
 
 // one warp per set: factor, NES, NP
 template <class T>
-__global__ void stats_set_kernel(const T* __restrict__ es, int K, int64_t P, T* __restrict__ out,
-                                 T* __restrict__ fac) {
+__global__ void stats_set_kernel(const T* __restrict__ es, int K, int64_t ld, const int64_t* __restrict__ counts,
+                                 T* __restrict__ out, T* __restrict__ fac) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= K) return;
-    const T* row = es + (int64_t)warp * P;
+    const T* row = es + (int64_t)warp * ld;
+    const int64_t P = counts ? counts[warp] : ld;
     const T es0 = row[0];
     T sum = T(0);
     unsigned long long np = 0;
@@ -72,7 +80,7 @@ __global__ void stats_set_kernel(const T* __restrict__ es, int K, int64_t P, T* 
 // max) and all-ones ("empty" for the min) belong only to NaN bit patterns.
 constexpr int kExtremaSets = 16;
 template <class T>
-__global__ void stats_extrema_kernel(const T* __restrict__ es, int K, int64_t P, const T* __restrict__ fac,
+__global__ void stats_extrema_kernel(const T* __restrict__ es, int K, int64_t ld, int64_t P, const T* __restrict__ fac,
                                      typename RadixKey<T>::U* __restrict__ mx,
                                      typename RadixKey<T>::U* __restrict__ mn) {
     using U = typename RadixKey<T>::U;
@@ -81,7 +89,7 @@ __global__ void stats_extrema_kernel(const T* __restrict__ es, int K, int64_t P,
     const int k0 = blockIdx.y * kExtremaSets, k1 = min(K, k0 + kExtremaSets);
     T hi = -INFINITY, lo = INFINITY;
     for (int k = k0; k < k1; k++) {
-        const T v = Exact<T>::mul(es[(int64_t)k * P + p], fac[k]);
+        const T v = Exact<T>::mul(es[(int64_t)k * ld + p], fac[k]);
         hi = hi < v ? v : hi;
         lo = lo > v ? v : lo;
     }
@@ -135,7 +143,8 @@ __global__ void stats_fwer_kernel(int K, int64_t P, const typename RadixKey<T>::
 //      satisfies v >= key* exactly when t(v) >= L + 1).
 // Layout of the FDR part of the scratch (unsigned long long):
 //   cnt_obs[K] | L[K] | sorted_pos[K] (T) | sorted_neg[K] (T) |
-//   H_pos[K+2] | H_neg[K+2] | totals[8]
+//   H_pos[K+2] | H_neg[K+2] (double weights) | totals[8]: [2], [3] observed
+//   counts per side (u64), [4], [5] null weight per side (double)
 
 template <class T>
 __device__ __forceinline__ int side_of(T s) { return s > T(0) ? 0 : (s <= T(0) ? 1 : -1); }
@@ -192,26 +201,35 @@ __device__ __forceinline__ unsigned upper_bound_t(const T* a, unsigned n, T v) {
 }
 
 constexpr int kHistThreads = 256;
+constexpr int kHistCols = kHistThreads * 8;  // null columns per block
+// grid (K, column chunks): block (k, c) bins the null scores of set k in the
+// chunks c, c + gridDim.y, ... of kHistCols columns of its columns 1..n_k-1
 template <class T>
 __global__ void __launch_bounds__(kHistThreads)
-stats_fdr_hist_kernel(const T* __restrict__ es, int K, int64_t P, const T* __restrict__ fac,
-                      const T* __restrict__ sorted_pos, const T* __restrict__ sorted_neg,
-                      unsigned long long* __restrict__ hpos, unsigned long long* __restrict__ hneg,
-                      unsigned long long* __restrict__ totals) {
+stats_fdr_hist_kernel(const T* __restrict__ es, int64_t ld, const int64_t* __restrict__ counts,
+                      const T* __restrict__ fac, const T* __restrict__ sorted_pos, const T* __restrict__ sorted_neg,
+                      double* __restrict__ hpos, double* __restrict__ hneg, unsigned long long* __restrict__ totals) {
+    const int64_t k = blockIdx.x;
+    const int64_t n = counts ? counts[k] : ld;
+    if (n < 2) return;
+    const double w = counts ? (double)(ld - 1) / (double)(n - 1) : 1.0;
     const unsigned npos = (unsigned)totals[2], nneg = (unsigned)totals[3];
-    const int64_t total = (int64_t)K * (P - 1);
-    unsigned long long cpos = 0, cneg = 0;
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
-         q += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t k = q / (P - 1), p = 1 + q % (P - 1);
-        const T v = Exact<T>::mul(es[k * P + p], fac[k]);
-        if (v >= T(0)) {
-            cpos++;
-            atomicAdd(&hpos[upper_bound_t(sorted_pos, npos, v)], 1ull);
-        }
-        if (v <= T(0)) {
-            cneg++;
-            atomicAdd(&hneg[upper_bound_t(sorted_neg, nneg, -v)], 1ull);
+    const T f = fac[k];
+    const T* row = es + k * ld;
+    double* wtot = reinterpret_cast<double*>(totals + 4);
+    double cpos = 0.0, cneg = 0.0;
+    for (int64_t c0 = 1 + (int64_t)blockIdx.y * kHistCols; c0 < n; c0 += (int64_t)gridDim.y * kHistCols) {
+        const int64_t c1 = c0 + kHistCols < n ? c0 + kHistCols : n;
+        for (int64_t p = c0 + threadIdx.x; p < c1; p += kHistThreads) {
+            const T v = Exact<T>::mul(row[p], f);
+            if (v >= T(0)) {
+                cpos += w;
+                atomicAdd(&hpos[upper_bound_t(sorted_pos, npos, v)], w);
+            }
+            if (v <= T(0)) {
+                cneg += w;
+                atomicAdd(&hneg[upper_bound_t(sorted_neg, nneg, -v)], w);
+            }
         }
     }
     for (int o = 16; o >= 1; o >>= 1) {
@@ -219,37 +237,37 @@ stats_fdr_hist_kernel(const T* __restrict__ es, int K, int64_t P, const T* __res
         cneg += __shfl_xor_sync(kFullMask, cneg, o);
     }
     if ((threadIdx.x & 31) == 0) {
-        if (cpos) atomicAdd(&totals[0], cpos);
-        if (cneg) atomicAdd(&totals[1], cneg);
+        if (cpos != 0.0) atomicAdd(&wtot[0], cpos);
+        if (cneg != 0.0) atomicAdd(&wtot[1], cneg);
     }
 }
 
 // in-place suffix sums of the two histograms (one block each)
-__global__ void stats_fdr_suffix_kernel(unsigned long long* __restrict__ hpos, unsigned long long* __restrict__ hneg,
+__global__ void stats_fdr_suffix_kernel(double* __restrict__ hpos, double* __restrict__ hneg,
                                         const unsigned long long* __restrict__ totals) {
-    unsigned long long* h = blockIdx.x == 0 ? hpos : hneg;
+    double* h = blockIdx.x == 0 ? hpos : hneg;
     const unsigned n = (unsigned)totals[2 + blockIdx.x] + 1;  // bins 0..m
-    __shared__ unsigned long long carry;
-    __shared__ unsigned long long wsum[32];
-    if (threadIdx.x == 0) carry = 0;
+    __shared__ double carry;
+    __shared__ double wsum[32];
+    if (threadIdx.x == 0) carry = 0.0;
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     // walk from the top bin down in chunks of blockDim.x
     for (int64_t top = (int64_t)n - 1; top >= 0; top -= blockDim.x) {
         const int64_t i = top - threadIdx.x;
-        unsigned long long v = i >= 0 ? h[i] : 0ull;
+        double v = i >= 0 ? h[i] : 0.0;
         for (int o = 1; o < 32; o <<= 1) {
-            const unsigned long long y = __shfl_up_sync(kFullMask, v, o);
+            const double y = __shfl_up_sync(kFullMask, v, o);
             if (lane >= o) v += y;
         }
         if (lane == 31) wsum[warp] = v;
         __syncthreads();
-        unsigned long long before = carry;
+        double before = carry;
         for (int w = 0; w < warp; w++) before += wsum[w];
         if (i >= 0) h[i] = v + before;
         __syncthreads();
         if (threadIdx.x == 0) {
-            unsigned long long t = 0;
+            double t = 0.0;
             for (int w = 0; w < nw; w++) t += wsum[w];
             carry += t;
         }
@@ -260,8 +278,7 @@ __global__ void stats_fdr_suffix_kernel(unsigned long long* __restrict__ hpos, u
 template <class T>
 __global__ void stats_fdr_final_kernel(int K, const unsigned long long* __restrict__ cnt_obs,
                                        const unsigned long long* __restrict__ lcount,
-                                       const unsigned long long* __restrict__ spos,
-                                       const unsigned long long* __restrict__ sneg,
+                                       const double* __restrict__ spos, const double* __restrict__ sneg,
                                        const unsigned long long* __restrict__ totals, T* __restrict__ out) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= K) return;
@@ -273,10 +290,11 @@ __global__ void stats_fdr_final_kernel(int K, const unsigned long long* __restri
         const bool up = s > T(0);
         const unsigned long long L = lcount[k];
         const unsigned long long m = up ? totals[2] : totals[3];
-        const unsigned long long c_null = L + 1 <= m ? (up ? spos : sneg)[L + 1] : 0ull;
-        const double null_side = (double)(up ? totals[0] : totals[1]);
+        const double* wtot = reinterpret_cast<const double*>(totals + 4);
+        const double c_null = L + 1 <= m ? (up ? spos : sneg)[L + 1] : 0.0;
+        const double null_side = up ? wtot[0] : wtot[1];
         const double obs_side = (double)m;
-        const double fn = null_side > 0 ? (double)c_null / null_side : 0.0;
+        const double fn = null_side > 0 ? c_null / null_side : 0.0;
         const double fo = (double)cnt_obs[k] / obs_side;
         const double r = fn / fo;
         q = (T)(r < 1.0 ? r : 1.0);
@@ -294,44 +312,57 @@ template size_t stats_scratch_bytes<float>(int, int64_t);
 template size_t stats_scratch_bytes<double>(int, int64_t);
 
 template <class T>
-cudaError_t launch_stats(const T* es, int K, int64_t P, T* stats, void* scratch, cudaStream_t st) {
-    if (K <= 0 || P <= 0) return cudaSuccess;
+cudaError_t launch_stats_ragged(const T* es, int K, int64_t ld, const int64_t* counts, int64_t p_fwer, T* stats,
+                                void* scratch, cudaStream_t st) {
+    if (K <= 0 || ld <= 0 || p_fwer <= 0 || p_fwer > ld) return K <= 0 ? cudaSuccess : cudaErrorInvalidValue;
     unsigned char* s = static_cast<unsigned char*>(scratch);
     auto align16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
     size_t off = 0;
     using U = typename RadixKey<T>::U;
     T* fac = reinterpret_cast<T*>(s + off);
     U* mx = reinterpret_cast<U*>(fac + K);
-    U* mn = mx + P;
-    off = align16(sizeof(T) * ((size_t)K + 2 * (size_t)P));
+    U* mn = mx + p_fwer;
+    off = align16(sizeof(T) * ((size_t)K + 2 * (size_t)p_fwer));
     unsigned long long* cnt_obs = reinterpret_cast<unsigned long long*>(s + off);
     unsigned long long* lcount = cnt_obs + K;
     off = align16(off + sizeof(unsigned long long) * 2 * (size_t)K);
     T* sorted_pos = reinterpret_cast<T*>(s + off);
     T* sorted_neg = sorted_pos + K;
     off = align16(off + sizeof(T) * 2 * (size_t)K);
-    unsigned long long* hpos = reinterpret_cast<unsigned long long*>(s + off);
-    unsigned long long* hneg = hpos + (K + 2);
-    unsigned long long* totals = hneg + (K + 2);
-    cudaError_t e = cudaMemsetAsync(hpos, 0, sizeof(unsigned long long) * (2 * ((size_t)K + 2) + 8), st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(mx, 0x00, sizeof(U) * (size_t)P, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(mn, 0xff, sizeof(U) * (size_t)P, st);
+    double* hpos = reinterpret_cast<double*>(s + off);
+    double* hneg = hpos + (K + 2);
+    unsigned long long* totals = reinterpret_cast<unsigned long long*>(hneg + (K + 2));
+    cudaError_t e = cudaMemsetAsync(hpos, 0, sizeof(double) * (2 * ((size_t)K + 2) + 8), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(mx, 0x00, sizeof(U) * (size_t)p_fwer, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(mn, 0xff, sizeof(U) * (size_t)p_fwer, st);
     if (e != cudaSuccess) return e;
     const int wpb = 8;  // warps per block
-    stats_set_kernel<T><<<(K + wpb - 1) / wpb, wpb * 32, 0, st>>>(es, K, P, stats, fac);
-    stats_extrema_kernel<T><<<dim3((unsigned)((P + 127) / 128), (K + kExtremaSets - 1) / kExtremaSets), 128, 0, st>>>(
-        es, K, P, fac, mx, mn);
-    stats_fwer_kernel<T><<<(K + wpb - 1) / wpb, wpb * 32, 0, st>>>(K, P, mx, mn, stats);
+    stats_set_kernel<T><<<(K + wpb - 1) / wpb, wpb * 32, 0, st>>>(es, K, ld, counts, stats, fac);
+    stats_extrema_kernel<T><<<dim3((unsigned)((p_fwer + 127) / 128), (K + kExtremaSets - 1) / kExtremaSets), 128, 0,
+                              st>>>(es, K, ld, p_fwer, fac, mx, mn);
+    stats_fwer_kernel<T><<<(K + wpb - 1) / wpb, wpb * 32, 0, st>>>(K, p_fwer, mx, mn, stats);
     stats_fdr_obs_kernel<T><<<(K + 127) / 128, 128, 0, st>>>(K, stats, cnt_obs, lcount, sorted_pos, sorted_neg,
                                                               totals);
-    const int64_t nnull = (int64_t)K * (P - 1);
-    const unsigned hblocks = nnull > 0 ? (unsigned)((nnull + kHistThreads * 8 - 1) / (kHistThreads * 8)) : 1u;
-    stats_fdr_hist_kernel<T><<<hblocks, kHistThreads, 0, st>>>(es, K, P, fac, sorted_pos, sorted_neg, hpos, hneg,
-                                                               totals);
+    if (ld > 1) {
+        const int64_t need = (ld - 1 + kHistCols - 1) / kHistCols;
+        const unsigned chunks = (unsigned)(need < 65535 ? need : 65535);
+        stats_fdr_hist_kernel<T><<<dim3((unsigned)K, chunks), kHistThreads, 0, st>>>(
+            es, ld, counts, fac, sorted_pos, sorted_neg, hpos, hneg, totals);
+    }
     stats_fdr_suffix_kernel<<<2, 1024, 0, st>>>(hpos, hneg, totals);
     stats_fdr_final_kernel<T><<<(K + 255) / 256, 256, 0, st>>>(K, cnt_obs, lcount, hpos, hneg, totals, stats);
-    launches_add(7);
+    launches_add(ld > 1 ? 7 : 6);
     return cudaGetLastError();
+}
+template cudaError_t launch_stats_ragged<float>(const float*, int, int64_t, const int64_t*, int64_t, float*, void*,
+                                                cudaStream_t);
+template cudaError_t launch_stats_ragged<double>(const double*, int, int64_t, const int64_t*, int64_t, double*, void*,
+                                                 cudaStream_t);
+
+template <class T>
+cudaError_t launch_stats(const T* es, int K, int64_t P, T* stats, void* scratch, cudaStream_t st) {
+    if (K <= 0 || P <= 0) return cudaSuccess;
+    return launch_stats_ragged<T>(es, K, P, nullptr, P, stats, scratch, st);
 }
 template cudaError_t launch_stats<float>(const float*, int, int64_t, float*, void*, cudaStream_t);
 template cudaError_t launch_stats<double>(const double*, int, int64_t, double*, void*, cudaStream_t);

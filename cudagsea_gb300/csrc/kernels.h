@@ -59,6 +59,12 @@ template <class T>
 size_t stats_scratch_bytes(int K, int64_t P);
 template <class T>
 cudaError_t launch_stats(const T* es, int K, int64_t P, T* stats, void* scratch, cudaStream_t st);
+// Ragged form: row k of es (stride ld) holds counts[k] scores (device array;
+// null means ld for every set); FWER over the first p_fwer columns.  Scratch
+// of stats_scratch_bytes<T>(K, ld) suffices.
+template <class T>
+cudaError_t launch_stats_ragged(const T* es, int K, int64_t ld, const int64_t* counts, int64_t p_fwer, T* stats,
+                                void* scratch, cudaStream_t st);
 
 // Chosen form (tcgen05 class statistics, fp32 inputs).  Operand buffers:
 // A1/A2 chosen_a_bytes(G, S) each, B chosen_b_bytes(P_batch, S).
@@ -75,6 +81,25 @@ cudaError_t launch_chosen_metric(int metric, bool fp64_variance, const uint32_t*
                                  int num_perms, int64_t nA, int64_t nB, const float* mu, const double* t1,
                                  const double* t2, const unsigned char* A1, const unsigned char* A2,
                                  unsigned char* Bm, float* keys, int* error_flag, cudaStream_t st);
+
+// mean, standard deviation and skewness (biased, in double) of keys[0..G)
+template <class T>
+cudaError_t launch_moments(const T* keys, int G, double* moments, cudaStream_t st);
+
+// Learned-allocator helpers (k_adaptive.cu)
+template <class T>
+cudaError_t launch_set_means(const T* es, int64_t ld, int64_t P, int K, double* means, cudaStream_t st);
+int model_max_queries();
+template <class T>
+cudaError_t launch_model_samples(const T* es, int64_t ld, int64_t P, const int64_t* off, int K, const double* mom,
+                                 const double* means, int queries, const int64_t* slot, float* x, float* t,
+                                 float* xv, float* tv, cudaStream_t st);
+template <class T>
+cudaError_t launch_model_features(const T* es, int64_t ld, const int64_t* off, int K, const double* mom, float* x,
+                                  cudaStream_t st);
+template <class T>
+cudaError_t launch_exceed(const T* es, int64_t ld, const int32_t* list, int n_list, int64_t lo, int64_t hi,
+                          unsigned long long* exceed, double* sumabs, cudaStream_t st);
 
 // number of kernel launches issued by the launchers above since the last reset
 int64_t launches_take();

@@ -209,6 +209,108 @@ int gsea_plan_stage_times(gsea_plan plan, double* ms /* [GSEA_NUM_STAGES] */);
 int gsea_stats_device_noalloc(const void* es, int64_t num_sets, int64_t num_perms, int precision,
                               void* stats, void* stream);
 
+/* ---- learned permutation allocator -----------------------------------
+ *      No counterpart in the reference, which gives every set the same
+ *      number of permutations.  A small network (5 -> 64 -> 64 -> 2, tanh,
+ *      BF16 parameters, FP32 accumulation) maps per-set features
+ *        x = [log n_k, |ES_k| * sqrt(n_k), mu/sd, skewness, cv of |metric|]
+ *      (n_k members, ES_k observed score, moments of the observed ranking
+ *      metric) to the null tail P(|ES_null| >= |ES_k|) and the null mean
+ *      E|ES_null| of the set.  It is trained on the GPU (own forward and
+ *      backward kernels, Adam) on null scores that a plan produced, and it
+ *      is used only as a prior of the sequential stopping rule of
+ *      gsea_plan_execute_adaptive: every reported p, NES, FWER and FDR is
+ *      still counted from permutations.                                   */
+#define GSEA_MODEL_INPUTS 5
+#define GSEA_MODEL_HIDDEN 64
+#define GSEA_MODEL_OUTPUTS 2
+/* parameter vector: W1[64][5] b1[64] W2[64][64] b2[64] W3[2][64] b3[2] */
+#define GSEA_MODEL_PARAMS 4674
+/* normaliser vector: x_mean[5] x_scale[5] (x_n = (x - mean) * scale),
+ * y_mean y_std (log null mean = z1 * y_std + y_mean), sigma_tail (sd of the
+ * logit error of the tail on held-out sets), sigma_mean (sd of the log error
+ * of the null mean), trained (0/1) */
+#define GSEA_MODEL_NORMS 15
+typedef struct gsea_model_s* gsea_model;
+/* parameters drawn from `seed` (Glorot-uniform weights, zero biases) on the
+ * current device (device < 0) or on `device` */
+int gsea_model_create(uint32_t seed, int device, gsea_model* out);
+int gsea_model_destroy(gsea_model m);
+/* FP32 master parameters and normalisers (either pointer may be NULL) */
+int gsea_model_get(gsea_model m, float* params, float* norms);
+int gsea_model_set(gsea_model m, const float* params, const float* norms);
+/* inference on device arrays: x [n][5] raw features -> y [n][2] =
+ * (predicted tail probability, predicted null mean) */
+int gsea_model_predict(gsea_model m, const float* x, int64_t n, float* y, void* stream);
+/* mean loss over n device samples and its gradient with respect to the
+ * parameters (device grad [GSEA_MODEL_PARAMS], device loss [1]); targets
+ * t [n][2] = (tail probability, log null mean).  Loss per sample:
+ * BCE(sigmoid(z0), t0) + 0.5 * (z1 - (t1 - y_mean) / y_std)^2, evaluated with
+ * the BF16-rounded parameters. */
+int gsea_model_loss_grad(gsea_model m, const float* x, const float* t, int64_t n, float* grad, float* loss,
+                         void* stream);
+/* sets the normalisers from the samples, then `steps` Adam steps (minibatch
+ * `batch`, cosine-decayed learning rate `lr`) captured in a CUDA graph;
+ * loss_curve (host, may be NULL) receives the loss of every step */
+int gsea_model_train(gsea_model m, const float* x, const float* t, int64_t n, int steps, int batch, float lr,
+                     float* loss_curve);
+/* held-out calibration: sigma_tail / sigma_mean from n device samples */
+int gsea_model_calibrate(gsea_model m, const float* x, const float* t, int64_t n);
+
+/* Training samples from a plan's last execute (dense ES of all sets,
+ * permutation 0 observed, plan perm_offset 0): for every set, `queries`
+ * thresholds u_j = m_k * 0.25 * 1.25^j (m_k = mean |ES| of the set) with
+ * targets (#{p: |ES_p| >= u_j} / P, log m_k), plus the observed score.
+ * x [K*(queries+1)][5], t [..][2] device arrays of the caller.  Sets with
+ * k % holdout == holdout - 1 (holdout > 0) go to the second pair of arrays
+ * (x_val, t_val), the rest to the first; counts returned in n_train / n_val. */
+int gsea_plan_model_samples(gsea_plan p, int queries, int holdout, float* x, float* t, int64_t* n_train,
+                            float* x_val, float* t_val, int64_t* n_val);
+
+typedef struct gsea_adaptive_params {
+    int64_t pilot_perms; /* permutations every set gets, perm 0 included (default 1000) */
+    double growth;       /* factor of the permutation count between rounds (2) */
+    double z;            /* stop when posterior mean - z * sd >= stop_p (3) */
+    double q_call;       /* FDR level of the calls the rule protects (0.25) */
+    double margin;       /* stop_p = margin * largest pilot p among pilot calls (2) */
+    double p_floor;      /* lower bound of stop_p (0.01) */
+    double prior_cap;    /* prior pseudo-permutations <= prior_cap * pilot_perms (4) */
+    double fallback_tol; /* model dropped if its median |log m~ - log m^| on the pilot exceeds (0.25) */
+} gsea_adaptive_params;
+void gsea_adaptive_params_init(gsea_adaptive_params* ap);
+typedef struct gsea_adaptive_report {
+    int64_t rounds;          /* permutation rounds run, pilot included */
+    int64_t scores;          /* enrichment scores computed (sum of the set counts) */
+    int64_t stopped_pilot;   /* sets stopped after the pilot */
+    int64_t full_sets;       /* sets that reached num_perms */
+    double stop_p;           /* p threshold of the stopping rule */
+    int32_t model_used;      /* 1 if the model's prior was applied */
+    double model_mean_err;   /* median |log m~ - log m^| on the pilot */
+} gsea_adaptive_report;
+/* Adaptive permutation test on the plan's inputs, num_perms permutations at
+ * most per set: a pilot of pilot_perms permutations for every set, then
+ * rounds of growing permutation counts for the sets the rule keeps.  The
+ * plan's ES rows hold counts[k] scores each (the rest of a row is left as
+ * it was); its statistics are the ragged statistics of those rows (FWER over
+ * the pilot permutations).  model may be NULL (empirical rule only).
+ * counts (host, K) and report may be NULL.  Requires perm_offset 0. */
+int gsea_plan_execute_adaptive(gsea_plan p, gsea_model model, const gsea_adaptive_params* ap, int64_t* counts,
+                               gsea_adaptive_report* report);
+/* The stopping rule alone (host arrays, no device): set k (counts[k] scores,
+ * exceed[k] of them with |S| >= |ES_k|) stops when the Beta posterior
+ * Beta(a0 + exceed, b0 + counts - exceed) has mean - z * sd >= stop_p, with
+ * a0 = 0.5 + p_model[k] * prior[k], b0 = 0.5 + (1 - p_model[k]) * prior[k]
+ * (p_model / prior NULL: Jeffreys prior alone).  The prior is dropped for a
+ * set whose exceed/counts lies more than z sd from the prior predictive
+ * (sd^2 = p (1 - p) (prior + counts) / (counts (prior + 1))).  stop[k] = 1 / 0. */
+int gsea_adaptive_decide(int64_t num_sets, const int64_t* counts, const int64_t* exceed, const float* p_model,
+                         const float* prior, double stop_p, double z, uint8_t* stop);
+/* Ragged statistics (ES, NES, NP, FWER, FDR) of a device ES matrix whose row
+ * k (stride ld) holds counts[k] scores (device int64 array); FWER over the
+ * first p_fwer columns.  Allocates its scratch; synchronous.               */
+int gsea_stats_ragged(const void* es, int64_t num_sets, int64_t ld, const int64_t* counts, int64_t p_fwer,
+                      int precision, void* stats, void* stream);
+
 /* ---- Broad files (replace read_gct / read_cls / read_gmt,
  *      src/include/read_data_files.cuh:46-321, and the loader proxies
  *      src/cudaGSEA_wrapper.cuh:15-25): parse a .gct / .cls / .gmt triple,

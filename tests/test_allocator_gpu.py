@@ -1,0 +1,206 @@
+"""The learned permutation allocator on the GPU: the network's kernels against
+the numpy oracle (loss, gradient, prediction), its training on null scores
+the permutation kernels produce, the ragged statistics, and the adaptive test
+judged against the full permutation test (identical calls at FDR < 0.25,
+bit-identical scores for every permutation a set received)."""
+import numpy as np
+import pytest
+
+from cudagsea_gb300 import allocator, api, synthetic
+from cudagsea_gb300 import _native as N
+from oracle import model as M
+from tests.test_model_oracle import random_problem
+
+pytestmark = pytest.mark.gpu
+
+Q_CALL = 0.25
+P_MAX = 4000
+
+
+def f32(a):
+    return np.ascontiguousarray(a, np.float32)
+
+
+def test_model_loss_gradient_and_prediction_match_oracle(gpu):
+    p, norms, x, t = random_problem(rows=1000, seed=11)  # 1000 rows: a partial last tile
+    p, norms, x, t = f32(p), f32(norms), f32(x), f32(t)
+    m = allocator.Model(seed=1)
+    m.set(p, norms)
+    g, l = m.loss_grad(x, t)
+    lo, go = M.loss_grad(M.bf16(p), norms, x, t)
+    assert abs(l - lo) <= 2e-6 * abs(lo) + 1e-7
+    scale = np.abs(go).max()
+    assert np.abs(g - go).max() <= 1e-4 * scale, np.abs(g - go).max() / scale
+    # every parameter block, relative to its own size
+    for a, b in ((M.OFF_W1, M.OFF_B1), (M.OFF_B1, M.OFF_W2), (M.OFF_W2, M.OFF_B2), (M.OFF_B2, M.OFF_W3),
+                 (M.OFF_W3, M.OFF_B3), (M.OFF_B3, M.NPARAM)):
+        blk = np.abs(go[a:b]).max()
+        assert np.abs(g[a:b] - go[a:b]).max() <= 1e-4 * blk + 1e-7, (a, b)
+    y = m.predict(x).cpu().numpy()
+    yo = M.predict(p, norms, x)
+    np.testing.assert_allclose(y, yo, rtol=1e-4, atol=1e-6)
+    # the master parameters are FP32, the computing copies BF16
+    assert np.array_equal(m.get()[0], p)
+    m.close()
+
+
+def case(seed, K=400):
+    return synthetic.make(3000, 60, K, P_MAX, seed=seed, n_class_b=30, sd_range=(0.5, 2.5), n_shift=150,
+                          shift_range=(0.2, 0.8), set_min=15, set_max=250, enriched_frac=0.1)
+
+
+def full_run(d, P=P_MAX):
+    plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, P, "twopass_signal2noise")
+    plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+    plan.execute()
+    es, st = plan.read()
+    return plan, es, st.reshape(5, -1)
+
+
+_MODEL = {}
+
+
+def trained_model():
+    """A model trained on the null scores of a calibration data set (another
+    seed of the same shape) by the library's own kernels."""
+    if "m" not in _MODEL:
+        plan, _, _ = full_run(case(seed=901))
+        x, t, xv, tv = allocator.model_samples(plan, queries=16, holdout=10)
+        m = allocator.Model(seed=5)
+        curve = m.train(x, t, steps=1500, batch=4096, lr=3e-3)
+        sig = m.calibrate(xv, tv)
+        _MODEL["m"], _MODEL["curve"], _MODEL["sig"] = m, curve, sig
+        _MODEL["samples"] = (x.cpu().numpy(), t.cpu().numpy(), plan.read()[0], plan)
+    return _MODEL["m"]
+
+
+def test_training_samples_follow_their_definition(gpu):
+    trained_model()
+    x, t, es, plan = _MODEL["samples"]
+    d = case(seed=901)
+    sizes = np.diff(d.set_offsets)
+    q = 16
+    for k in (0, 1, 5, 12):  # training sets (k % 10 != 9): rows k - k // 10 ...
+        r0 = (k - k // 10) * (q + 1)
+        a = np.abs(es[k].astype(np.float64))
+        m = a.mean()
+        assert np.isclose(t[r0, 1], np.log(m), rtol=1e-6)
+        for j in (0, 3, 15):
+            u = m * 0.25 * 1.25 ** j
+            assert t[r0 + j, 0] == np.float32(np.count_nonzero(a >= u) / a.size)
+            assert np.isclose(x[r0 + j, 1], u * np.sqrt(sizes[k]), rtol=1e-6)
+        assert t[r0 + q, 0] == np.float32(np.count_nonzero(a >= a[0]) / a.size)
+        assert np.isclose(x[r0, 0], np.log(sizes[k]), rtol=1e-6)
+
+
+def test_training_lowers_loss_and_calibrates(gpu):
+    trained_model()
+    curve, (s_tail, s_mean) = _MODEL["curve"], _MODEL["sig"]
+    assert np.all(np.isfinite(curve))
+    assert curve[-100:].mean() < 0.75 * curve[:20].mean()
+    # held-out sets: tail within ~0.5 logit, null mean within ~10 %
+    assert s_tail < 0.5, s_tail
+    assert s_mean < 0.1, s_mean
+
+
+def test_ragged_statistics_match_oracle(gpu):
+    import torch
+    rs = np.random.RandomState(7)
+    K, ld = 37, 900
+    es = rs.normal(0, 0.3, (K, ld)).astype(np.float32)
+    es[:, 0] += rs.normal(0, 0.6, K).astype(np.float32)
+    es[5, 0] = np.nan  # a set without hits
+    counts = rs.randint(40, ld + 1, K).astype(np.int64)
+    counts[0] = ld
+    p_fwer = int(counts.min())
+    got = allocator.stats_ragged(torch.as_tensor(es).cuda(), counts, p_fwer).cpu().numpy().reshape(5, -1)
+    ref = M.stats_ragged(es, counts, p_fwer).reshape(5, -1)
+    assert np.array_equal(got[:4].view(np.uint32), ref[:4].view(np.uint32))
+    np.testing.assert_allclose(got[4], ref[4], rtol=1e-6)
+    # full counts: the ragged form is the dense one, bit for bit
+    d = synthetic.small(num_perms=512)
+    plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, 512, 8)
+    plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+    plan.execute()
+    es_d, st_d = plan.read()
+    got = allocator.stats_ragged(torch.as_tensor(es_d).cuda(), np.full(d.num_sets, 512), 512).cpu().numpy()
+    assert np.array_equal(got.view(np.uint32), st_d.view(np.uint32))
+
+
+def check_against_full(d, res, es_full, st_full, plan):
+    es_a, st_a = plan.read()
+    st_a = st_a.reshape(5, -1)
+    counts = res.counts
+    assert counts.min() >= 250 and counts.max() <= P_MAX
+    # every score a set received is the full run's score of that permutation
+    for k in range(d.num_sets):
+        assert np.array_equal(es_a[k, :counts[k]].view(np.uint32), es_full[k, :counts[k]].view(np.uint32)), k
+    # sets run to completion: ES, NES, NP identical to the full test
+    full = counts == P_MAX
+    assert full.any()
+    for r in (0, 1, 2):
+        assert np.array_equal(st_a[r, full].view(np.uint32), st_full[r, full].view(np.uint32))
+    # the calls at FDR < 0.25 are the full test's
+    calls_full = np.where(st_full[4] < Q_CALL)[0]
+    calls = np.where(st_a[4] < Q_CALL)[0]
+    assert calls_full.size > 0
+    assert np.array_equal(calls, calls_full), (set(calls) ^ set(calls_full))
+    # every called set ran the full test
+    assert np.all(counts[calls] == P_MAX)
+    return res.report["scores"]
+
+
+def test_adaptive_without_model_matches_full_test(gpu):
+    d = case(seed=77)
+    plan_f, es_f, st_f = full_run(d)
+    plan_f.close()
+    plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, P_MAX, "twopass_signal2noise")
+    plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+    res = allocator.execute_adaptive(plan, None, pilot_perms=250)
+    assert res.report["model_used"] == 0
+    scores = check_against_full(d, res, es_f, st_f, plan)
+    assert scores < 0.8 * d.num_sets * P_MAX
+    assert res.report["scores"] == int(res.counts.sum())
+    assert res.report["stopped_pilot"] > 0
+
+
+def test_learned_prior_saves_permutations_with_identical_calls(gpu):
+    """What the trained network gains: the same calls as the full test and as
+    the rule without it, with fewer enrichment scores computed."""
+    m = trained_model()
+    d = case(seed=77)
+    plan_f, es_f, st_f = full_run(d)
+    plan_f.close()
+    out = {}
+    for name, model in (("empirical", None), ("learned", m)):
+        plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, P_MAX, "twopass_signal2noise")
+        plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+        res = allocator.execute_adaptive(plan, model, pilot_perms=250)
+        out[name] = (check_against_full(d, res, es_f, st_f, plan), res.report)
+        plan.close()
+    assert out["learned"][1]["model_used"] == 1
+    assert out["learned"][1]["model_mean_err"] < 0.1
+    assert out["learned"][0] < out["empirical"][0], out
+    assert out["learned"][1]["stopped_pilot"] > out["empirical"][1]["stopped_pilot"]
+
+
+def test_model_fallback_on_mismatched_model(gpu):
+    """A model whose null means are far off is dropped: the run is the
+    empirical rule's, call for call and count for count."""
+    m = trained_model()
+    p, n = m.get()
+    bad = allocator.Model(seed=2)
+    n2 = n.copy()
+    n2[10] += 3.0  # every predicted null mean x e^3
+    bad.set(p, n2)
+    d = case(seed=77)
+    counts = {}
+    for name, model in (("none", None), ("bad", bad)):
+        plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, P_MAX, "twopass_signal2noise")
+        plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+        res = allocator.execute_adaptive(plan, model, pilot_perms=250)
+        counts[name] = (res.counts, res.report)
+        plan.close()
+    assert counts["bad"][1]["model_used"] == 0
+    assert counts["bad"][1]["model_mean_err"] > 2.0
+    assert np.array_equal(counts["bad"][0], counts["none"][0])
