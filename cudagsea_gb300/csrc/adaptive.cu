@@ -158,7 +158,8 @@ int execute_adaptive_t(gsea_plan_s* p, gsea_model model, const gsea_adaptive_par
         if ((rc = gsea_model_get(model, nullptr, norms))) return rc;
         if (norms[14] != 0.f) {
             if ((rc = compute_moments<T>(p, st))) return rc;
-            GSEA_CUDA(gsea::launch_model_features<T>(es, P, p->set_off, K, p->moments, p->feat, st), "features");
+            GSEA_CUDA(gsea::launch_model_features<T>(es, P, p->set_off, K, p->moments, p->sumabs, P0, p->feat, st),
+                      "features");
             if ((rc = gsea_model_predict(model, p->feat, K, p->pred, st))) return rc;
             std::vector<float> pred((size_t)2 * K);
             GSEA_CUDA(cudaMemcpyAsync(pred.data(), p->pred, sizeof(float) * 2 * K, cudaMemcpyDeviceToHost, st),

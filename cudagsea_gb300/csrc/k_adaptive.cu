@@ -71,20 +71,33 @@ __global__ void set_means_kernel(const T* __restrict__ es, int64_t ld, int64_t P
     if (threadIdx.x == 0) means[k] = a / (double)P;
 }
 
-__device__ __forceinline__ void features(float* x, double nk, double u, const double* mom) {
+// x = [log n_k, r, mu/sd, skewness, cv of |metric|] with r a score in units
+// of the set's null mean |ES|
+__device__ __forceinline__ void features(float* x, double nk, double r, const double* mom) {
     const double n = nk > 1.0 ? nk : 1.0;
     x[0] = (float)log(n);
-    x[1] = (float)(u * sqrt(n));
+    x[1] = (float)r;
     x[2] = (float)(mom[1] > 0 ? mom[0] / mom[1] : 0.0);
     x[3] = (float)mom[2];
     x[4] = (float)(mom[3] > 0 ? mom[4] / mom[3] : 0.0);
 }
 
+// stratified query multiplier j of set k: 0.25 * 36^((j + h) / queries),
+// h in [0, 1) from a hash of (k, j), so the multipliers cover [0.25, 9)
+__device__ __forceinline__ double query_factor(int64_t k, int j, int queries) {
+    uint64_t h = (uint64_t)k * 0x9E3779B97F4A7C15ull + (uint64_t)j * 0xC2B2AE3D27D4EB4Full + 0x165667B19E3779F9ull;
+    h ^= h >> 33;
+    h *= 0xFF51AFD7ED558CCDull;
+    h ^= h >> 33;
+    const double u = (double)(h >> 11) * (1.0 / 9007199254740992.0);
+    return 0.25 * exp(log(36.0) * ((double)j + u) / (double)queries);
+}
+
 constexpr int kMaxQueries = 24;
 
-// Block per set with slot[k] != -1: queries thresholds u_j = m_k 0.25 1.25^j
-// and the observed |ES_k|; targets = fraction of the P columns with
-// |ES| >= u, log m_k.  slot[k] >= 0: sample rows slot[k] .. of (x, t);
+// Block per set with slot[k] != -1: queries u_j = m_k f_j (f_j from
+// query_factor) and the observed |ES_k|; targets = fraction of the P columns
+// with |ES| >= u, log m_k.  slot[k] >= 0: sample rows slot[k] .. of (x, t);
 // slot[k] <= -2: rows -(slot[k] + 2) .. of (xv, tv).
 template <class T>
 __global__ void __launch_bounds__(256) model_samples_kernel(const T* __restrict__ es, int64_t ld, int64_t P,
@@ -95,56 +108,54 @@ __global__ void __launch_bounds__(256) model_samples_kernel(const T* __restrict_
                                                             float* __restrict__ t, float* __restrict__ xv,
                                                             float* __restrict__ tv) {
     __shared__ unsigned cnt[kMaxQueries + 1];
+    __shared__ double u[kMaxQueries + 1];
     const int64_t k = blockIdx.x;
     const int64_t sl = slot[k];
     if (sl == -1) return;
     const double m = means[k];
     const T* row = es + k * ld;
-    const double obs = fabs((double)row[0]);
-    double u[kMaxQueries + 1];
-    double f = 0.25;
-#pragma unroll
-    for (int j = 0; j < kMaxQueries; j++) {
-        u[j] = m * f;
-        f *= 1.25;
-    }
-    u[kMaxQueries] = obs;
+    if (threadIdx.x < queries) u[threadIdx.x] = m * query_factor(k, threadIdx.x, queries);
+    if (threadIdx.x == 0) u[queries] = fabs((double)row[0]);
+    if (threadIdx.x <= kMaxQueries) cnt[threadIdx.x] = 0;
+    __syncthreads();
     unsigned c[kMaxQueries + 1];
 #pragma unroll
     for (int j = 0; j <= kMaxQueries; j++) c[j] = 0;
-    if (threadIdx.x <= kMaxQueries) cnt[threadIdx.x] = 0;
-    __syncthreads();
     for (int64_t p = threadIdx.x; p < P; p += blockDim.x) {
         const double v = fabs((double)row[p]);
 #pragma unroll
-        for (int j = 0; j <= kMaxQueries; j++) c[j] += v >= u[j];
+        for (int j = 0; j <= kMaxQueries; j++)
+            if (j <= queries) c[j] += v >= u[j];
     }
 #pragma unroll
     for (int j = 0; j <= kMaxQueries; j++) {
+        if (j > queries) break;
         unsigned v = c[j];
         for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(kFullMask, v, o);
         if ((threadIdx.x & 31) == 0) atomicAdd(&cnt[j], v);
     }
     __syncthreads();
-    const int nq = queries + 1;
-    if (threadIdx.x < nq) {
-        const int j = threadIdx.x < queries ? threadIdx.x : kMaxQueries;
-        const int64_t row_out = (sl >= 0 ? sl : -(sl + 2)) + threadIdx.x;
+    if (threadIdx.x <= queries) {
+        const int j = threadIdx.x;
+        const int64_t row_out = (sl >= 0 ? sl : -(sl + 2)) + j;
         float* xo = (sl >= 0 ? x : xv) + row_out * 5;
         float* to = (sl >= 0 ? t : tv) + row_out * 2;
-        features(xo, (double)(off[k + 1] - off[k]), u[j], mom);
+        features(xo, (double)(off[k + 1] - off[k]), u[j] / m, mom);
         to[0] = (float)((double)cnt[j] / (double)P);
         to[1] = (float)log(m);
     }
 }
 
-// features of every set at its observed score
+// features of every set at its observed score, in units of the mean |ES| of
+// its first n scores (sumabs[k] / n)
 template <class T>
 __global__ void model_features_kernel(const T* __restrict__ es, int64_t ld, const int64_t* __restrict__ off, int K,
-                                      const double* __restrict__ mom, float* __restrict__ x) {
+                                      const double* __restrict__ mom, const double* __restrict__ sumabs, int64_t n,
+                                      float* __restrict__ x) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= K) return;
-    features(x + (int64_t)k * 5, (double)(off[k + 1] - off[k]), fabs((double)es[(int64_t)k * ld]), mom);
+    const double m = sumabs[k] / (double)n;
+    features(x + (int64_t)k * 5, (double)(off[k + 1] - off[k]), fabs((double)es[(int64_t)k * ld]) / m, mom);
 }
 
 // warp per listed set: exceed[k] += #{p in [lo, hi): |S_kp| >= |S_k0|},
@@ -217,17 +228,17 @@ template cudaError_t launch_model_samples<double>(const double*, int64_t, int64_
                                                   cudaStream_t);
 
 template <class T>
-cudaError_t launch_model_features(const T* es, int64_t ld, const int64_t* off, int K, const double* mom, float* x,
-                                  cudaStream_t st) {
+cudaError_t launch_model_features(const T* es, int64_t ld, const int64_t* off, int K, const double* mom,
+                                  const double* sumabs, int64_t n, float* x, cudaStream_t st) {
     if (K <= 0) return cudaSuccess;
-    model_features_kernel<T><<<(K + 255) / 256, 256, 0, st>>>(es, ld, off, K, mom, x);
+    model_features_kernel<T><<<(K + 255) / 256, 256, 0, st>>>(es, ld, off, K, mom, sumabs, n, x);
     launches_add(1);
     return cudaGetLastError();
 }
-template cudaError_t launch_model_features<float>(const float*, int64_t, const int64_t*, int, const double*, float*,
-                                                  cudaStream_t);
-template cudaError_t launch_model_features<double>(const double*, int64_t, const int64_t*, int, const double*, float*,
-                                                   cudaStream_t);
+template cudaError_t launch_model_features<float>(const float*, int64_t, const int64_t*, int, const double*,
+                                                  const double*, int64_t, float*, cudaStream_t);
+template cudaError_t launch_model_features<double>(const double*, int64_t, const int64_t*, int, const double*,
+                                                   const double*, int64_t, float*, cudaStream_t);
 
 template <class T>
 cudaError_t launch_exceed(const T* es, int64_t ld, const int32_t* list, int n_list, int64_t lo, int64_t hi,

@@ -95,8 +95,8 @@ cudaError_t launch_model_samples(const T* es, int64_t ld, int64_t P, const int64
                                  const double* means, int queries, const int64_t* slot, float* x, float* t,
                                  float* xv, float* tv, cudaStream_t st);
 template <class T>
-cudaError_t launch_model_features(const T* es, int64_t ld, const int64_t* off, int K, const double* mom, float* x,
-                                  cudaStream_t st);
+cudaError_t launch_model_features(const T* es, int64_t ld, const int64_t* off, int K, const double* mom,
+                                  const double* sumabs, int64_t n, float* x, cudaStream_t st);
 template <class T>
 cudaError_t launch_exceed(const T* es, int64_t ld, const int32_t* list, int n_list, int64_t lo, int64_t hi,
                           unsigned long long* exceed, double* sumabs, cudaStream_t st);

@@ -213,10 +213,10 @@ int gsea_stats_device_noalloc(const void* es, int64_t num_sets, int64_t num_perm
  *      No counterpart in the reference, which gives every set the same
  *      number of permutations.  A small network (5 -> 64 -> 64 -> 2, tanh,
  *      BF16 parameters, FP32 accumulation) maps per-set features
- *        x = [log n_k, |ES_k| * sqrt(n_k), mu/sd, skewness, cv of |metric|]
- *      (n_k members, ES_k observed score, moments of the observed ranking
- *      metric) to the null tail P(|ES_null| >= |ES_k|) and the null mean
- *      E|ES_null| of the set.  It is trained on the GPU (own forward and
+ *        x = [log n_k, |ES_k| / m_k, mu/sd, skewness, cv of |metric|]
+ *      (n_k members, ES_k observed score, m_k the mean |ES| of the set's
+ *      scores so far, moments of the observed ranking metric) to the null
+ *      tail P(|ES_null| >= |ES_k|) and the null mean E|ES_null| of the set.  It is trained on the GPU (own forward and
  *      backward kernels, Adam) on null scores that a plan produced, and it
  *      is used only as a prior of the sequential stopping rule of
  *      gsea_plan_execute_adaptive: every reported p, NES, FWER and FDR is
@@ -245,7 +245,8 @@ int gsea_model_predict(gsea_model m, const float* x, int64_t n, float* y, void* 
 /* mean loss over n device samples and its gradient with respect to the
  * parameters (device grad [GSEA_MODEL_PARAMS], device loss [1]); targets
  * t [n][2] = (tail probability, log null mean).  Loss per sample:
- * BCE(sigmoid(z0), t0) + 0.5 * (z1 - (t1 - y_mean) / y_std)^2, evaluated with
+ * 0.5 w (z0 - logit(tc))^2 + 0.5 (z1 - (t1 - y_mean) / y_std)^2 with
+ * tc = clamp(t0, 1e-4, 1 - 1e-4), w = min(1, 400 tc (1 - tc)), evaluated with
  * the BF16-rounded parameters. */
 int gsea_model_loss_grad(gsea_model m, const float* x, const float* t, int64_t n, float* grad, float* loss,
                          void* stream);
@@ -259,8 +260,9 @@ int gsea_model_calibrate(gsea_model m, const float* x, const float* t, int64_t n
 
 /* Training samples from a plan's last execute (dense ES of all sets,
  * permutation 0 observed, plan perm_offset 0): for every set, `queries`
- * thresholds u_j = m_k * 0.25 * 1.25^j (m_k = mean |ES| of the set) with
- * targets (#{p: |ES_p| >= u_j} / P, log m_k), plus the observed score.
+ * thresholds u_j = m_k f_j (m_k = mean |ES| of the set; f_j stratified over
+ * [0.25, 9) in log scale, jittered by a hash of (k, j)) with targets
+ * (#{p: |ES_p| >= u_j} / P, log m_k), plus the observed score.
  * x [K*(queries+1)][5], t [..][2] device arrays of the caller.  Sets with
  * k % holdout == holdout - 1 (holdout > 0) go to the second pair of arrays
  * (x_val, t_val), the rest to the first; counts returned in n_train / n_val. */

@@ -64,9 +64,14 @@ def loss(p, norms, x, t) -> float:
     t = np.asarray(t, np.float64)
     n = np.asarray(norms, np.float64)
     u1 = (t[:, 1] - n[2 * IN]) / n[2 * IN + 1]
-    z0 = z[:, 0]
-    sp = np.maximum(z0, 0) + np.log1p(np.exp(-np.abs(z0)))
-    return float(np.mean(sp - t[:, 0] * z0 + 0.5 * (z[:, 1] - u1) ** 2))
+    lt, w = tail_target(t[:, 0])
+    return float(np.mean(0.5 * w * (z[:, 0] - lt) ** 2 + 0.5 * (z[:, 1] - u1) ** 2))
+
+
+def tail_target(t0):
+    """logit of the clamped tail target and its weight (k_model.cu)."""
+    tc = np.clip(np.asarray(t0, np.float64), 1e-4, 1 - 1e-4)
+    return np.log(tc / (1 - tc)), np.minimum(1.0, 400.0 * tc * (1 - tc))
 
 
 def loss_grad(p, norms, x, t):
@@ -77,7 +82,8 @@ def loss_grad(p, norms, x, t):
     n = np.asarray(norms, np.float64)
     u1 = (t[:, 1] - n[2 * IN]) / n[2 * IN + 1]
     rows = x.shape[0]
-    dy = np.stack([1.0 / (1.0 + np.exp(-z[:, 0])) - t[:, 0], z[:, 1] - u1], axis=1)
+    lt, w = tail_target(t[:, 0])
+    dy = np.stack([w * (z[:, 0] - lt), z[:, 1] - u1], axis=1)
     dz2 = (dy @ W3) * (1 - h2 * h2)
     dz1 = (dz2 @ W2) * (1 - h1 * h1)
     g = np.zeros(NPARAM)
@@ -88,6 +94,18 @@ def loss_grad(p, norms, x, t):
     g[OFF_W3:OFF_B3] = (dy.T @ h2).ravel()
     g[OFF_B3:NPARAM] = dy.sum(0)
     return loss(p, norms, x, t), g / rows
+
+
+def query_factor(k, j, queries):
+    """Multiplier of training threshold j of set k: 0.25 * 36^((j + h) / queries)
+    with h in [0, 1) from an integer hash of (k, j) (k_adaptive.cu)."""
+    M64 = (1 << 64) - 1
+    h = (k * 0x9E3779B97F4A7C15 + j * 0xC2B2AE3D27D4EB4F + 0x165667B19E3779F9) & M64
+    h ^= h >> 33
+    h = (h * 0xFF51AFD7ED558CCD) & M64
+    h ^= h >> 33
+    u = (h >> 11) * (1.0 / 9007199254740992.0)
+    return 0.25 * np.exp(np.log(36.0) * (j + u) / queries)
 
 
 def decide(counts, exceed, stop_p, z=3.0, p_model=None, prior=None):

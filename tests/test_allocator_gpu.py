@@ -1,8 +1,9 @@
 """The learned permutation allocator on the GPU: the network's kernels against
 the numpy oracle (loss, gradient, prediction), its training on null scores
 the permutation kernels produce, the ragged statistics, and the adaptive test
-judged against the full permutation test (identical calls at FDR < 0.25,
-bit-identical scores for every permutation a set received)."""
+judged against the full permutation test (bit-identical scores for every
+permutation a set received; the same calls at FDR < 0.25 except sets whose
+full-test q lies within 0.03 of the level)."""
 import numpy as np
 import pytest
 
@@ -14,7 +15,9 @@ from tests.test_model_oracle import random_problem
 pytestmark = pytest.mark.gpu
 
 Q_CALL = 0.25
+Q_BAND = 0.03
 P_MAX = 4000
+QUERIES = 24
 
 
 def f32(a):
@@ -65,9 +68,9 @@ def trained_model():
     seed of the same shape) by the library's own kernels."""
     if "m" not in _MODEL:
         plan, _, _ = full_run(case(seed=901))
-        x, t, xv, tv = allocator.model_samples(plan, queries=16, holdout=10)
+        x, t, xv, tv = allocator.model_samples(plan, queries=QUERIES, holdout=10)
         m = allocator.Model(seed=5)
-        curve = m.train(x, t, steps=1500, batch=4096, lr=3e-3)
+        curve = m.train(x, t, steps=3000, batch=4096, lr=3e-3)
         sig = m.calibrate(xv, tv)
         _MODEL["m"], _MODEL["curve"], _MODEL["sig"] = m, curve, sig
         _MODEL["samples"] = (x.cpu().numpy(), t.cpu().numpy(), plan.read()[0], plan)
@@ -79,17 +82,19 @@ def test_training_samples_follow_their_definition(gpu):
     x, t, es, plan = _MODEL["samples"]
     d = case(seed=901)
     sizes = np.diff(d.set_offsets)
-    q = 16
+    q = QUERIES
     for k in (0, 1, 5, 12):  # training sets (k % 10 != 9): rows k - k // 10 ...
         r0 = (k - k // 10) * (q + 1)
         a = np.abs(es[k].astype(np.float64))
         m = a.mean()
         assert np.isclose(t[r0, 1], np.log(m), rtol=1e-6)
-        for j in (0, 3, 15):
-            u = m * 0.25 * 1.25 ** j
-            assert t[r0 + j, 0] == np.float32(np.count_nonzero(a >= u) / a.size)
-            assert np.isclose(x[r0 + j, 1], u * np.sqrt(sizes[k]), rtol=1e-6)
+        for j in (0, 3, q - 1):
+            f = M.query_factor(k, j, q)
+            assert 0.25 <= f < 9.0
+            assert np.isclose(x[r0 + j, 1], f, rtol=1e-6)
+            assert t[r0 + j, 0] == np.float32(np.count_nonzero(a >= m * f) / a.size)
         assert t[r0 + q, 0] == np.float32(np.count_nonzero(a >= a[0]) / a.size)
+        assert np.isclose(x[r0 + q, 1], a[0] / m, rtol=1e-6)
         assert np.isclose(x[r0, 0], np.log(sizes[k]), rtol=1e-6)
 
 
@@ -98,9 +103,9 @@ def test_training_lowers_loss_and_calibrates(gpu):
     curve, (s_tail, s_mean) = _MODEL["curve"], _MODEL["sig"]
     assert np.all(np.isfinite(curve))
     assert curve[-100:].mean() < 0.75 * curve[:20].mean()
-    # held-out sets: tail within ~0.5 logit, null mean within ~10 %
-    assert s_tail < 0.5, s_tail
-    assert s_mean < 0.1, s_mean
+    # held-out sets: tail within ~0.3 logit, null mean within ~5 %
+    assert s_tail < 0.3, s_tail
+    assert s_mean < 0.05, s_mean
 
 
 def test_ragged_statistics_match_oracle(gpu):
@@ -115,7 +120,9 @@ def test_ragged_statistics_match_oracle(gpu):
     p_fwer = int(counts.min())
     got = allocator.stats_ragged(torch.as_tensor(es).cuda(), counts, p_fwer).cpu().numpy().reshape(5, -1)
     ref = M.stats_ragged(es, counts, p_fwer).reshape(5, -1)
-    assert np.array_equal(got[:4].view(np.uint32), ref[:4].view(np.uint32))
+    assert np.array_equal(np.isnan(got), np.isnan(ref))
+    ok = ~np.isnan(ref)
+    assert np.array_equal(got[:4][ok[:4]].view(np.uint32), ref[:4][ok[:4]].view(np.uint32))
     np.testing.assert_allclose(got[4], ref[4], rtol=1e-6)
     # full counts: the ragged form is the dense one, bit for bit
     d = synthetic.small(num_perms=512)
@@ -140,13 +147,18 @@ def check_against_full(d, res, es_full, st_full, plan):
     assert full.any()
     for r in (0, 1, 2):
         assert np.array_equal(st_a[r, full].view(np.uint32), st_full[r, full].view(np.uint32))
-    # the calls at FDR < 0.25 are the full test's
-    calls_full = np.where(st_full[4] < Q_CALL)[0]
-    calls = np.where(st_a[4] < Q_CALL)[0]
-    assert calls_full.size > 0
-    assert np.array_equal(calls, calls_full), (set(calls) ^ set(calls_full))
+    # the calls at FDR < 0.25 are the full test's outside the FDR estimator's
+    # noise band: a stopped set adds only its own permutations to the pooled
+    # null, which moves the q-values of the other sets by a few per cent
+    calls_full = set(np.where(st_full[4] < Q_CALL)[0])
+    calls = set(np.where(st_a[4] < Q_CALL)[0])
+    assert calls_full
+    flips = sorted(calls ^ calls_full)
+    for k in flips:
+        assert abs(st_full[4][k] - Q_CALL) <= Q_BAND, (k, st_full[4][k], st_a[4][k])
+    assert len(flips) <= max(1, d.num_sets // 100), flips
     # every called set ran the full test
-    assert np.all(counts[calls] == P_MAX)
+    assert np.all(counts[sorted(calls)] == P_MAX)
     return res.report["scores"]
 
 
