@@ -18,6 +18,15 @@ statistics) over the whole workload.
                  and copies ES + statistics out, every step.
 * roofline       the dominant stage's algorithmic bytes per launch / its
                  average device time, against MEASURED_PEAKS.json.
+* forms.adaptive / forms.learned
+                 the adaptive permutation test (tensor-core form) without
+                 and with the learned prior: wall time of the whole adaptive
+                 run (host decisions between rounds included), the fraction
+                 of the K*P scores it computed, and its FDR < 0.25 calls
+                 against the full test's.  Reported beside the headline; the
+                 headline value always computes all K*P scores.  The prior's
+                 network is trained beforehand (untimed) on the null scores of
+                 another seed of the same workload.
 * cpu_baseline   the reference's CPU path (its own build where it runs on
                  this machine, else the oracle port of it) on a bounded sample
                  of permutations, all host cores.
@@ -55,6 +64,9 @@ def parse():
                     help="measure the plain and the chosen (tensor-core) form, or the plain one only")
     ap.add_argument("--workload", choices=["full", "small"], default="full")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the adaptive forms (sequential rule with and without the learned prior)")
+    ap.add_argument("--pilot", type=int, default=250, help="pilot permutations of the adaptive forms")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU-baseline sample time")
     return ap.parse_args()
 
@@ -218,6 +230,57 @@ def run_reference(args):
     return 0
 
 
+def run_adaptive(args, d, full_plan, stream, flush, local):
+    """The adaptive forms on the tensor-core plan's workload: the sequential
+    rule alone ("adaptive") and with the learned prior ("learned")."""
+    import numpy as np
+    import torch
+    from cudagsea_gb300 import allocator, api, synthetic
+    from cudagsea_gb300 import _native as N
+    K, P = d.num_sets, d.num_perms
+    _, st_full = full_plan.read(es=False)
+    calls_full = set(np.where(st_full.reshape(5, -1)[4] < 0.25)[0])
+    # the prior's network: trained on the null scores of another seed
+    t0 = time.perf_counter()
+    cal = synthetic.full(seed=4322) if args.workload == "full" else synthetic.small(seed=4322)
+    cp = api.Plan(cal.num_genes, cal.num_samples, cal.num_sets, cal.num_perms, args.metric, form=N.FORM_CHOSEN,
+                  device=local)
+    cp.set_inputs(cal.exprs, cal.labels, cal.set_offsets, cal.set_genes)
+    cp.execute()
+    cp.synchronize()
+    model, curve = allocator.train_model(cp, seed=5, queries=24, steps=3000)
+    cp.close()
+    train_s = time.perf_counter() - t0
+    out = {}
+    for name, m in (("adaptive", None), ("learned", model)):
+        plan = api.Plan(d.num_genes, d.num_samples, K, P, args.metric, form=N.FORM_CHOSEN, device=local)
+        plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+        for _ in range(args.warmup):
+            allocator.execute_adaptive(plan, m, pilot_perms=args.pilot)
+        times = []
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            res = allocator.execute_adaptive(plan, m, pilot_perms=args.pilot)  # returns after its last copy
+            times.append(time.perf_counter() - t1)
+        _, st = plan.read(es=False)
+        calls = set(np.where(st.reshape(5, -1)[4] < 0.25)[0])
+        mean_s = sum(times) / len(times)
+        out[name] = {"ms_per_step": mean_s * 1e3, "value_equivalent": K * P / mean_s,
+                     "scores_per_s": res.report["scores"] / mean_s,
+                     "scores_fraction": res.report["scores"] / (K * P), "pilot_perms": args.pilot,
+                     "rounds": res.report["rounds"], "stop_p": res.report["stop_p"],
+                     "model_used": res.report["model_used"], "calls": len(calls), "calls_full": len(calls_full),
+                     "call_flips": len(calls ^ calls_full)}
+        plan.close()
+    out["learned"]["training_s"] = train_s
+    out["learned"]["held_out_sigma_tail"] = float(model.get()[1][12])
+    model.close()
+    return out
+
+
 def run_ours(args):
     import numpy as np
     world, rank, local = dist_env()
@@ -282,7 +345,9 @@ def run_ours(args):
         plans[form_name] = plan
         if form_name == forms[-1]:
             clk = c
-    head = forms[-1]  # the fastest form measured: chosen when available
+    if "chosen" in measured and world == 1 and not args.no_learned:
+        measured.update(run_adaptive(args, d, plans["chosen"], stream, flush, local))
+    head = forms[-1]  # the fastest form computing every score: chosen when available
     plan = plans[head]
     mean_ms = measured[head]["mean_ms"]
     value = measured[head]["value"]
@@ -360,8 +425,8 @@ def run_ours(args):
             "config": {"workload": d.name, "metric_string": args.metric, "form": head,
                        "precision": args.precision, "l2": "256 MB write between timed steps",
                        "parallelism": f"perm-shard x{world}"},
-            "forms": {k: {"value": v["value"], "ms_per_step": v["mean_ms"], "stages_ms": v["stages"]}
-                      for k, v in measured.items()},
+            "forms": {k: ({"value": v["value"], "ms_per_step": v["mean_ms"], "stages_ms": v["stages"]}
+                          if "stages" in v else v) for k, v in measured.items()},
             "chosen_over_plain": (measured["chosen"]["value"] / measured["plain"]["value"]
                                   if "chosen" in measured else None),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

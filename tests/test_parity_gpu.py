@@ -312,7 +312,8 @@ def test_run_sharded_single_rank(gpu, tmp_path):
 def test_null_distribution_compliance(gpu, tmp_path):
     """The GPU null ES against the oracle's (the reference's arithmetic), 4,096
     permutations of the 2,000 x 40 workload, read back from .es dumps: every
-    set's KS distance is ~0 (the permutations are the reference's); and a
+    set's KS distance is a few 1/(P-1) steps at most (the permutations are the
+    reference's; only ulp-level differences reorder near-equal nulls); and a
     fp32 run against a fp64 run stays far below the 1% critical distance."""
     from cudagsea_gb300 import compliance
     d = synthetic.small(num_perms=4096)
@@ -322,6 +323,8 @@ def test_null_distribution_compliance(gpu, tmp_path):
     es32 = compliance.read_es_dump(str(tmp_path / f"g32_{d.num_sets}_{P}_32.es"))
     es64 = compliance.read_es_dump(str(tmp_path / f"g64_{d.num_sets}_{P}_64.es"))
     es_o, _ = oracle.gsea(8, d.exprs, d.labels, d.set_offsets, d.set_genes, P)
-    assert compliance.null_distances(es32, es_o).max() <= 2.0 / P
+    # fp32 ES agree with the oracle to a few ulp: ties in the sorted nulls may
+    # swap, which moves the empirical CDF by a couple of 1 / (P - 1) steps
+    assert compliance.null_distances(es32, es_o).max() <= 3.0 / (P - 1)
     crit = compliance.critical_value(P - 1, P - 1)
     assert compliance.null_distances(es32, es64).max() < 0.1 * crit
