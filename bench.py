@@ -62,7 +62,8 @@ def parse():
     ap.add_argument("--precision", type=int, default=32)
     ap.add_argument("--form", choices=["both", "plain-only"], default="both",
                     help="measure the plain and the chosen (tensor-core) form, or the plain one only")
-    ap.add_argument("--workload", choices=["full", "small"], default="full")
+    ap.add_argument("--workload", choices=["full", "small", "learned"], default="full",
+                    help="learned: the 20,000-set / 100,000-permutation allocator workload (own JSON line)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the adaptive forms (sequential rule with and without the learned prior)")
@@ -281,6 +282,83 @@ def run_adaptive(args, d, full_plan, stream, flush, local):
     return out
 
 
+def run_learned(args):
+    """The learned-allocator workload: 20,000 x 200, 20,000 sets (5 % enriched),
+    100,000 permutations.  Times the full test (plain and tensor-core forms,
+    every score computed) and the adaptive test (tensor-core form) without and
+    with the learned prior, and counts the FDR < 0.25 calls that differ."""
+    import numpy as np
+    import torch
+    from cudagsea_gb300 import allocator, api, build, synthetic
+    from cudagsea_gb300 import _native as N
+    build.build()
+    d = synthetic.learned()
+    K, P = d.num_sets, d.num_perms
+    steps = max(1, min(args.steps, 2))
+    res = {}
+    full_stats = None
+    for name, form in (("plain", N.FORM_PLAIN), ("chosen", N.FORM_CHOSEN)):
+        plan = api.Plan(d.num_genes, d.num_samples, K, P, args.metric, form=form)
+        plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+        plan.execute()
+        plan.synchronize()
+        times = []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            plan.execute()
+            plan.synchronize()
+            times.append(time.perf_counter() - t0)
+        mean = sum(times) / len(times)
+        res[name] = {"s_per_run": mean, "value": K * P / mean}
+        if name == "chosen":
+            full_stats = plan.read(es=False)[1].reshape(5, -1)
+        plan.close()
+    calls_full = set(np.where(full_stats[4] < 0.25)[0])
+    t0 = time.perf_counter()
+    cal = synthetic.learned(seed=6262, num_sets=2000, num_perms=4000)
+    cp = api.Plan(cal.num_genes, cal.num_samples, cal.num_sets, cal.num_perms, args.metric, form=N.FORM_CHOSEN)
+    cp.set_inputs(cal.exprs, cal.labels, cal.set_offsets, cal.set_genes)
+    cp.execute()
+    cp.synchronize()
+    model, _ = allocator.train_model(cp, seed=5, queries=24, steps=3000)
+    cp.close()
+    train_s = time.perf_counter() - t0
+    for name, m in (("adaptive", None), ("learned", model)):
+        plan = api.Plan(d.num_genes, d.num_samples, K, P, args.metric, form=N.FORM_CHOSEN)
+        plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+        allocator.execute_adaptive(plan, m, pilot_perms=args.pilot)
+        times = []
+        for _ in range(steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r = allocator.execute_adaptive(plan, m, pilot_perms=args.pilot)
+            times.append(time.perf_counter() - t0)
+        st = plan.read(es=False)[1].reshape(5, -1)
+        calls = set(np.where(st[4] < 0.25)[0])
+        flips = sorted(calls ^ calls_full)
+        mean = sum(times) / len(times)
+        res[name] = {"s_per_run": mean, "value_equivalent": K * P / mean, "scores_per_s": r.report["scores"] / mean,
+                     "scores_fraction": r.report["scores"] / (K * P), "rounds": r.report["rounds"],
+                     "stop_p": r.report["stop_p"], "stopped_after_pilot": r.report["stopped_pilot"],
+                     "full_sets": r.report["full_sets"], "model_used": r.report["model_used"],
+                     "calls": len(calls), "calls_full": len(calls_full), "call_flips": len(flips),
+                     "flip_q_full": [float(full_stats[4][k]) for k in flips[:10]]}
+        plan.close()
+    res["learned"]["training_s"] = train_s
+    res["learned"]["held_out_sigma_tail"] = float(model.get()[1][12])
+    model.close()
+    out = {"metric": METRIC_NAME + ", adaptive (equivalent: K*P / wall time of the whole test)",
+           "value": res["learned"]["value_equivalent"], "unit": UNIT, "n_gpus": 1, "steps": steps,
+           "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": d.name, "metric_string": args.metric, "pilot_perms": args.pilot,
+                      "timing": "host wall clock, synchronised, whole test incl. statistics"},
+           "forms": res,
+           "learned_over_plain_full": res["learned"]["value_equivalent"] / res["plain"]["value"],
+           "learned_over_chosen_full": res["learned"]["value_equivalent"] / res["chosen"]["value"]}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_ours(args):
     import numpy as np
     world, rank, local = dist_env()
@@ -448,6 +526,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "learned":
+        return run_learned(args)
     return run_ours(args)
 
 

@@ -66,7 +66,8 @@ def _csr(sets: List[np.ndarray]):
 def make(num_genes: int, num_samples: int, num_sets: int, num_perms: int, *, seed: int = 1234,
          n_class_b: Optional[int] = None, sd=2.0, sd_range=None, n_shift: int = 50,
          shift=1.0, shift_range=None, set_min: int = 15, set_max: int = 200,
-         enriched_frac: float = 0.0, clamp: Optional[float] = None, name: str = "") -> GseaInput:
+         enriched_frac: float = 0.0, clamp: Optional[float] = None, null_background: bool = False,
+         name: str = "") -> GseaInput:
     rs = np.random.RandomState(seed)
     G, S = num_genes, num_samples
     nB = S // 2 if n_class_b is None else n_class_b
@@ -88,6 +89,7 @@ def make(num_genes: int, num_samples: int, num_sets: int, num_perms: int, *, see
         x = np.maximum(x, clamp)
     exprs = np.ascontiguousarray(x.astype(np.float32))
     sets = []
+    unshifted = np.setdiff1d(np.arange(G), shifted) if null_background else None
     hi = min(set_max, G)
     lo = min(set_min, hi)
     for k in range(num_sets):
@@ -97,11 +99,23 @@ def make(num_genes: int, num_samples: int, num_sets: int, num_perms: int, *, see
             enr = rs.choice(shifted, size=n_enr, replace=False)
             rest = rs.choice(np.setdiff1d(np.arange(G), enr), size=n - n_enr, replace=False)
             members = np.concatenate([enr, rest])
+        elif null_background:  # a null set: unshifted genes only
+            members = rs.choice(unshifted, size=n, replace=False)
         else:
             members = rs.choice(G, size=n, replace=False)
         sets.append(np.sort(members))
     off, genes = _csr(sets)
     return GseaInput(exprs, labels, off, genes, num_perms, name)
+
+
+def learned(seed: int = 5150, num_sets: int = 20000, num_perms: int = 100000) -> GseaInput:
+    """20,000 genes x 200 samples (100/100) as full(), 20,000 sets U[15,500]
+    of which 5 % are enriched for the shifted genes and the other 95 % are
+    null sets drawn from the unshifted genes; up to 100,000 permutations per
+    set."""
+    return make(20000, 200, num_sets, num_perms, seed=seed, n_class_b=100, sd_range=(0.3, 3.0),
+                n_shift=500, shift_range=(0.5, 2.0), set_min=15, set_max=500, enriched_frac=0.05,
+                clamp=1e-3, null_background=True, name=f"learned_20000x200_K{num_sets}_P{num_perms}")
 
 
 def small(seed: int = 1234, num_perms: int = 1024) -> GseaInput:
