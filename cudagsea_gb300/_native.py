@@ -50,6 +50,16 @@ class Config(ctypes.Structure):
     ]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [
+        ("metric_pb", ctypes.c_int32),
+        ("chosen_tile", ctypes.c_int32),
+        ("sort_variant", ctypes.c_int32),
+        ("es_warps", ctypes.c_int32),
+        ("es_stage", ctypes.c_int32),
+    ]
+
+
 class AdaptiveParams(ctypes.Structure):
     _fields_ = [
         ("pilot_perms", ctypes.c_int64),
@@ -115,6 +125,10 @@ SIGNATURES = [
     ("gsea_plan_set_profiling", ctypes.c_int, [_p, ctypes.c_int]),
     ("gsea_plan_stage_times", ctypes.c_int, [_p, ctypes.POINTER(ctypes.c_double)]),
     ("gsea_stats_device_noalloc", ctypes.c_int, [_p, _i64, _i64, ctypes.c_int, _p, _p]),
+    ("gsea_tuning_init", None, [ctypes.POINTER(Tuning)]),
+    ("gsea_plan_set_tuning", ctypes.c_int, [_p, ctypes.POINTER(Tuning)]),
+    ("gsea_plan_get_tuning", ctypes.c_int, [_p, ctypes.POINTER(Tuning)]),
+    ("gsea_plan_autotune", ctypes.c_int, [_p, _i64, ctypes.POINTER(Tuning), ctypes.POINTER(ctypes.c_double)]),
     ("gsea_model_create", ctypes.c_int, [ctypes.c_uint32, ctypes.c_int, ctypes.POINTER(_p)]),
     ("gsea_model_destroy", ctypes.c_int, [_p]),
     ("gsea_model_get", ctypes.c_int, [_p, _p, _p]),

@@ -149,6 +149,30 @@ class Plan:
         N.check(N.lib().gsea_plan_read_buffer(self._h, which, N.ptr(out), out.nbytes))
         return out
 
+    # ---- launch configuration
+    def set_tuning(self, **kw) -> None:
+        """metric_pb, chosen_tile, sort_variant, es_warps, es_stage (0 / -1 = automatic)."""
+        t = N.Tuning()
+        N.lib().gsea_tuning_init(ctypes.byref(t))
+        for k, v in kw.items():
+            if not hasattr(t, k):
+                raise TypeError(f"unknown tuning field {k}")
+            setattr(t, k, v)
+        N.check(N.lib().gsea_plan_set_tuning(self._h, ctypes.byref(t)))
+
+    def get_tuning(self) -> Dict[str, int]:
+        t = N.Tuning()
+        N.check(N.lib().gsea_plan_get_tuning(self._h, ctypes.byref(t)))
+        return {name: getattr(t, name) for name, _ in N.Tuning._fields_}
+
+    def autotune(self, sample_perms: int = 0) -> Tuple[Dict[str, int], Dict[str, float]]:
+        """Time every launch configuration on the plan's inputs and keep the fastest."""
+        t = N.Tuning()
+        ms = (ctypes.c_double * 3)()
+        N.check(N.lib().gsea_plan_autotune(self._h, sample_perms, ctypes.byref(t), ms))
+        return ({name: getattr(t, name) for name, _ in N.Tuning._fields_},
+                {"metric": ms[0], "sort": ms[1], "es": ms[2]})
+
     def set_profiling(self, on: bool = True) -> None:
         N.check(N.lib().gsea_plan_set_profiling(self._h, int(on)))
 

@@ -240,6 +240,10 @@ int run_range_t(gsea_plan_s* p, cudaStream_t st, int64_t lo, int64_t hi, const i
     sb.order = p->debug ? p->order : nullptr;
     sb.scratch = p->sort_scratch;
     sb.scratch_bytes = p->sort_scratch_bytes;
+    sb.variant = p->tuning.sort_variant;
+    gsea::EsTuning et;
+    et.warps = p->tuning.es_warps;
+    et.stage = p->tuning.es_stage;
     int rc;
     for (int64_t b0 = lo; b0 < hi; b0 += p->pb) {
         const int nb = (int)(hi - b0 < p->pb ? hi - b0 : p->pb);
@@ -250,11 +254,13 @@ int run_range_t(gsea_plan_s* p, cudaStream_t st, int64_t lo, int64_t hi, const i
             GSEA_CUDA(gsea::launch_chosen_metric(c.metric, c.form == GSEA_FORM_CHOSEN_FP64, p->masks, p->words, G, S,
                                                  nb, p->nA, p->nB, p->gene_mu,
                                                  p->gene_t1, p->gene_t2, p->opA1, p->opA2, p->opB,
-                                                 static_cast<float*>(p->keys), p->dev_error, st),
+                                                 static_cast<float*>(p->keys), p->dev_error, st,
+                                                 p->tuning.chosen_tile),
                       "tensor-core class statistics");
         } else {
             GSEA_CUDA(gsea::launch_metric<T>(c.metric, static_cast<const T*>(p->exprs), G, S, p->masks, p->words,
-                                             nb, p->nA, p->nB, static_cast<T*>(p->keys), p->fast_ok, st),
+                                             nb, p->nA, p->nB, static_cast<T*>(p->keys), p->fast_ok, st,
+                                             p->tuning.metric_pb),
                       "metric kernel");
         }
         if ((rc = mark(p, 1, st))) return rc;
@@ -263,7 +269,7 @@ int run_range_t(gsea_plan_s* p, cudaStream_t st, int64_t lo, int64_t hi, const i
         if ((rc = mark(p, 2, st))) return rc;
         GSEA_CUDA(gsea::launch_es<T>(p->ranks, p->ranks16, static_cast<const T*>(p->sorted), G, nb, p->set_off,
                                      p->set_genes, set_list, static_cast<const T*>(p->decay), n_sets,
-                                     static_cast<T*>(p->es), P, b0, st),
+                                     static_cast<T*>(p->es), P, b0, st, et),
                   "enrichment kernel");
         if ((rc = mark(p, 3, st))) return rc;
     }

@@ -21,7 +21,9 @@
 //     bulk copy each (cp.async.bulk) completing on an mbarrier; three stages
 //     in flight, a stage refilled as soon as the MMAs of its chunk retired;
 //   * one thread issues tcgen05.mma (M=128, N=256, K=16) with shared-memory
-//     descriptors and tcgen05.commit to the stage's mbarrier;
+//     descriptors and tcgen05.commit to the stage's mbarrier (the tile may be
+//     tuned to 128 permutations: N=128, 256 TMEM columns, 16 KB of B per
+//     chunk; the sums are the same MMA chain per element either way);
 //   * eight warps read the accumulators with tcgen05.ld (a warp reads its
 //     lane quarter, 32 lanes x 16 columns at a time, over half of the
 //     columns), finalise the metric and store the keys.
@@ -48,12 +50,13 @@ namespace gsea {
 namespace chosen {
 
 constexpr int BM = 128;          // genes per CTA (TMEM lanes)
-constexpr int BN = 256;          // permutations per CTA
+constexpr int BN = 256;          // permutations per CTA (the default tile; 128 is the other)
 constexpr int BK = 64;           // K elements per chunk
 constexpr int A_CHUNK = BM * BK * 2;   // 16 KB
-constexpr int B_CHUNK = BN * BK * 2;   // 32 KB
-constexpr int STAGE_BYTES = 2 * A_CHUNK + B_CHUNK;
+constexpr int B_CHUNK = BN * BK * 2;   // 32 KB (a 128-permutation tile uses half)
 constexpr int STAGES = 3;
+template <int TN>
+constexpr int stage_bytes() { return 2 * A_CHUNK + TN * BK * 2; }
 constexpr int THREADS = 256;     // 8 warps: two per TMEM lane quarter in the epilogue
 constexpr long long kWaitCycles = 2000000000ll;  // ~1 s at 2 GHz
 
@@ -177,7 +180,7 @@ __device__ __forceinline__ float variance(float ms, float m) {
     return (ms - p) - e;
 }
 
-template <int COMB, bool FP64SUB>
+template <int COMB, bool FP64SUB, int TN>
 __global__ void __launch_bounds__(THREADS, 1)
 class_stats_kernel(const unsigned char* __restrict__ A1, const unsigned char* __restrict__ A2,
                    const unsigned char* __restrict__ B, int chunks, int G, int num_perms,
@@ -189,11 +192,15 @@ class_stats_kernel(const unsigned char* __restrict__ A1, const unsigned char* __
     __shared__ __align__(8) uint64_t bar_done[STAGES];
     __shared__ uint32_t tmem_slot;
     __shared__ int failed;
+    constexpr int TB_CHUNK = TN * BK * 2;
+    constexpr int TSTAGE = stage_bytes<TN>();
+    constexpr int TCOLS = 2 * TN;  // two FP32 accumulators of TN columns
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int gt = blockIdx.x, pt = blockIdx.y;
 
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(&tmem_slot))
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "n"(TCOLS)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -211,18 +218,18 @@ class_stats_kernel(const unsigned char* __restrict__ A1, const unsigned char* __
     const uint32_t tmem = tmem_slot;
 
     if (tid == 0) {
-        const uint32_t idesc = make_idesc(BM, BN);
+        const uint32_t idesc = make_idesc(BM, TN);
         uint32_t ph_full[STAGES] = {}, ph_done[STAGES] = {};
         bool ok = true;
         // stage s holds chunk c with c % STAGES == s
         auto load = [&](int c) {
             const int s = c % STAGES;
-            unsigned char* st = smem + s * STAGE_BYTES;
+            unsigned char* st = smem + s * TSTAGE;
             const uint32_t bar = smem_u32(&bar_full[s]);
-            mbar_expect_tx(bar, STAGE_BYTES);
+            mbar_expect_tx(bar, TSTAGE);
             bulk_copy(smem_u32(st), A1 + ((size_t)gt * chunks + c) * A_CHUNK, A_CHUNK, bar);
             bulk_copy(smem_u32(st + A_CHUNK), A2 + ((size_t)gt * chunks + c) * A_CHUNK, A_CHUNK, bar);
-            bulk_copy(smem_u32(st + 2 * A_CHUNK), B + ((size_t)pt * chunks + c) * B_CHUNK, B_CHUNK, bar);
+            bulk_copy(smem_u32(st + 2 * A_CHUNK), B + ((size_t)pt * chunks + c) * TB_CHUNK, TB_CHUNK, bar);
         };
         const int pre = chunks < STAGES ? chunks : STAGES;
         for (int c = 0; c < pre; c++) load(c);
@@ -234,7 +241,7 @@ class_stats_kernel(const unsigned char* __restrict__ A1, const unsigned char* __
             ph_full[s] ^= 1;
             if (!ok) break;
             fence_after();
-            const uint32_t a1 = smem_u32(smem + s * STAGE_BYTES), a2 = a1 + A_CHUNK, b = a1 + 2 * A_CHUNK;
+            const uint32_t a1 = smem_u32(smem + s * TSTAGE), a2 = a1 + A_CHUNK, b = a1 + 2 * A_CHUNK;
 #pragma unroll
             for (int kk = 0; kk < BK / 16; kk++) {
                 // K = 16 spans two core matrices along K: LBO = 128 B apart,
@@ -245,7 +252,7 @@ class_stats_kernel(const unsigned char* __restrict__ A1, const unsigned char* __
                 const uint64_t db = make_desc(b + koff, 128, (BK / 8) * 128);
                 const uint32_t acc = (c > 0 || kk > 0) ? 1u : 0u;
                 mma_bf16(tmem, da1, db, idesc, acc);
-                mma_bf16(tmem + BN, da2, db, idesc, acc);
+                mma_bf16(tmem + TN, da2, db, idesc, acc);
             }
             mma_commit(smem_u32(&bar_done[s]));
             committed = c + 1;
@@ -288,14 +295,14 @@ class_stats_kernel(const unsigned char* __restrict__ A1, const unsigned char* __
         const float t1 = gv ? (float)gene_t1[g] : 0.f, t2 = gv ? (float)gene_t2[g] : 0.f;
         const float inA = 1.f / nA, inB = 1.f / nB;
         const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
-        for (int cb = half * (BN / 32); cb < (half + 1) * (BN / 32); cb++) {
+        for (int cb = half * (TN / 32); cb < (half + 1) * (TN / 32); cb++) {
             uint32_t va[16], vq[16];
             tmem_ld16(tmem + lane_base + cb * 16, va);
-            tmem_ld16(tmem + lane_base + BN + cb * 16, vq);
+            tmem_ld16(tmem + lane_base + TN + cb * 16, vq);
             tmem_wait_ld();
 #pragma unroll
             for (int j = 0; j < 16; j++) {
-                const int p = pt * BN + cb * 16 + j;
+                const int p = pt * TN + cb * 16 + j;
                 const float sA = __uint_as_float(va[j]), sA2 = __uint_as_float(vq[j]);
                 // class means and mean squares (centred); B from the totals
                 const float mAc = sA * inA;
@@ -313,7 +320,7 @@ class_stats_kernel(const unsigned char* __restrict__ A1, const unsigned char* __
     __syncthreads();
     if (warp == 0) {
         fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(TCOLS) : "memory");
     }
 }
 
@@ -372,7 +379,9 @@ __global__ void split_operands_kernel(const T* __restrict__ X, int G, int S, int
 }
 
 // B: class-A indicator of every (permutation, sample), repeated for the three
-// parts; one thread per (permutation, sample); the buffer is zeroed before.
+// parts, in tiles of TN permutations; one thread per (permutation, sample);
+// the buffer is zeroed before.
+template <int TN>
 __global__ void label_operand_kernel(const uint32_t* __restrict__ masks, int words, int S, int num_perms,
                                      int chunks, unsigned char* __restrict__ Bm) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -380,11 +389,11 @@ __global__ void label_operand_kernel(const uint32_t* __restrict__ masks, int wor
     if (p >= num_perms) return;
     const bool a = (masks[(size_t)p * words + (s >> 5)] >> (s & 31)) & 1u;
     const __nv_bfloat16 v = __float2bfloat16(a ? 1.f : 0.f);
-    const int pt = p / BN, row = p % BN;
+    const int pt = p / TN, row = p % TN;
     for (int part = 0; part < 3; part++) {
         const int k = part * S + s;
         const int c = k / BK, kk = k % BK;
-        *reinterpret_cast<__nv_bfloat16*>(Bm + ((size_t)pt * chunks + c) * B_CHUNK + core_offset(row, kk)) = v;
+        *reinterpret_cast<__nv_bfloat16*>(Bm + ((size_t)pt * chunks + c) * (TN * BK * 2) + core_offset(row, kk)) = v;
     }
 }
 
@@ -413,22 +422,23 @@ cudaError_t launch_chosen_prepare(const T* X, int G, int S, float* mu, double* t
 template cudaError_t launch_chosen_prepare<float>(const float*, int, int, float*, double*, double*, unsigned char*,
                                                   unsigned char*, cudaStream_t);
 
-cudaError_t launch_chosen_metric(int metric, bool fp64_variance, const uint32_t* masks, int words, int G, int S,
-                                 int num_perms, int64_t nA, int64_t nB, const float* mu, const double* t1,
-                                 const double* t2, const unsigned char* A1, const unsigned char* A2,
-                                 unsigned char* Bm, float* keys, int* error_flag, cudaStream_t st) {
+namespace {
+template <int TN>
+cudaError_t launch_chosen_tn(int comb, bool fp64_variance, const uint32_t* masks, int words, int G, int S,
+                             int num_perms, int64_t nA, int64_t nB, const float* mu, const double* t1,
+                             const double* t2, const unsigned char* A1, const unsigned char* A2, unsigned char* Bm,
+                             float* keys, int* error_flag, cudaStream_t st) {
     using namespace chosen;
     const int chunks = chosen_chunks(S);
-    cudaError_t e = cudaMemsetAsync(Bm, 0, chosen_b_bytes(num_perms, S), st);
+    const size_t bbytes = (size_t)((num_perms + TN - 1) / TN) * chunks * (TN * BK * 2);
+    cudaError_t e = cudaMemsetAsync(Bm, 0, bbytes, st);
     if (e != cudaSuccess) return e;
-    label_operand_kernel<<<dim3((num_perms + 127) / 128, S), 128, 0, st>>>(masks, words, S, num_perms, chunks, Bm);
-    const int comb = metric == 0 || metric == 3 ? 0 : metric == 1 || metric == 4 ? 1 : metric == 2 || metric == 5 ? 2
-                   : (metric == 6 || metric == 8 || metric == 10 || metric == 12) ? 3 : 4;
-    const dim3 grid((G + BM - 1) / BM, (num_perms + BN - 1) / BN);
-    const size_t smem = (size_t)STAGES * STAGE_BYTES;
+    label_operand_kernel<TN><<<dim3((num_perms + 127) / 128, S), 128, 0, st>>>(masks, words, S, num_perms, chunks, Bm);
+    const dim3 grid((G + BM - 1) / BM, (num_perms + TN - 1) / TN);
+    const size_t smem = (size_t)STAGES * stage_bytes<TN>();
 #define GSEA_CHOSEN(C)                                                                                        \
     {                                                                                                         \
-        auto kern = fp64_variance ? class_stats_kernel<C, true> : class_stats_kernel<C, false>;              \
+        auto kern = fp64_variance ? class_stats_kernel<C, true, TN> : class_stats_kernel<C, false, TN>;      \
         e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);               \
         if (e != cudaSuccess) return e;                                                                       \
         kern<<<grid, THREADS, smem, st>>>(A1, A2, Bm, chunks, G, num_perms, mu, t1, t2, (float)nA, (float)nB, \
@@ -444,6 +454,21 @@ cudaError_t launch_chosen_metric(int metric, bool fp64_variance, const uint32_t*
 #undef GSEA_CHOSEN
     launches_add(2);
     return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t launch_chosen_metric(int metric, bool fp64_variance, const uint32_t* masks, int words, int G, int S,
+                                 int num_perms, int64_t nA, int64_t nB, const float* mu, const double* t1,
+                                 const double* t2, const unsigned char* A1, const unsigned char* A2,
+                                 unsigned char* Bm, float* keys, int* error_flag, cudaStream_t st, int tile_n) {
+    const int comb = metric == 0 || metric == 3 ? 0 : metric == 1 || metric == 4 ? 1 : metric == 2 || metric == 5 ? 2
+                   : (metric == 6 || metric == 8 || metric == 10 || metric == 12) ? 3 : 4;
+    if (tile_n == 128)
+        return launch_chosen_tn<128>(comb, fp64_variance, masks, words, G, S, num_perms, nA, nB, mu, t1, t2, A1, A2,
+                                     Bm, keys, error_flag, st);
+    if (tile_n != 0 && tile_n != 256) return cudaErrorInvalidValue;
+    return launch_chosen_tn<256>(comb, fp64_variance, masks, words, G, S, num_perms, nA, nB, mu, t1, t2, A1, A2, Bm,
+                                 keys, error_flag, st);
 }
 
 }  // namespace gsea

@@ -426,24 +426,36 @@ cudaError_t launch_es_w(const RankT* ranks, const T* sorted_abs, int G, int P, c
 template <class T, class RankT>
 cudaError_t launch_es_t(const RankT* ranks, const T* sorted_abs, int G, int P, const int64_t* off,
                         const int32_t* genes, const int32_t* order, const T* decay, int K, T* es, int64_t stride,
-                        int64_t col0, cudaStream_t st) {
+                        int64_t col0, EsTuning tune, cudaStream_t st) {
     int dev = 0, max_smem = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const size_t cap = (size_t)max_smem - 64;  // static shared counter
     const int grid = P < sms ? P : sms;
-    if (es_smem_bytes<T, RankT, 32, true>(G) <= cap)
-        return launch_es_w<T, RankT, 32, true>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-    if (es_smem_bytes<T, RankT, 16, true>(G) <= cap)
-        return launch_es_w<T, RankT, 16, true>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-    if (es_smem_bytes<T, RankT, 8, true>(G) <= cap)
-        return launch_es_w<T, RankT, 8, true>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-    if (es_smem_bytes<T, RankT, 32, false>(G) <= cap)
-        return launch_es_w<T, RankT, 32, false>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-    if (es_smem_bytes<T, RankT, 8, false>(G) <= cap)
-        return launch_es_w<T, RankT, 8, false>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-    return cudaErrorInvalidValue;
+    // candidates in the automatic order: most warps first, staged before not
+    struct Cand { int warps; bool stage; size_t smem; };
+    const Cand cands[] = {{32, true, es_smem_bytes<T, RankT, 32, true>(G)},
+                          {16, true, es_smem_bytes<T, RankT, 16, true>(G)},
+                          {8, true, es_smem_bytes<T, RankT, 8, true>(G)},
+                          {32, false, es_smem_bytes<T, RankT, 32, false>(G)},
+                          {16, false, es_smem_bytes<T, RankT, 16, false>(G)},
+                          {8, false, es_smem_bytes<T, RankT, 8, false>(G)}};
+    for (const Cand& c : cands) {
+        if (c.smem > cap) continue;
+        if (tune.warps && tune.warps != c.warps) continue;
+        if (tune.stage >= 0 && (tune.stage != 0) != c.stage) continue;
+#define GSEA_ES(W, S) \
+    return launch_es_w<T, RankT, W, S>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st)
+        if (c.warps == 32 && c.stage) GSEA_ES(32, true);
+        if (c.warps == 16 && c.stage) GSEA_ES(16, true);
+        if (c.warps == 8 && c.stage) GSEA_ES(8, true);
+        if (c.warps == 32) GSEA_ES(32, false);
+        if (c.warps == 16) GSEA_ES(16, false);
+        GSEA_ES(8, false);
+#undef GSEA_ES
+    }
+    return cudaErrorInvalidValue;  // the requested configuration does not fit
 }
 
 }  // namespace
@@ -451,13 +463,14 @@ cudaError_t launch_es_t(const RankT* ranks, const T* sorted_abs, int G, int P, c
 template <class T>
 cudaError_t launch_es(const void* ranks, bool ranks16, const T* sorted_abs, int G, int num_perms,
                       const int64_t* set_offsets, const int32_t* set_genes, const int32_t* set_order,
-                      const T* decay, int K, T* es, int64_t es_stride, int64_t perm_col0, cudaStream_t st) {
+                      const T* decay, int K, T* es, int64_t es_stride, int64_t perm_col0, cudaStream_t st,
+                      EsTuning tune) {
     if (num_perms <= 0 || K <= 0) return cudaSuccess;
     if (ranks16)
         return launch_es_t<T, uint16_t>(static_cast<const uint16_t*>(ranks), sorted_abs, G, num_perms, set_offsets,
-                                        set_genes, set_order, decay, K, es, es_stride, perm_col0, st);
+                                        set_genes, set_order, decay, K, es, es_stride, perm_col0, tune, st);
     return launch_es_t<T, uint32_t>(static_cast<const uint32_t*>(ranks), sorted_abs, G, num_perms, set_offsets,
-                                    set_genes, set_order, decay, K, es, es_stride, perm_col0, st);
+                                    set_genes, set_order, decay, K, es, es_stride, perm_col0, tune, st);
 }
 
 // decay[n] = (T)(1.0 / (G - n)) for n < G, 0 for n = G: the miss step of a
@@ -479,8 +492,10 @@ template cudaError_t launch_decay_table<float>(int, float*, cudaStream_t);
 template cudaError_t launch_decay_table<double>(int, double*, cudaStream_t);
 
 template cudaError_t launch_es<float>(const void*, bool, const float*, int, int, const int64_t*, const int32_t*,
-                                      const int32_t*, const float*, int, float*, int64_t, int64_t, cudaStream_t);
+                                      const int32_t*, const float*, int, float*, int64_t, int64_t, cudaStream_t,
+                                      EsTuning);
 template cudaError_t launch_es<double>(const void*, bool, const double*, int, int, const int64_t*, const int32_t*,
-                                       const int32_t*, const double*, int, double*, int64_t, int64_t, cudaStream_t);
+                                       const int32_t*, const double*, int, double*, int64_t, int64_t, cudaStream_t,
+                                       EsTuning);
 
 }  // namespace gsea

@@ -365,10 +365,9 @@ metric_fast_kernel(const float* __restrict__ X, int G, int S, const uint32_t* __
     }
 }
 
-template <int ACC, int COMB>
-cudaError_t launch_metric_fast(const float* X, int G, int S, const uint32_t* masks, int words, int num_perms,
-                               int64_t nA, int64_t nB, float* keys, const int* fast_ok, cudaStream_t st) {
-    constexpr int PB = 8;
+template <int ACC, int COMB, int PB>
+cudaError_t launch_metric_fast_pb(const float* X, int G, int S, const uint32_t* masks, int words, int num_perms,
+                                  int64_t nA, int64_t nB, float* keys, const int* fast_ok, cudaStream_t st) {
     const int threads = 128;
     dim3 grid((G + threads - 1) / threads, (num_perms + PB - 1) / PB);
     const size_t smem = sizeof(ulonglong2) * (size_t)S * (PB / 2) + sizeof(uint32_t) * PB * words;
@@ -380,6 +379,15 @@ cudaError_t launch_metric_fast(const float* X, int G, int S, const uint32_t* mas
     kern<<<grid, threads, smem, st>>>(X, G, S, masks, words, num_perms, (float)nA, (float)nB, keys, fast_ok);
     launches_add(1);
     return cudaGetLastError();
+}
+
+// pb: permutations per thread (4 or 8; 0 = 8), identical keys either way
+template <int ACC, int COMB>
+cudaError_t launch_metric_fast(const float* X, int G, int S, const uint32_t* masks, int words, int num_perms,
+                               int64_t nA, int64_t nB, float* keys, const int* fast_ok, int pb, cudaStream_t st) {
+    if (pb == 4)
+        return launch_metric_fast_pb<ACC, COMB, 4>(X, G, S, masks, words, num_perms, nA, nB, keys, fast_ok, st);
+    return launch_metric_fast_pb<ACC, COMB, 8>(X, G, S, masks, words, num_perms, nA, nB, keys, fast_ok, st);
 }
 
 template <int ACC, int COMB, class T>
@@ -398,20 +406,21 @@ cudaError_t launch_metric_t(const T* X, int G, int S, const uint32_t* masks, int
 template <class T>
 cudaError_t launch_metric_impl(int metric, const T* X, int G, int S, const uint32_t* masks,
                                int words, int num_perms, int64_t nA, int64_t nB, T* keys,
-                               const int* fast_ok, cudaStream_t st) {
+                               const int* fast_ok, cudaStream_t st, int pb) {
+    if (pb != 0 && pb != 4 && pb != 8) return cudaErrorInvalidValue;
     if (num_perms <= 0) return cudaSuccess;
     if constexpr (std::is_same<T, float>::value) {
       if (fast_ok && (size_t)S * 4 * 16 + 32 * (size_t)words <= 100 * 1024) {
         const float* Xf = X;
         float* kf = keys;
         switch (metric) {
-            case 0: return launch_metric_fast<ACC_NAIVE, COMB_DIFF>(Xf, G, S, masks, words, num_perms, nA, nB, kf, fast_ok, st);
-            case 1: return launch_metric_fast<ACC_NAIVE, COMB_RATIO>(Xf, G, S, masks, words, num_perms, nA, nB, kf, fast_ok, st);
-            case 2: return launch_metric_fast<ACC_NAIVE, COMB_LOG2>(Xf, G, S, masks, words, num_perms, nA, nB, kf, fast_ok, st);
-            case 6: return launch_metric_fast<ACC_ONEPASS, COMB_S2N>(Xf, G, S, masks, words, num_perms, nA, nB, kf, fast_ok, st);
-            case 7: return launch_metric_fast<ACC_ONEPASS, COMB_TTEST>(Xf, G, S, masks, words, num_perms, nA, nB, kf, fast_ok, st);
-            case 8: return launch_metric_fast<ACC_TWOPASS, COMB_S2N>(Xf, G, S, masks, words, num_perms, nA, nB, kf, fast_ok, st);
-            case 9: return launch_metric_fast<ACC_TWOPASS, COMB_TTEST>(Xf, G, S, masks, words, num_perms, nA, nB, kf, fast_ok, st);
+            case 0: return launch_metric_fast<ACC_NAIVE, COMB_DIFF>(Xf, G, S, masks, words, num_perms, nA, nB, kf, fast_ok, pb, st);
+            case 1: return launch_metric_fast<ACC_NAIVE, COMB_RATIO>(Xf, G, S, masks, words, num_perms, nA, nB, kf, fast_ok, pb, st);
+            case 2: return launch_metric_fast<ACC_NAIVE, COMB_LOG2>(Xf, G, S, masks, words, num_perms, nA, nB, kf, fast_ok, pb, st);
+            case 6: return launch_metric_fast<ACC_ONEPASS, COMB_S2N>(Xf, G, S, masks, words, num_perms, nA, nB, kf, fast_ok, pb, st);
+            case 7: return launch_metric_fast<ACC_ONEPASS, COMB_TTEST>(Xf, G, S, masks, words, num_perms, nA, nB, kf, fast_ok, pb, st);
+            case 8: return launch_metric_fast<ACC_TWOPASS, COMB_S2N>(Xf, G, S, masks, words, num_perms, nA, nB, kf, fast_ok, pb, st);
+            case 9: return launch_metric_fast<ACC_TWOPASS, COMB_TTEST>(Xf, G, S, masks, words, num_perms, nA, nB, kf, fast_ok, pb, st);
             default: break;
         }
       }

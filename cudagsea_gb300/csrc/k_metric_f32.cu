@@ -4,7 +4,7 @@ namespace gsea {
 template <>
 cudaError_t launch_metric<float>(int metric, const float* X, int G, int S, const uint32_t* masks,
                                  int words, int num_perms, int64_t nA, int64_t nB, float* keys,
-                                 const int* fast_ok, cudaStream_t st) {
-    return launch_metric_impl<float>(metric, X, G, S, masks, words, num_perms, nA, nB, keys, fast_ok, st);
+                                 const int* fast_ok, cudaStream_t st, int pb) {
+    return launch_metric_impl<float>(metric, X, G, S, masks, words, num_perms, nA, nB, keys, fast_ok, st, pb);
 }
 }  // namespace gsea

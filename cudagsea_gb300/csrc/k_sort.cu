@@ -350,7 +350,8 @@ cudaError_t launch_regs(const T* keys, int G, int P, bool desc, const SortBuffer
 
 template <class T, class RankT>
 cudaError_t launch_sort_t(const T* keys, int G, int P, bool desc, const SortBuffers& o, cudaStream_t st) {
-    if (sizeof(T) == 4) {
+    if (o.variant == 1 && !(sizeof(T) == 4 && G <= kThreads * 20)) return cudaErrorInvalidValue;
+    if (sizeof(T) == 4 && o.variant != 2) {
         if (G <= kThreads * 4) return launch_regs<T, RankT, 4>(keys, G, P, desc, o, st);
         if (G <= kThreads * 8) return launch_regs<T, RankT, 8>(keys, G, P, desc, o, st);
         if (G <= kThreads * 12) return launch_regs<T, RankT, 12>(keys, G, P, desc, o, st);
@@ -371,7 +372,7 @@ cudaError_t launch_sort_t(const T* keys, int G, int P, bool desc, const SortBuff
 template <class T>
 size_t sort_scratch_bytes(int G, int num_perms) {
     using U = typename RadixKey<T>::U;
-    if (sizeof(T) == 4 && G <= kThreads * 20) return 0;
+    // sized for the tiled variant, which any G may be tuned to
     const int grid = num_perms < num_sms() ? num_perms : num_sms();
     return (sizeof(U) + sizeof(uint32_t)) * 2 * (size_t)G * (size_t)(grid > 0 ? grid : 1);
 }

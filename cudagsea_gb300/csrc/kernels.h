@@ -17,7 +17,8 @@ cudaError_t launch_permute(const uint8_t* labels, int S, int64_t num_perms, int6
 template <class T>
 cudaError_t launch_metric(int metric, const T* exprs, int G, int S, const uint32_t* masks,
                           int words, int num_perms, int64_t nA, int64_t nB, T* keys,
-                          const int* fast_ok, cudaStream_t st);
+                          const int* fast_ok, cudaStream_t st, int pb = 0);
+// (pb: permutations per thread of the packed fp32 form, 4 or 8; 0 = 8)
 
 // fast_ok = 1 if every expression value is finite with |x| < 2^60, else 0
 template <class T>
@@ -34,6 +35,7 @@ struct SortBuffers {
     uint32_t* order;      // optional
     void* scratch;        // per-CTA ping-pong buffers for the tiled variant
     size_t scratch_bytes;
+    int variant = 0;      // 0 automatic, 1 register radix sort (fp32, G <= 20,480), 2 tiled
 };
 template <class T>
 size_t sort_scratch_bytes(int G, int num_perms);
@@ -46,10 +48,19 @@ cudaError_t launch_sort(const T* keys, int G, int num_perms, bool ascending, con
 // set_order (optional) lists the sets in the order warps should take them
 // (largest first balances the warps of a CTA).
 // decay (G+1 entries, from launch_decay_table) holds the miss step per hit count.
+// ES launch configuration: warps per CTA (8, 16, 32; 0 = the most that fit)
+// and whether a CTA stages its permutation's ranks and weights in shared
+// memory (1), reads them from L2 (0) or takes the first that fits (-1).
+// Every configuration gives identical scores.
+struct EsTuning {
+    int warps = 0;
+    int stage = -1;
+};
 template <class T>
 cudaError_t launch_es(const void* ranks, bool ranks16, const T* sorted_abs, int G, int num_perms,
                       const int64_t* set_offsets, const int32_t* set_genes, const int32_t* set_order,
-                      const T* decay, int K, T* es, int64_t es_stride, int64_t perm_col0, cudaStream_t st);
+                      const T* decay, int K, T* es, int64_t es_stride, int64_t perm_col0, cudaStream_t st,
+                      EsTuning tune = EsTuning());
 template <class T>
 cudaError_t launch_decay_table(int G, T* decay, cudaStream_t st);
 
@@ -80,7 +91,10 @@ cudaError_t launch_chosen_prepare(const T* X, int G, int S, float* mu, double* t
 cudaError_t launch_chosen_metric(int metric, bool fp64_variance, const uint32_t* masks, int words, int G, int S,
                                  int num_perms, int64_t nA, int64_t nB, const float* mu, const double* t1,
                                  const double* t2, const unsigned char* A1, const unsigned char* A2,
-                                 unsigned char* Bm, float* keys, int* error_flag, cudaStream_t st);
+                                 unsigned char* Bm, float* keys, int* error_flag, cudaStream_t st,
+                                 int tile_n = 0);
+// (tile_n: permutations per tensor-core tile, 128 or 256; 0 = 256.  The B
+// buffer of chosen_b_bytes fits either.)
 
 // mean, standard deviation and skewness (biased, in double) of keys[0..G)
 template <class T>

@@ -34,6 +34,7 @@ inline int cuda_fail(cudaError_t e, const char* what) {
 
 struct gsea_plan_s {
     gsea_config cfg;
+    gsea_tuning tuning{0, 0, 0, 0, -1};
     int device = 0;
     cudaStream_t stream = nullptr;
     size_t tsize = 4;

@@ -209,6 +209,29 @@ int gsea_plan_stage_times(gsea_plan plan, double* ms /* [GSEA_NUM_STAGES] */);
 int gsea_stats_device_noalloc(const void* es, int64_t num_sets, int64_t num_perms, int precision,
                               void* stats, void* stream);
 
+/* ---- launch configuration and autotuner ---------------------------------
+ *      No counterpart in the reference (its launch shapes are constants).
+ *      Every setting computes identical results; only the speed differs.
+ *      0 / -1 leave a choice automatic.                                    */
+typedef struct gsea_tuning {
+    int32_t metric_pb;    /* plain fp32 metric: permutations per thread, 4 or 8 */
+    int32_t chosen_tile;  /* tensor-core form: permutations per tile, 128 or 256 */
+    int32_t sort_variant; /* 1 register radix sort (fp32, G <= 20,480), 2 tiled */
+    int32_t es_warps;     /* warps per CTA of the enrichment kernel: 8, 16 or 32 */
+    int32_t es_stage;     /* 1 stage the permutation in shared memory, 0 read it from L2, -1 automatic */
+} gsea_tuning;
+/* all automatic */
+void gsea_tuning_init(gsea_tuning* t);
+int gsea_plan_set_tuning(gsea_plan plan, const gsea_tuning* t);
+int gsea_plan_get_tuning(gsea_plan plan, gsea_tuning* t);
+/* Times every candidate of every stage on the plan's inputs (sample_perms
+ * permutations, at most one device batch; 0 = 2 x the SM count), keeps the
+ * fastest of each stage in the plan and returns it in *best (may be NULL).
+ * ms_out (may be NULL) receives the fastest time of the metric, sort and ES
+ * stages on the sample.  Overwrites the first sample_perms columns of the
+ * plan's ES matrix; needs gsea_plan_set_inputs first.                     */
+int gsea_plan_autotune(gsea_plan plan, int64_t sample_perms, gsea_tuning* best, double* ms_out);
+
 /* ---- learned permutation allocator -----------------------------------
  *      No counterpart in the reference, which gives every set the same
  *      number of permutations.  A small network (5 -> 64 -> 64 -> 2, tanh,

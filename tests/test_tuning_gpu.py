@@ -1,0 +1,93 @@
+"""Launch configurations: every tuning choice of the metric, sort and
+enrichment kernels (and the tensor-core tile) computes the same results as the
+automatic one; the autotuner returns a configuration that runs and keeps the
+results unchanged."""
+import numpy as np
+import pytest
+
+from cudagsea_gb300 import api, synthetic
+from cudagsea_gb300 import _native as N
+
+pytestmark = pytest.mark.gpu
+
+
+def run(d, form=N.FORM_PLAIN, precision=32, **tuning):
+    plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, d.num_perms, "twopass_signal2noise",
+                    precision=precision, form=form)
+    plan.set_debug(True)
+    if tuning:
+        plan.set_tuning(**tuning)
+    plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+    plan.execute()
+    es, st = plan.read()
+    dt = np.float64 if precision == 64 else np.float32
+    keys = plan.read_buffer(N.BUF_KEYS, dt, (plan.perm_batch, d.num_genes))
+    plan.close()
+    return keys, es, st
+
+
+def same(a, b):
+    u = np.uint64 if a.dtype == np.float64 else np.uint32
+    return np.array_equal(a.view(u), b.view(u))
+
+
+@pytest.fixture(scope="module")
+def data():
+    return synthetic.make(6000, 48, 120, 600, seed=31, n_class_b=20, sd_range=(0.5, 2.0), n_shift=100,
+                          shift_range=(0.3, 1.0), set_min=15, set_max=300, enriched_frac=0.2)
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_plain_tunings_are_bit_identical(gpu, data, precision):
+    ref = run(data, precision=precision)
+    variants = [dict(sort_variant=2), dict(es_warps=8, es_stage=1), dict(es_warps=16, es_stage=0),
+                dict(es_warps=32, es_stage=0)]
+    if precision == 32:
+        variants += [dict(metric_pb=4), dict(sort_variant=1)]
+    for v in variants:
+        got = run(data, precision=precision, **v)
+        for a, b in zip(ref, got):
+            assert same(a, b), v
+
+
+def test_tensor_core_tiles_are_bit_identical(gpu, data):
+    ref = run(data, form=N.FORM_CHOSEN, chosen_tile=256)
+    got = run(data, form=N.FORM_CHOSEN, chosen_tile=128)
+    for a, b in zip(ref, got):
+        assert same(a, b)
+
+
+def test_invalid_tuning_is_rejected(gpu, data):
+    plan = api.Plan(data.num_genes, data.num_samples, data.num_sets, 64, 8)
+    with pytest.raises(N.GseaError):
+        plan.set_tuning(es_warps=12)
+    with pytest.raises(N.GseaError):
+        plan.set_tuning(chosen_tile=64)
+    # fp64 keys cannot take the register sort
+    p64 = api.Plan(data.num_genes, data.num_samples, data.num_sets, 64, 8, precision=64)
+    p64.set_tuning(sort_variant=1)
+    p64.set_inputs(data.exprs, data.labels, data.set_offsets, data.set_genes)
+    with pytest.raises(N.GseaError):
+        p64.execute()
+        p64.synchronize()
+    plan.close()
+    p64.close()
+
+
+@pytest.mark.parametrize("form", [N.FORM_PLAIN, N.FORM_CHOSEN])
+def test_autotune_keeps_results(gpu, data, form):
+    ref = run(data, form=form)
+    plan = api.Plan(data.num_genes, data.num_samples, data.num_sets, data.num_perms, "twopass_signal2noise",
+                    form=form)
+    plan.set_debug(True)
+    plan.set_inputs(data.exprs, data.labels, data.set_offsets, data.set_genes)
+    best, ms = plan.autotune(128)
+    assert best["es_warps"] in (8, 16, 32) and best["es_stage"] in (0, 1)
+    assert best["sort_variant"] in (1, 2)
+    assert (best["chosen_tile"] in (128, 256)) if form == N.FORM_CHOSEN else (best["metric_pb"] in (4, 8))
+    assert all(v > 0 for v in ms.values())
+    assert plan.get_tuning() == best
+    plan.execute()
+    es, st = plan.read()
+    assert same(es, ref[1]) and same(st, ref[2])
+    plan.close()
