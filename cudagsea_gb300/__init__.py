@@ -10,10 +10,10 @@ Compute runs only in libgsea103.so: every compute call raises if the library
 has not been built (``cudagsea_gb300.build.build()``); there is no CPU
 fallback.
 """
-from .api import (METRICS, GSEA, ExpressionTable, GseaResult, Plan, getCudaDevice, gsea,
+from .api import (METRICS, GSEA, Batch, ExpressionTable, GseaResult, Plan, getCudaDevice, gsea,
                   listCudaDevices, metric_id, setCudaDevice)
 from ._native import GseaError, FORM_CHOSEN, FORM_CHOSEN_FP64, FORM_PLAIN
 
-__all__ = ["METRICS", "GSEA", "ExpressionTable", "GseaResult", "Plan", "getCudaDevice", "gsea",
+__all__ = ["METRICS", "GSEA", "Batch", "ExpressionTable", "GseaResult", "Plan", "getCudaDevice", "gsea",
            "listCudaDevices", "metric_id", "setCudaDevice", "GseaError", "FORM_PLAIN", "FORM_CHOSEN",
            "FORM_CHOSEN_FP64"]

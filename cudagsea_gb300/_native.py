@@ -129,6 +129,15 @@ SIGNATURES = [
     ("gsea_plan_set_tuning", ctypes.c_int, [_p, ctypes.POINTER(Tuning)]),
     ("gsea_plan_get_tuning", ctypes.c_int, [_p, ctypes.POINTER(Tuning)]),
     ("gsea_plan_autotune", ctypes.c_int, [_p, _i64, ctypes.POINTER(Tuning), ctypes.POINTER(ctypes.c_double)]),
+    ("gsea_batch_create", ctypes.c_int, [_i64, ctypes.POINTER(Config), ctypes.c_int, ctypes.POINTER(_p)]),
+    ("gsea_batch_destroy", ctypes.c_int, [_p]),
+    ("gsea_batch_set_inputs", ctypes.c_int, [_p, _i64, _p, _p, _p, _p]),
+    ("gsea_batch_autotune", ctypes.c_int, [_p, _i64]),
+    ("gsea_batch_execute", ctypes.c_int, [_p, _p]),
+    ("gsea_batch_synchronize", ctypes.c_int, [_p]),
+    ("gsea_batch_read", ctypes.c_int, [_p, _i64, _p, _p]),
+    ("gsea_batch_plan", ctypes.c_int, [_p, _i64, ctypes.POINTER(_p)]),
+    ("gsea_batch_info", ctypes.c_int, [_p, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
     ("gsea_model_create", ctypes.c_int, [ctypes.c_uint32, ctypes.c_int, ctypes.POINTER(_p)]),
     ("gsea_model_destroy", ctypes.c_int, [_p]),
     ("gsea_model_get", ctypes.c_int, [_p, _p, _p]),

@@ -205,6 +205,87 @@ class Plan:
             pass
 
 
+class Batch:
+    """Many independent GSEA instances run together in one CUDA graph
+    (gsea_batch in the C ABI).  `instances`: GseaInput-like objects (exprs,
+    labels, set_offsets, set_genes, num_perms); one metric / precision / form
+    for all, or a metric per instance."""
+
+    def __init__(self, instances, metric: Union[str, int, Sequence] = "twopass_signal2noise", precision: int = 32,
+                 form: int = N.FORM_PLAIN, streams: int = 0, seed: int = 42, device: int = -1):
+        L = N.lib()
+        n = len(instances)
+        cfgs = (N.Config * n)()
+        metrics = list(metric) if isinstance(metric, (list, tuple)) else [metric] * n
+        for i, d in enumerate(instances):
+            c = cfgs[i]
+            L.gsea_config_init(ctypes.byref(c))
+            c.num_samples, c.num_genes = d.exprs.shape
+            c.num_sets = len(d.set_offsets) - 1
+            c.num_perms = d.num_perms
+            c.metric = metric_id(metrics[i])
+            c.precision, c.form, c.seed, c.device = precision, form, seed, device
+        h = ctypes.c_void_p()
+        N.check(L.gsea_batch_create(n, cfgs, streams, ctypes.byref(h)))
+        self._h = h
+        self.cfgs = cfgs
+        self.dtype = np.float64 if precision == 64 else np.float32
+        for i, d in enumerate(instances):
+            x = np.ascontiguousarray(d.exprs, self.dtype)
+            lab = np.ascontiguousarray(d.labels, np.uint8)
+            off = np.ascontiguousarray(d.set_offsets, np.int64)
+            gs = np.ascontiguousarray(d.set_genes, np.int32)
+            N.check(L.gsea_batch_set_inputs(h, i, N.ptr(x), N.ptr(lab), N.ptr(off), N.ptr(gs)))
+
+    def __len__(self):
+        return len(self.cfgs)
+
+    def autotune(self, sample_perms: int = 0) -> None:
+        N.check(N.lib().gsea_batch_autotune(self._h, sample_perms))
+
+    def execute(self, stream: Optional[int] = None) -> None:
+        N.check(N.lib().gsea_batch_execute(self._h, ctypes.c_void_p(stream) if stream else None))
+
+    def synchronize(self) -> None:
+        N.check(N.lib().gsea_batch_synchronize(self._h))
+
+    def read(self, i: int, es: bool = True, stats: bool = True):
+        c = self.cfgs[i]
+        e = np.empty((c.num_sets, c.num_perms), self.dtype) if es else None
+        s = np.empty(5 * c.num_sets, self.dtype) if stats else None
+        N.check(N.lib().gsea_batch_read(self._h, i, N.ptr(e), N.ptr(s)))
+        return e, s
+
+    def info(self) -> Dict[str, int]:
+        a, b, c = ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_int64(0)
+        N.check(N.lib().gsea_batch_info(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return {"graph_nodes": a.value, "es_classes": b.value, "launches": c.value}
+
+    def tuning(self, i: int) -> Dict[str, int]:
+        p = ctypes.c_void_p()
+        N.check(N.lib().gsea_batch_plan(self._h, i, ctypes.byref(p)))
+        t = N.Tuning()
+        N.check(N.lib().gsea_plan_get_tuning(p, ctypes.byref(t)))
+        return {name: getattr(t, name) for name, _ in N.Tuning._fields_}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            N.lib().gsea_batch_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def gsea(exprs_pm: np.ndarray, labels: np.ndarray, set_offsets: np.ndarray, set_genes: np.ndarray,
          num_perms: int, metric: Union[str, int] = "twopass_signal2noise", precision: int = 32,
          ascending: bool = False, dump_prefix: Optional[str] = None) -> Tuple[np.ndarray, np.ndarray]:

@@ -229,7 +229,8 @@ int check_device_error(gsea_plan_s* p) {
 }
 
 template <class T>
-int run_range_t(gsea_plan_s* p, cudaStream_t st, int64_t lo, int64_t hi, const int32_t* set_list, int n_sets) {
+int run_range_t(gsea_plan_s* p, cudaStream_t st, int64_t lo, int64_t hi, const int32_t* set_list, int n_sets,
+                bool with_es = true) {
     const gsea_config& c = p->cfg;
     const int G = (int)c.num_genes, S = (int)c.num_samples;
     const int64_t P = c.num_perms;
@@ -267,6 +268,7 @@ int run_range_t(gsea_plan_s* p, cudaStream_t st, int64_t lo, int64_t hi, const i
         GSEA_CUDA(gsea::launch_sort<T>(static_cast<const T*>(p->keys), G, nb, c.ascending != 0, sb, st),
                   "sort kernel");
         if ((rc = mark(p, 2, st))) return rc;
+        if (!with_es) continue;
         GSEA_CUDA(gsea::launch_es<T>(p->ranks, p->ranks16, static_cast<const T*>(p->sorted), G, nb, p->set_off,
                                      p->set_genes, set_list, static_cast<const T*>(p->decay), n_sets,
                                      static_cast<T*>(p->es), P, b0, st, et),
@@ -322,6 +324,21 @@ int plan_run_range(gsea_plan_s* p, cudaStream_t st, int64_t lo, int64_t hi, cons
                                   : run_range_t<float>(p, st, lo, hi, set_list, n_sets);
 }
 int plan_dev_alloc(void** ptr, size_t bytes, const char* what) { return dev_alloc(ptr, bytes, what); }
+int plan_run_stage1(gsea_plan_s* p, cudaStream_t st) {
+    return p->cfg.precision == 64 ? run_range_t<double>(p, st, 0, p->cfg.num_perms, nullptr, 0, false)
+                                  : run_range_t<float>(p, st, 0, p->cfg.num_perms, nullptr, 0, false);
+}
+int plan_run_stats(gsea_plan_s* p, cudaStream_t st) {
+    const int K = (int)p->cfg.num_sets;
+    const int64_t P = p->cfg.num_perms;
+    cudaError_t e = p->cfg.precision == 64
+                        ? gsea::launch_stats<double>(static_cast<const double*>(p->es), K, P,
+                                                     static_cast<double*>(p->stats), p->stats_scratch, st)
+                        : gsea::launch_stats<float>(static_cast<const float*>(p->es), K, P,
+                                                    static_cast<float*>(p->stats), p->stats_scratch, st);
+    GSEA_CUDA(e, "statistics kernels");
+    return GSEA_OK;
+}
 }  // namespace gsea
 
 extern "C" {

@@ -302,6 +302,78 @@ __device__ __noinline__ T set_score_walk(uint32_t* bm, int w0, int w1, const T* 
     return best;
 }
 
+// One permutation on the calling CTA: stage its ranks and weights (STAGE),
+// then warps take sets from the CTA-wide counter until all K are scored.
+// s_w / s_rank: staging (STAGE), bm: this warp's zeroed bitmap region.
+// Begins and ends with the CTA in step (the staging may be reused after).
+template <class T, class RankT, int WARPS, bool STAGE, int WPL>
+__device__ __forceinline__ void es_one_perm(const RankT* rk, const T* wt, int G, const int64_t* __restrict__ set_off,
+                                            const int32_t* __restrict__ set_genes,
+                                            const int32_t* __restrict__ set_order, const T* __restrict__ decay, int K,
+                                            T* __restrict__ es_col, int64_t es_stride, T* s_w, RankT* s_rank,
+                                            uint32_t* bm, int* next_set) {
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int words = (G + 31) >> 5;
+    const int wpl = WPL > 0 ? WPL : (words + 31) >> 5;  // bitmap words per lane
+    const int w0 = min(lane * wpl, words), w1 = min(w0 + wpl, words);
+    __syncthreads();  // previous permutation finished with the staging and the counter
+    if (tid == 0) *next_set = 0;
+    if (STAGE) {
+        for (int i = tid; i < G; i += WARPS * 32) {
+            s_w[i] = wt[i];
+            s_rank[i] = rk[i];
+        }
+        rk = s_rank;
+        wt = s_w;
+    }
+    __syncthreads();
+    while (true) {
+        int slot = 0;
+        if (lane == 0) slot = atomicAdd(next_set, 1);
+        slot = __shfl_sync(kFullMask, slot, 0);
+        if (slot >= K) break;
+        const int k = set_order ? set_order[slot] : slot;
+        const int64_t a = set_off[k], b = set_off[k + 1];
+        // mark the members' ranks (duplicates and unknown ids fall away)
+        for (int64_t base = a; base < b; base += 128) {
+            int g[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int64_t idx = base + lane + 32 * i;
+                g[i] = idx < b ? __ldg(set_genes + idx) : -1;
+            }
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                if (g[i] >= 0 && g[i] < G) {
+                    const uint32_t r = (uint32_t)rk[g[i]];
+                    atomicOr(&bm[r >> 5], 1u << (r & 31));
+                }
+            }
+        }
+        __syncwarp();
+        T score;
+        if (WPL > 0 && b - a <= 2 * (int64_t)words)  // the list fits in the bitmap region
+            score = set_score_list<T, (WPL > 0 ? WPL : 4), (sizeof(T) == 4 ? 10 : 6)>(bm, lane * WPL, wt, decay, G,
+                                                                                    lane);
+        else
+            score = set_score_walk<T>(bm, w0, w1, wt, decay, G, lane);
+        if (lane == 0) es_col[(int64_t)k * es_stride] = score;
+        __syncwarp();
+    }
+}
+
+// shared memory of a CTA: staging for G genes (STAGE) + WARPS bitmap regions
+template <class T, class RankT, bool STAGE>
+__device__ __forceinline__ void es_smem_layout(unsigned char* smem, int G, int region, T*& s_w, RankT*& s_rank,
+                                               uint32_t*& bm) {
+    const int warp = threadIdx.x >> 5;
+    s_w = reinterpret_cast<T*>(smem);
+    s_rank = reinterpret_cast<RankT*>(smem + (STAGE ? sizeof(T) * (size_t)G : 0));
+    size_t bm_off = STAGE ? (sizeof(T) + sizeof(RankT)) * (size_t)G : 0;
+    bm_off = (bm_off + 15) & ~(size_t)15;
+    bm = reinterpret_cast<uint32_t*>(smem + bm_off) + (size_t)warp * region;
+}
+
 // WPL > 0: bitmap words per lane held in registers by the list procedure
 // (G <= 1024*WPL, ranks < 65536); WPL == 0: general procedure only.
 template <class T, class RankT, int WARPS, bool STAGE, int WPL>
@@ -313,66 +385,54 @@ es_kernel(const RankT* __restrict__ ranks, const T* __restrict__ sorted_abs, int
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int next_set;
     const int words = (G + 31) >> 5;
-    // per-warp bitmap region: WPL*32 words for the register procedure
-    const int region = WPL > 0 ? WPL * 32 : words;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    T* s_w = reinterpret_cast<T*>(smem);
-    RankT* s_rank = reinterpret_cast<RankT*>(smem + (STAGE ? sizeof(T) * (size_t)G : 0));
-    size_t bm_off = STAGE ? (sizeof(T) + sizeof(RankT)) * (size_t)G : 0;
-    bm_off = (bm_off + 15) & ~(size_t)15;
-    uint32_t* bm = reinterpret_cast<uint32_t*>(smem + bm_off) + (size_t)warp * region;
-    for (int w = lane; w < region; w += 32) bm[w] = 0u;
+    const int region = WPL > 0 ? WPL * 32 : words;  // per-warp bitmap words
+    T* s_w;
+    RankT* s_rank;
+    uint32_t* bm;
+    es_smem_layout<T, RankT, STAGE>(smem, G, region, s_w, s_rank, bm);
+    for (int w = threadIdx.x & 31; w < region; w += 32) bm[w] = 0u;
+    for (int p = blockIdx.x; p < num_perms; p += gridDim.x)
+        es_one_perm<T, RankT, WARPS, STAGE, WPL>(ranks + (int64_t)p * G, sorted_abs + (int64_t)p * G, G, set_off,
+                                                  set_genes, set_order, decay, K, es + col0 + p, es_stride, s_w,
+                                                  s_rank, bm, &next_set);
+}
 
-    const int wpl = WPL > 0 ? WPL : (words + 31) >> 5;  // bitmap words per lane
-    const int w0 = min(lane * wpl, words), w1 = min(w0 + wpl, words);
-
-    for (int p = blockIdx.x; p < num_perms; p += gridDim.x) {
-        const RankT* rk = ranks + (int64_t)p * G;
-        const T* wt = sorted_abs + (int64_t)p * G;
-        __syncthreads();  // previous permutation finished with the staging and the counter
-        if (tid == 0) next_set = 0;
-        if (STAGE) {
-            for (int i = tid; i < G; i += WARPS * 32) {
-                s_w[i] = wt[i];
-                s_rank[i] = rk[i];
-            }
-            rk = s_rank;
-            wt = s_w;
-        }
+// Persistent multi-instance form: every CTA takes (instance, permutation)
+// items from a global counter until all are done; items run in task order
+// (tasks sorted by decreasing cost by the caller) and a task's permutations
+// in order.  item_end[t] = items of tasks 0..t; Gmax sizes the staging and
+// the bitmap regions of the size class (every task: G <= Gmax, and
+// G <= 1024*WPL for WPL > 0).
+template <class T, class RankT, int WARPS, bool STAGE, int WPL>
+__global__ void __launch_bounds__(WARPS * 32)
+es_batch_kernel(const EsTask<T>* __restrict__ tasks, const int64_t* __restrict__ item_end, int ntasks,
+                int64_t nitems, unsigned long long* __restrict__ counter, int Gmax) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int next_set;
+    __shared__ long long s_item;
+    const int region = WPL > 0 ? WPL * 32 : (Gmax + 31) >> 5;
+    T* s_w;
+    RankT* s_rank;
+    uint32_t* bm;
+    es_smem_layout<T, RankT, STAGE>(smem, Gmax, region, s_w, s_rank, bm);
+    for (int w = threadIdx.x & 31; w < region; w += 32) bm[w] = 0u;
+    while (true) {
+        __syncthreads();  // everyone read s_item of the previous round
+        if (threadIdx.x == 0) s_item = (long long)atomicAdd(counter, 1ull);
         __syncthreads();
-        while (true) {
-            int slot = 0;
-            if (lane == 0) slot = atomicAdd(&next_set, 1);
-            slot = __shfl_sync(kFullMask, slot, 0);
-            if (slot >= K) break;
-            const int k = set_order ? set_order[slot] : slot;
-            const int64_t a = set_off[k], b = set_off[k + 1];
-            // mark the members' ranks (duplicates and unknown ids fall away)
-            for (int64_t base = a; base < b; base += 128) {
-                int g[4];
-#pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    const int64_t idx = base + lane + 32 * i;
-                    g[i] = idx < b ? __ldg(set_genes + idx) : -1;
-                }
-#pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    if (g[i] >= 0 && g[i] < G) {
-                        const uint32_t r = (uint32_t)rk[g[i]];
-                        atomicOr(&bm[r >> 5], 1u << (r & 31));
-                    }
-                }
-            }
-            __syncwarp();
-            T score;
-            if (WPL > 0 && b - a <= 2 * (int64_t)words)  // the list fits in the bitmap region
-                score = set_score_list<T, (WPL > 0 ? WPL : 4), (sizeof(T) == 4 ? 10 : 6)>(bm, lane * WPL, wt, decay,
-                                                                                        G, lane);
-            else
-                score = set_score_walk<T>(bm, w0, w1, wt, decay, G, lane);
-            if (lane == 0) es[(int64_t)k * es_stride + col0 + p] = score;
-            __syncwarp();
+        const int64_t item = s_item;
+        if (item >= nitems) break;
+        int lo = 0, hi = ntasks - 1;  // first task with item_end > item
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (item_end[mid] > item) hi = mid; else lo = mid + 1;
         }
+        const EsTask<T>& tk = tasks[lo];
+        const int64_t p = item - (lo > 0 ? item_end[lo - 1] : 0);
+        const RankT* rk = static_cast<const RankT*>(tk.ranks) + p * tk.G;
+        es_one_perm<T, RankT, WARPS, STAGE, WPL>(rk, tk.sorted + p * tk.G, tk.G, tk.off, tk.genes, tk.order,
+                                                  tk.decay, tk.K, tk.es + tk.col0 + p, tk.stride, s_w, s_rank, bm,
+                                                  &next_set);
     }
 }
 
@@ -458,7 +518,81 @@ cudaError_t launch_es_t(const RankT* ranks, const T* sorted_abs, int G, int P, c
     return cudaErrorInvalidValue;  // the requested configuration does not fit
 }
 
+template <class T, int WARPS, bool STAGE, int WPL>
+cudaError_t launch_es_batch_v(const EsTask<T>* tasks, const int64_t* item_end, int ntasks, int64_t nitems,
+                              unsigned long long* counter, int Gmax, cudaStream_t st) {
+    const size_t smem = es_smem_bytes<T, uint16_t, WARPS, STAGE>(Gmax);
+    auto kern = es_batch_kernel<T, uint16_t, WARPS, STAGE, WPL>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 1, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, WARPS * 32, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidValue;
+    const int64_t want = (int64_t)sms * per_sm;
+    const int grid = (int)(nitems < want ? nitems : want);
+    e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, WARPS * 32, smem, st>>>(tasks, item_end, ntasks, nitems, counter, Gmax);
+    launches_add(1);
+    return cudaGetLastError();
+}
+
+template <class T, int WARPS, bool STAGE>
+cudaError_t launch_es_batch_w(const EsTask<T>* tasks, const int64_t* item_end, int ntasks, int64_t nitems,
+                              unsigned long long* counter, int Gmax, int wpl, cudaStream_t st) {
+    switch (wpl) {
+        case 4: return launch_es_batch_v<T, WARPS, STAGE, 4>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
+        case 8: return launch_es_batch_v<T, WARPS, STAGE, 8>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
+        case 12: return launch_es_batch_v<T, WARPS, STAGE, 12>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
+        case 16: return launch_es_batch_v<T, WARPS, STAGE, 16>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
+        case 20: return launch_es_batch_v<T, WARPS, STAGE, 20>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
+        case 0: return launch_es_batch_v<T, WARPS, STAGE, 0>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
 }  // namespace
+
+int es_size_class(int G) { return es_wpl(G, G <= 65536); }
+
+template <class T>
+cudaError_t launch_es_batch(const EsTask<T>* tasks, const int64_t* item_end, int ntasks, int64_t nitems,
+                            unsigned long long* counter, int Gmax, int wpl, EsTuning tune, cudaStream_t st) {
+    if (nitems <= 0 || ntasks <= 0) return cudaSuccess;
+    if (Gmax > 65536 || es_wpl(Gmax, true) != wpl) return cudaErrorInvalidValue;
+    int dev = 0, max_smem = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const size_t cap = (size_t)max_smem - 64;
+    struct Cand { int warps; bool stage; size_t smem; };
+    const Cand cands[] = {{32, true, es_smem_bytes<T, uint16_t, 32, true>(Gmax)},
+                          {16, true, es_smem_bytes<T, uint16_t, 16, true>(Gmax)},
+                          {8, true, es_smem_bytes<T, uint16_t, 8, true>(Gmax)},
+                          {32, false, es_smem_bytes<T, uint16_t, 32, false>(Gmax)},
+                          {16, false, es_smem_bytes<T, uint16_t, 16, false>(Gmax)},
+                          {8, false, es_smem_bytes<T, uint16_t, 8, false>(Gmax)}};
+    for (const Cand& c : cands) {
+        if (c.smem > cap) continue;
+        if (tune.warps && tune.warps != c.warps) continue;
+        if (tune.stage >= 0 && (tune.stage != 0) != c.stage) continue;
+#define GSEA_ESB(W, S) return launch_es_batch_w<T, W, S>(tasks, item_end, ntasks, nitems, counter, Gmax, wpl, st)
+        if (c.warps == 32 && c.stage) GSEA_ESB(32, true);
+        if (c.warps == 16 && c.stage) GSEA_ESB(16, true);
+        if (c.warps == 8 && c.stage) GSEA_ESB(8, true);
+        if (c.warps == 32) GSEA_ESB(32, false);
+        if (c.warps == 16) GSEA_ESB(16, false);
+        GSEA_ESB(8, false);
+#undef GSEA_ESB
+    }
+    return cudaErrorInvalidValue;
+}
+template cudaError_t launch_es_batch<float>(const EsTask<float>*, const int64_t*, int, int64_t, unsigned long long*,
+                                            int, int, EsTuning, cudaStream_t);
+template cudaError_t launch_es_batch<double>(const EsTask<double>*, const int64_t*, int, int64_t,
+                                             unsigned long long*, int, int, EsTuning, cudaStream_t);
 
 template <class T>
 cudaError_t launch_es(const void* ranks, bool ranks16, const T* sorted_abs, int G, int num_perms,

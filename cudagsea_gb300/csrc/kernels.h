@@ -64,6 +64,32 @@ cudaError_t launch_es(const void* ranks, bool ranks16, const T* sorted_abs, int 
 template <class T>
 cudaError_t launch_decay_table(int G, T* decay, cudaStream_t st);
 
+// One instance of a multi-instance ES launch: scores es[k][col0 + p] (row
+// stride `stride`) of its P permutations from ranks (uint16, G <= 65536) and
+// sorted |keys|.
+template <class T>
+struct EsTask {
+    const void* ranks;
+    const T* sorted;
+    const int64_t* off;
+    const int32_t* genes;
+    const int32_t* order;
+    const T* decay;
+    T* es;
+    int64_t col0;
+    int64_t stride;
+    int G;
+    int K;
+};
+// bitmap words per lane of the register procedure for G (0: general procedure)
+int es_size_class(int G);
+// Persistent ES over every (task, permutation) item of one size class (all
+// tasks with es_size_class(G) == wpl, G <= Gmax), items taken from *counter
+// (zeroed here); tasks and item_end (inclusive item prefix) in device memory.
+template <class T>
+cudaError_t launch_es_batch(const EsTask<T>* tasks, const int64_t* item_end, int ntasks, int64_t nitems,
+                            unsigned long long* counter, int Gmax, int wpl, EsTuning tune, cudaStream_t st);
+
 // Final statistics (ES, NES, NP, FWER, FDR) from es[K][P]; scratch sized by
 // stats_scratch_bytes.
 template <class T>

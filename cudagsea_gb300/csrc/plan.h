@@ -97,4 +97,10 @@ namespace gsea {
 // (row stride num_perms).  No statistics.
 int plan_run_range(gsea_plan_s* p, cudaStream_t st, int64_t lo, int64_t hi, const int32_t* set_list, int n_sets);
 int plan_dev_alloc(void** ptr, size_t bytes, const char* what);
+// permutation, metric and sort of every permutation (one device batch) without
+// the enrichment kernel; and the statistics of the plan's ES matrix
+int plan_run_stage1(gsea_plan_s* p, cudaStream_t st);
+int plan_run_stats(gsea_plan_s* p, cudaStream_t st);
+// autotune the metric and sort stages of a plan on n permutations (tune.cu)
+int plan_autotune_front(gsea_plan_s* p, int64_t n);
 }  // namespace gsea

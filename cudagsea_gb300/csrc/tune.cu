@@ -61,8 +61,10 @@ float time_best(F run, cudaStream_t st, Timer& t) {
     return best;
 }
 
+constexpr unsigned kMetric = 1, kSort = 2, kEs = 4;
+
 template <class T>
-int autotune_t(gsea_plan_s* p, int64_t n64, gsea_tuning* best_out, double* ms_out) {
+int autotune_t(gsea_plan_s* p, int64_t n64, unsigned stages, gsea_tuning* best_out, double* ms_out) {
     const gsea_config& c = p->cfg;
     const int G = (int)c.num_genes, S = (int)c.num_samples, K = (int)c.num_sets;
     const int n = (int)n64;
@@ -75,6 +77,7 @@ int autotune_t(gsea_plan_s* p, int64_t n64, gsea_tuning* best_out, double* ms_ou
     if (c.form != GSEA_FORM_PLAIN) mc = {256, 128};
     else mc = {8, 4};
     float mbest = 1e30f;
+    if (!(stages & kMetric)) mc = {c.form != GSEA_FORM_PLAIN ? best.chosen_tile : best.metric_pb};
     for (int v : mc) {
         auto run = [&]() -> cudaError_t {
             if (c.form != GSEA_FORM_PLAIN)
@@ -102,7 +105,9 @@ int autotune_t(gsea_plan_s* p, int64_t n64, gsea_tuning* best_out, double* ms_ou
     sb.scratch = p->sort_scratch;
     sb.scratch_bytes = p->sort_scratch_bytes;
     float sbest = 1e30f;
-    for (int v : {1, 2}) {
+    std::vector<int> sc = {1, 2};
+    if (!(stages & kSort)) sc = {best.sort_variant};
+    for (int v : sc) {
         sb.variant = v;
         const float ms = time_best(
             [&]() { return gsea::launch_sort<T>(static_cast<const T*>(p->keys), G, n, c.ascending != 0, sb, st); }, st,
@@ -116,6 +121,7 @@ int autotune_t(gsea_plan_s* p, int64_t n64, gsea_tuning* best_out, double* ms_ou
     float ebest = 1e30f;
     for (int w : {32, 16, 8}) {
         for (int stage : {1, 0}) {
+            if (!(stages & kEs)) break;
             gsea::EsTuning et;
             et.warps = w;
             et.stage = stage;
@@ -135,7 +141,8 @@ int autotune_t(gsea_plan_s* p, int64_t n64, gsea_tuning* best_out, double* ms_ou
     }
     GSEA_CUDA(cudaStreamSynchronize(st), "stream sync");
     GSEA_CUDA(cudaGetLastError(), "autotune");
-    if (ebest >= 1e30f || sbest >= 1e30f || mbest >= 1e30f) return fail(GSEA_ERR_CUDA, "no launch configuration ran");
+    if ((ebest >= 1e30f && (stages & kEs)) || sbest >= 1e30f || mbest >= 1e30f)
+        return fail(GSEA_ERR_CUDA, "no launch configuration ran");
     p->tuning = best;
     if (best_out) *best_out = best;
     if (ms_out) {
@@ -156,6 +163,15 @@ bool valid(const gsea_tuning* t) {
 }
 
 }  // namespace
+
+namespace gsea {
+// the metric and sort stages only (the batch tunes its ES kernels per class)
+int plan_autotune_front(gsea_plan_s* p, int64_t n) {
+    n = std::min(n, p->pb);
+    return p->cfg.precision == 64 ? autotune_t<double>(p, n, kMetric | kSort, nullptr, nullptr)
+                                  : autotune_t<float>(p, n, kMetric | kSort, nullptr, nullptr);
+}
+}  // namespace gsea
 
 extern "C" {
 
@@ -190,7 +206,8 @@ int gsea_plan_autotune(gsea_plan p, int64_t sample_perms, gsea_tuning* best, dou
     GSEA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device), "device attribute");
     int64_t n = sample_perms ? sample_perms : 2 * (int64_t)sms;
     n = std::min(n, p->pb);
-    return p->cfg.precision == 64 ? autotune_t<double>(p, n, best, ms_out) : autotune_t<float>(p, n, best, ms_out);
+    return p->cfg.precision == 64 ? autotune_t<double>(p, n, kMetric | kSort | kEs, best, ms_out)
+                                  : autotune_t<float>(p, n, kMetric | kSort | kEs, best, ms_out);
 }
 
 }  // extern "C"

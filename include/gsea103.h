@@ -232,6 +232,39 @@ int gsea_plan_get_tuning(gsea_plan plan, gsea_tuning* t);
  * plan's ES matrix; needs gsea_plan_set_inputs first.                     */
 int gsea_plan_autotune(gsea_plan plan, int64_t sample_perms, gsea_tuning* best, double* ms_out);
 
+/* ---- batched instances -------------------------------------------------
+ *      Many independent GSEA problems run together.  No counterpart in the
+ *      reference (one problem per call).  Instances share precision and
+ *      form; each has its own genes, samples, sets, permutations and metric
+ *      (num_genes <= 65,536).  An execute runs, for every instance, the
+ *      permutation, metric and sort of all its permutations (one device
+ *      batch: num_perms x num_genes buffers per instance) spread over a pool
+ *      of streams; then one persistent enrichment launch per size class
+ *      (bitmap words per lane) over every (instance, permutation) item,
+ *      largest instances first; then every instance's statistics.  The
+ *      first execute captures all of it into one CUDA graph; later executes
+ *      replay that graph (gsea_batch_set_inputs or gsea_batch_autotune
+ *      make the next execute capture again).                               */
+typedef struct gsea_batch_s* gsea_batch;
+/* streams: size of the stream pool (0 = 16) */
+int gsea_batch_create(int64_t num_instances, const gsea_config* cfgs, int streams, gsea_batch* out);
+int gsea_batch_destroy(gsea_batch b);
+int gsea_batch_set_inputs(gsea_batch b, int64_t instance, const void* exprs, const uint8_t* labels,
+                          const int64_t* set_offsets, const int32_t* set_genes);
+/* tunes every instance's metric and sort stages and every size class's
+ * enrichment launch on sample_perms permutations (0 = 2 x the SM count);
+ * runs one full pass of the first stage to have real data to time on */
+int gsea_batch_autotune(gsea_batch b, int64_t sample_perms);
+/* asynchronous on `stream` (NULL: the batch's own stream) */
+int gsea_batch_execute(gsea_batch b, void* stream);
+int gsea_batch_synchronize(gsea_batch b);
+int gsea_batch_read(gsea_batch b, int64_t instance, void* es_out, void* stats_out);
+/* the plan holding an instance's buffers (owned by the batch) */
+int gsea_batch_plan(gsea_batch b, int64_t instance, gsea_plan* plan);
+/* nodes of the captured graph, enrichment size classes, kernel launches in
+ * one execute (any output may be NULL; 0 before the first execute)        */
+int gsea_batch_info(gsea_batch b, int64_t* graph_nodes, int64_t* es_classes, int64_t* launches);
+
 /* ---- learned permutation allocator -----------------------------------
  *      No counterpart in the reference, which gives every set the same
  *      number of permutations.  A small network (5 -> 64 -> 64 -> 2, tanh,
