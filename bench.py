@@ -62,8 +62,10 @@ def parse():
     ap.add_argument("--precision", type=int, default=32)
     ap.add_argument("--form", choices=["both", "plain-only"], default="both",
                     help="measure the plain and the chosen (tensor-core) form, or the plain one only")
-    ap.add_argument("--workload", choices=["full", "small", "learned"], default="full",
-                    help="learned: the 20,000-set / 100,000-permutation allocator workload (own JSON line)")
+    ap.add_argument("--workload", choices=["full", "small", "learned", "batched"], default="full",
+                    help="learned: the 20,000-set / 100,000-permutation allocator workload; batched: 256 uneven "
+                         "instances in one CUDA graph (each its own JSON line)")
+    ap.add_argument("--instances", type=int, default=256, help="instances of the batched workload")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the adaptive forms (sequential rule with and without the learned prior)")
@@ -359,6 +361,76 @@ def run_learned(args):
     return 0
 
 
+def run_batched(args):
+    """256 uneven instances (genes U[5k, 30k], samples U[20, 500], sets
+    U[50, 5,000], 1,000 permutations each, fp32, tensor-core form) in one
+    CUDA graph, autotuned; against the same instances executed one plan after
+    another on one stream (same buffers, same tuning)."""
+    import ctypes
+    import torch
+    from cudagsea_gb300 import api, build, synthetic
+    from cudagsea_gb300 import _native as N
+    build.build()
+    t0 = time.perf_counter()
+    ds = synthetic.batch_instances(args.instances)
+    gen_s = time.perf_counter() - t0
+    total = sum(d.num_sets * d.num_perms for d in ds)
+    t0 = time.perf_counter()
+    b = api.Batch(ds, args.metric, precision=32, form=N.FORM_CHOSEN)
+    setup_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    b.autotune()
+    tune_s = time.perf_counter() - t0
+    stream = torch.cuda.Stream()
+    for _ in range(max(1, args.warmup)):  # the first execute captures the graph
+        b.execute(stream.cuda_stream)
+    b.synchronize()
+    steps = max(1, min(args.steps, 5))
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    with Clocks(0) as clk:
+        for s0, s1 in ev:
+            s0.record(stream)
+            b.execute(stream.cuda_stream)
+            s1.record(stream)
+        torch.cuda.synchronize()
+    b.synchronize()
+    graph_ms = sum(a.elapsed_time(c) for a, c in ev) / steps
+    # the same instances one plan after another on one stream
+    L = N.lib()
+    handles = []
+    for i in range(len(ds)):
+        h = ctypes.c_void_p()
+        N.check(L.gsea_batch_plan(b._h, i, ctypes.byref(h)))
+        handles.append(h)
+    for h in handles:
+        N.check(L.gsea_plan_execute(h, ctypes.c_void_p(stream.cuda_stream)))
+    torch.cuda.synchronize()
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record(stream)
+    for h in handles:
+        N.check(L.gsea_plan_execute(h, ctypes.c_void_p(stream.cuda_stream)))
+    s1.record(stream)
+    torch.cuda.synchronize()
+    seq_ms = s0.elapsed_time(s1)
+    info = b.info()
+    b.close()
+    out = {"metric": METRIC_NAME + f", {len(ds)} batched instances", "value": total / (graph_ms / 1e3), "unit": UNIT,
+           "n_gpus": 1, "steps": steps, "warmup": args.warmup, "ms_per_step": graph_ms, "higher_is_better": True,
+           "dtype": "f32", "data": "synthetic",
+           "config": {"workload": f"batched_{len(ds)}_instances_P1000", "form": "chosen", "metric_string": args.metric,
+                      "instances": len(ds), "scores_per_step": total,
+                      "genes": [min(d.num_genes for d in ds), max(d.num_genes for d in ds)],
+                      "samples": [min(d.num_samples for d in ds), max(d.num_samples for d in ds)],
+                      "sets": [min(d.num_sets for d in ds), max(d.num_sets for d in ds)]},
+           "forms": {"batched_graph": {"value": total / (graph_ms / 1e3), "ms_per_step": graph_ms},
+                     "sequential_plans": {"value": total / (seq_ms / 1e3), "ms_per_step": seq_ms}},
+           "batched_over_sequential": seq_ms / graph_ms,
+           "graph": info, "setup_s": {"generate": gen_s, "plans": setup_s, "autotune": tune_s},
+           "clocks": clk.summary()}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_ours(args):
     import numpy as np
     world, rank, local = dist_env()
@@ -528,6 +600,8 @@ def main():
         return run_reference(args)
     if args.workload == "learned":
         return run_learned(args)
+    if args.workload == "batched":
+        return run_batched(args)
     return run_ours(args)
 
 

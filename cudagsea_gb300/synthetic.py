@@ -142,3 +142,32 @@ def tiny(seed: int = 7, G: int = 37, S: int = 5, K: int = 3, P: int = 3, n_class
     """Exhaustive-check shapes (default 37 genes x 5 samples, 3 sets, 3 permutations)."""
     return make(G, S, K, P, seed=seed, n_class_b=n_class_b, sd=2.0, n_shift=min(5, G), shift=1.0,
                 set_min=min(3, G), set_max=min(12, G), name=f"tiny_{G}x{S}_K{K}_P{P}")
+
+
+def batch_instances(n: int = 256, seed: int = 77, num_perms: int = 1000, genes=(5000, 30000), samples=(20, 500),
+                    sets=(50, 5000), set_size=(15, 500)):
+    """`n` uneven instances: genes ~ U[5,000, 30,000], samples ~ U[20, 500] with
+    class B a U[30 %, 70 %] share, K ~ U[50, 5,000] sets of size U[15, 500],
+    expression 8 + N(0, sd_g^2) with sd_g ~ U[0.3, 3] and 2.5 % of the genes
+    shifted by +-U[0.5, 2] in class B, `num_perms` permutations each.  Drawn
+    with numpy's PCG64 generator (fast enough for 256 instances)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        G = int(rng.integers(genes[0], genes[1] + 1))
+        S = int(rng.integers(samples[0], samples[1] + 1))
+        nB = int(np.clip(round(S * rng.uniform(0.3, 0.7)), 1, S - 1))
+        K = int(rng.integers(sets[0], sets[1] + 1))
+        labels = np.zeros(S, np.uint8)
+        labels[rng.permutation(S)[:nB]] = 1
+        sd = rng.uniform(0.3, 3.0, G).astype(np.float32)
+        x = rng.standard_normal((S, G), dtype=np.float32) * sd[None, :] + np.float32(8.0)
+        shifted = rng.choice(G, size=max(1, G // 40), replace=False)
+        amount = (rng.uniform(0.5, 2.0, shifted.size) * rng.choice([-1.0, 1.0], shifted.size)).astype(np.float32)
+        x[np.ix_(labels == 1, shifted)] += amount[None, :]
+        hi = min(set_size[1], G)
+        members = [np.sort(rng.choice(G, size=int(rng.integers(set_size[0], hi + 1)), replace=False))
+                   for _ in range(K)]
+        off, gs = _csr(members)
+        out.append(GseaInput(np.ascontiguousarray(x), labels, off, gs, num_perms, f"batch{i}_{G}x{S}_K{K}"))
+    return out
