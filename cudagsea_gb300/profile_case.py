@@ -1,0 +1,61 @@
+"""A profiling-size run of the pipeline: the headline shapes (20,000 genes x
+200 samples, 1,000 sets) with fewer permutations, so that an ncu capture of
+one kernel stays small.  Used by the commands recorded under profiles/.
+
+    python -m cudagsea_gb300.profile_case [--perms 152] [--reps 2]
+        [--precision 32|64] [--form plain|chosen|chosen64] [--batch 0]
+        [--model 0]
+
+--batch N   runs N uneven instances through gsea_batch instead (the
+            persistent multi-instance enrichment kernel)
+--model N   runs N training steps of the allocator network on samples of the
+            run (the model kernels)
+"""
+from __future__ import annotations
+
+import argparse
+
+from . import api, build, synthetic
+from . import _native as N
+
+FORMS = {"plain": N.FORM_PLAIN, "chosen": N.FORM_CHOSEN, "chosen64": N.FORM_CHOSEN_FP64}
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--perms", type=int, default=152)
+    ap.add_argument("--reps", type=int, default=2)
+    ap.add_argument("--precision", type=int, default=32)
+    ap.add_argument("--form", choices=sorted(FORMS), default="plain")
+    ap.add_argument("--batch", type=int, default=0)
+    ap.add_argument("--model", type=int, default=0)
+    a = ap.parse_args(argv)
+    build.build()
+    if a.batch:
+        ds = synthetic.batch_instances(a.batch, num_perms=a.perms)
+        b = api.Batch(ds, precision=a.precision, form=FORMS[a.form])
+        for _ in range(a.reps):
+            b.execute()
+        b.synchronize()
+        print("batch", b.info())
+        b.close()
+        return 0
+    d = synthetic.full(num_perms=a.perms)
+    plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, a.perms, "twopass_signal2noise",
+                    precision=a.precision, form=FORMS[a.form])
+    plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+    plan.set_profiling(True)
+    for i in range(a.reps):
+        plan.execute()
+        print(i, plan.stage_times(), flush=True)
+    if a.model:
+        from . import allocator
+        m, curve = allocator.train_model(plan, steps=a.model)
+        print("model loss", float(curve[0]), "->", float(curve[-1]))
+        m.close()
+    plan.close()
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
