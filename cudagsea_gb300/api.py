@@ -205,6 +205,24 @@ class Plan:
             pass
 
 
+def map_sets(gene_symbols: Sequence[str], gene_sets: Sequence[Sequence[str]]) -> Tuple[np.ndarray, np.ndarray]:
+    """Gene-set symbols -> CSR (offsets int64[K+1], genes int32) on the device
+    (gsea_map_sets): unknown symbols dropped, duplicates collapsed, ascending."""
+    L = N.lib()
+    gs = [s.encode() for s in gene_symbols]
+    garr = (ctypes.c_char_p * len(gs))(*gs)
+    members = [m.encode() for st in gene_sets for m in st]
+    marr = (ctypes.c_char_p * max(1, len(members)))(*members)
+    soff = np.zeros(len(gene_sets) + 1, np.int64)
+    soff[1:] = np.cumsum([len(st) for st in gene_sets]) if len(gene_sets) else []
+    off = np.empty(len(gene_sets) + 1, np.int64)
+    genes = np.empty(max(1, len(members)), np.int32)
+    nnz = ctypes.c_int64(0)
+    N.check(L.gsea_map_sets(len(gs), garr, len(gene_sets), N.ptr(soff), marr, N.ptr(off), N.ptr(genes),
+                            genes.size, ctypes.byref(nnz)))
+    return off, genes[:nnz.value].copy()
+
+
 class Batch:
     """Many independent GSEA instances run together in one CUDA graph
     (gsea_batch in the C ABI).  `instances`: GseaInput-like objects (exprs,

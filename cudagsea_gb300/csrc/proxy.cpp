@@ -4,15 +4,15 @@
 //
 // gsea_proxy<> (src/cudaGSEA_wrapper.cu:179-401) maps gene-set symbols to gene
 // indices by building one bitmap per 32/64-set batch on the host inside every
-// permutation batch (create_bitmaps.cuh:13-65).  Here symbols are mapped once
-// through a hash map into CSR index lists: unknown symbols are dropped and
-// duplicates collapse, which is exactly the membership the bitmaps encode.
+// permutation batch (create_bitmaps.cuh:13-65).  Here symbols are mapped once,
+// on the device (gsea_map_sets: hash table of the gene symbols, per-set
+// membership bitmasks, CSR): unknown symbols are dropped and duplicates
+// collapse, which is exactly the membership the bitmaps encode.
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <stdexcept>
 #include <string>
-#include <unordered_map>
 #include <vector>
 
 #include "../../include/gsea103.h"
@@ -35,24 +35,25 @@ struct Csr {
     std::vector<int32_t> genes;
 };
 
+// symbols -> CSR of gene indices on the device (gsea_map_sets, csrc/sets.cu)
 Csr map_sets(const std::vector<std::string>& gsymb, const std::vector<std::vector<std::string>>& pathw) {
-    std::unordered_map<std::string, int32_t> index;
-    index.reserve(gsymb.size() * 2);
-    for (size_t g = 0; g < gsymb.size(); g++) index.emplace(gsymb[g], (int32_t)g);
+    if (gsymb.empty()) throw status_error(GSEA_ERR_INVALID_ARGUMENT, "empty expression table");
+    std::vector<const char*> gp(gsymb.size());
+    for (size_t g = 0; g < gsymb.size(); g++) gp[g] = gsymb[g].c_str();
+    std::vector<int64_t> soff(pathw.size() + 1, 0);
+    std::vector<const char*> sp;
+    for (size_t k = 0; k < pathw.size(); k++) {
+        for (const auto& m : pathw[k]) sp.push_back(m.c_str());
+        soff[k + 1] = (int64_t)sp.size();
+    }
     Csr c;
     c.off.resize(pathw.size() + 1, 0);
-    std::vector<int32_t> tmp;
-    for (size_t k = 0; k < pathw.size(); k++) {
-        tmp.clear();
-        for (const auto& s : pathw[k]) {
-            auto it = index.find(s);
-            if (it != index.end()) tmp.push_back(it->second);
-        }
-        std::sort(tmp.begin(), tmp.end());
-        tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
-        c.genes.insert(c.genes.end(), tmp.begin(), tmp.end());
-        c.off[k + 1] = (int64_t)c.genes.size();
-    }
+    c.genes.resize(sp.size());
+    int64_t nnz = 0;
+    const int rc = gsea_map_sets((int64_t)gp.size(), gp.data(), (int64_t)pathw.size(), soff.data(), sp.data(),
+                                 c.off.data(), c.genes.data(), (int64_t)sp.size(), &nnz);
+    if (rc) throw status_error(rc, gsea_last_error());
+    c.genes.resize((size_t)nnz);
     return c;
 }
 

@@ -143,6 +143,19 @@ int gsea_proxy_run(int precision, const void* exprs, int64_t num_genes, int64_t 
                    const char* metric, int64_t num_perms, int sort_direction, int swap_labels,
                    const char* dump_filename, void* result_out);
 
+/* ---- gene-set membership on the device (replaces create_bitmaps,
+ *      src/include/create_bitmaps.cuh:13-65, which rebuilds host bitmaps for
+ *      every 32/64-set batch of every permutation batch).  Gene symbols are
+ *      hashed once into a device table, set members looked up (exact byte
+ *      comparison), per-set membership bitmasks built and compacted into CSR:
+ *      unknown symbols dropped, duplicates collapsed, genes ascending; a
+ *      repeated gene symbol maps to its first gene.  set_offsets_out gets
+ *      num_sets + 1 entries; set_genes_out (may be NULL to size the call)
+ *      the *nnz_out members if capacity >= *nnz_out.                       */
+int gsea_map_sets(int64_t num_genes, const char* const* gene_symbols, int64_t num_sets,
+                  const int64_t* set_symbol_offsets, const char* const* set_symbols, int64_t* set_offsets_out,
+                  int32_t* set_genes_out, int64_t capacity, int64_t* nnz_out);
+
 /* ---- plan API: device-resident inputs, repeated execution --------------- */
 int gsea_plan_create(const gsea_config* cfg, gsea_plan* out);
 int gsea_plan_destroy(gsea_plan plan);

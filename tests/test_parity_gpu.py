@@ -328,3 +328,34 @@ def test_null_distribution_compliance(gpu, tmp_path):
     assert compliance.null_distances(es32, es_o).max() <= 3.0 / (P - 1)
     crit = compliance.critical_value(P - 1, P - 1)
     assert compliance.null_distances(es32, es64).max() < 0.1 * crit
+
+
+def test_device_set_mapping_matches_host_rules(gpu):
+    """gsea_map_sets on the device = the host rules of create_bitmaps: unknown
+    symbols dropped, duplicates collapsed, ascending genes, a repeated gene
+    symbol mapped to its first gene; empty and all-unknown sets."""
+    rs = np.random.RandomState(5)
+    G = 3000
+    genes = [f"G{g}" for g in range(G)]
+    genes[17] = "G5"  # a repeated gene symbol
+    sets = []
+    for k in range(200):
+        n = int(rs.randint(0, 300))
+        members = [f"G{int(x)}" for x in rs.randint(0, G, n)]
+        members += [f"X{int(x)}" for x in rs.randint(0, 50, int(rs.randint(0, 5)))]  # unknown
+        members += members[: n // 10]  # duplicates
+        rs.shuffle(members)
+        sets.append(members)
+    sets.append([])
+    sets.append(["nope", "X1"])
+    off, gs = api.map_sets(genes, sets)
+    first = {}
+    for g, s in enumerate(genes):
+        first.setdefault(s, g)
+    exp_off, exp = [0], []
+    for st in sets:
+        idx = sorted({first[m] for m in st if m in first})
+        exp += idx
+        exp_off.append(len(exp))
+    assert np.array_equal(off, np.array(exp_off))
+    assert np.array_equal(gs, np.array(exp, np.int32))
