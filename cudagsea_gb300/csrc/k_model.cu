@@ -327,14 +327,11 @@ int grad_pass(gsea_model_s* m, const float* x, const float* t, int64_t n, int64_
     return GSEA_OK;
 }
 
+// the training kernel's shared-memory opt-in, on the current device
 int set_grad_smem() {
-    static bool done = false;
-    if (!done) {
-        GSEA_CUDA(cudaFuncSetAttribute(model_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)grad_smem_bytes()),
-                  "cudaFuncSetAttribute");
-        done = true;
-    }
+    GSEA_CUDA(cudaFuncSetAttribute(model_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)grad_smem_bytes()),
+              "cudaFuncSetAttribute");
     return GSEA_OK;
 }
 

@@ -216,3 +216,35 @@ def test_model_fallback_on_mismatched_model(gpu):
     assert counts["bad"][1]["model_used"] == 0
     assert counts["bad"][1]["model_mean_err"] > 2.0
     assert np.array_equal(counts["bad"][0], counts["none"][0])
+
+
+def test_adaptive_with_pilot_covering_every_permutation_is_the_full_test(gpu):
+    """pilot >= num_perms: one round, every set full -- the statistics are the
+    dense statistics bit for bit (FWER over all permutations, unit FDR weights)."""
+    d = synthetic.small(num_perms=512)
+    plan_f = api.Plan(d.num_genes, d.num_samples, d.num_sets, 512, 8)
+    plan_f.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+    plan_f.execute()
+    es_f, st_f = plan_f.read()
+    plan_f.close()
+    plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, 512, 8)
+    plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+    res = allocator.execute_adaptive(plan, None, pilot_perms=2000)
+    es, st = plan.read()
+    plan.close()
+    assert res.report["rounds"] == 1 and np.all(res.counts == 512)
+    assert np.array_equal(es.view(np.uint32), es_f.view(np.uint32))
+    assert np.array_equal(st.view(np.uint32), st_f.view(np.uint32))
+
+
+def test_adaptive_single_set_and_invalid_parameters(gpu):
+    d = synthetic.make(500, 20, 1, 300, seed=9, n_class_b=10, set_min=30, set_max=60)
+    plan = api.Plan(d.num_genes, d.num_samples, 1, 300, 8)
+    plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+    res = allocator.execute_adaptive(plan, None, pilot_perms=50)
+    assert 50 <= res.counts[0] <= 300
+    with pytest.raises(N.GseaError):
+        allocator.execute_adaptive(plan, None, pilot_perms=1)
+    with pytest.raises(N.GseaError):
+        allocator.execute_adaptive(plan, None, growth=1.0)
+    plan.close()

@@ -89,3 +89,17 @@ def test_batch_rejects_mixed_precision(gpu):
     cfgs[1].precision = 64
     h = ctypes.c_void_p()
     assert L.gsea_batch_create(2, cfgs, 0, ctypes.byref(h)) == 1
+
+
+def test_batch_single_instance_and_single_permutation(gpu):
+    d1 = synthetic.make(4000, 30, 25, 1, seed=3, n_class_b=15, set_min=15, set_max=100)
+    d2 = synthetic.make(1500, 22, 7, 33, seed=4, n_class_b=11, set_min=15, set_max=100)
+    for ds in ([d1], [d1, d2]):
+        ref = [solo(d, "twopass_signal2noise", 32, N.FORM_PLAIN) for d in ds]
+        b = api.Batch(ds, precision=32)
+        b.execute()
+        b.synchronize()
+        for i in range(len(ds)):
+            es, st = b.read(i)
+            assert same(es, ref[i][0]) and same(st, ref[i][1])
+        b.close()
