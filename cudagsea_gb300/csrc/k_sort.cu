@@ -197,14 +197,23 @@ sort_regs_kernel(const T* __restrict__ keys, int G, int num_perms, bool descendi
             for (int i = 0; i < ITEMS; i++) val[i] = exv[my0 + 32 * i];
             __syncthreads();
         }
+        // weights (and gene ids) at their positions: coalesced; ranks by gene:
+        // gathered in shared memory first so the global write is coalesced
+        // too (exch is free: every pass ended with a barrier)
         const int64_t base = (int64_t)p * G;
+        RankT* s_rk = reinterpret_cast<RankT*>(exch);  // [G] (exch holds TILE >= G keys)
 #pragma unroll
         for (int i = 0; i < ITEMS; i++) {
             const int pos = my0 + 32 * i;
-            if (val[i] < (uint32_t)G)
-                emit<RankT, T>(base, pos, val[i], value_of<T>(key[i], descending), ranks, sorted_abs,
-                               order);
+            if (val[i] < (uint32_t)G) {
+                s_rk[val[i]] = (RankT)pos;
+                sorted_abs[base + pos] = cuabs(value_of<T>(key[i], descending));
+                if (order) order[base + pos] = val[i];
+            }
         }
+        __syncthreads();
+        for (int g = threadIdx.x; g < G; g += kThreads) ranks[base + g] = s_rk[g];
+        __syncthreads();  // exch is reused by the next permutation
     }
 }
 
