@@ -231,8 +231,9 @@ template <class T, class RankT>
 __global__ void __launch_bounds__(kThreads, 1)
 sort_tiled_kernel(const T* __restrict__ keys, int G, int num_perms, bool descending,
                   RankT* __restrict__ ranks, T* __restrict__ sorted_abs, uint32_t* __restrict__ order,
-                  unsigned char* __restrict__ scratch) {
+                  unsigned char* __restrict__ scratch, bool stage_ranks) {
     using U = typename RadixKey<T>::U;
+    extern __shared__ __align__(16) unsigned char dyn_smem[];  // [G] RankT when stage_ranks
     __shared__ uint32_t cnt[kWarps][256];
     __shared__ uint32_t hist[256];
     __shared__ uint32_t base[256];
@@ -322,8 +323,21 @@ sort_tiled_kernel(const T* __restrict__ keys, int G, int num_perms, bool descend
             uint32_t* tv = vA; vA = vB; vB = tv;
         }
         const int64_t b = (int64_t)p * G;
-        for (int pos = tid; pos < G; pos += kThreads)
-            emit<RankT, T>(b, pos, vA[pos], value_of<T>(kA[pos], descending), ranks, sorted_abs, order);
+        if (stage_ranks) {
+            // ranks by gene gathered in shared memory, then written coalesced
+            RankT* s_rk = reinterpret_cast<RankT*>(dyn_smem);
+            for (int pos = tid; pos < G; pos += kThreads) {
+                const uint32_t gene = vA[pos];
+                s_rk[gene] = (RankT)pos;
+                sorted_abs[b + pos] = cuabs(value_of<T>(kA[pos], descending));
+                if (order) order[b + pos] = gene;
+            }
+            __syncthreads();
+            for (int g = tid; g < G; g += kThreads) ranks[b + g] = s_rk[g];
+        } else {
+            for (int pos = tid; pos < G; pos += kThreads)
+                emit<RankT, T>(b, pos, vA[pos], value_of<T>(kA[pos], descending), ranks, sorted_abs, order);
+        }
         __syncthreads();
         // restore the buffer roles for the next permutation
         kA = reinterpret_cast<U*>(mine);
@@ -369,9 +383,17 @@ cudaError_t launch_sort_t(const T* keys, int G, int P, bool desc, const SortBuff
     }
     const int grid = P < num_sms() ? P : num_sms();
     if (o.scratch_bytes < sort_scratch_bytes<T>(G, P)) return cudaErrorInvalidValue;
-    sort_tiled_kernel<T, RankT><<<grid, kThreads, 0, st>>>(keys, G, P, desc, static_cast<RankT*>(o.ranks),
-                                                          static_cast<T*>(o.sorted_abs), o.order,
-                                                          static_cast<unsigned char*>(o.scratch));
+    // stage the ranks by gene in shared memory when they fit beside the
+    // kernel's static counters (~33 KB)
+    const size_t rbytes = sizeof(RankT) * (size_t)G;
+    const bool stage = rbytes <= 160 * 1024;
+    const size_t dyn = stage ? rbytes : 0;
+    auto kern = sort_tiled_kernel<T, RankT>;
+    // opt in every time: static (~35 KB) + dynamic may pass the 48 KB default
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, kThreads, dyn, st>>>(keys, G, P, desc, static_cast<RankT*>(o.ranks), static_cast<T*>(o.sorted_abs),
+                                      o.order, static_cast<unsigned char*>(o.scratch), stage);
     launches_add(1);
     return cudaGetLastError();
 }
