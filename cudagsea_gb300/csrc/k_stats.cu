@@ -149,20 +149,22 @@ __global__ void stats_fwer_kernel(int K, int64_t P, const typename RadixKey<T>::
 template <class T>
 __device__ __forceinline__ int side_of(T s) { return s > T(0) ? 0 : (s <= T(0) ? 1 : -1); }
 
+// one warp per set; the lanes stride over the other sets and the counts are
+// warp-reduced
 template <class T>
 __global__ void stats_fdr_obs_kernel(int K, const T* __restrict__ out, unsigned long long* __restrict__ cnt_obs,
                                      unsigned long long* __restrict__ lcount, T* __restrict__ sorted_pos,
                                      T* __restrict__ sorted_neg, unsigned long long* __restrict__ totals) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (k >= K) return;
     const T s = out[K + k];
     // membership in the two sorted arrays: o >= 0 (positive), o <= 0 (negative)
     for (int side = 0; side < 2; side++) {
         const bool in = side == 0 ? (s >= T(0)) : (s <= T(0));
-        if (!in) continue;
+        if (!in) continue;  // warp-uniform
         const T key = side == 0 ? s : -s;
         unsigned long long less = 0, eq_before = 0;
-        for (int j = 0; j < K; j++) {
+        for (int j = lane; j < K; j += 32) {
             const T o = out[K + j];
             const bool jin = side == 0 ? (o >= T(0)) : (o <= T(0));
             if (!jin) continue;
@@ -170,23 +172,30 @@ __global__ void stats_fdr_obs_kernel(int K, const T* __restrict__ out, unsigned 
             less += oj < key;
             eq_before += (oj == key) && (j < k);
         }
-        (side == 0 ? sorted_pos : sorted_neg)[less + eq_before] = key;
-        atomicAdd(&totals[2 + side], 1ull);
-        if (side_of(s) == side) {
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) {
+            less += __shfl_xor_sync(kFullMask, less, o);
+            eq_before += __shfl_xor_sync(kFullMask, eq_before, o);
+        }
+        if (lane == 0) {
+            (side == 0 ? sorted_pos : sorted_neg)[less + eq_before] = key;
+            atomicAdd(&totals[2 + side], 1ull);
             // observed count on the set's own side: #{keys >= key} = m - less
-            lcount[k] = less;
+            if (side_of(s) == side) lcount[k] = less;
         }
     }
     const int sd = side_of(s);
     if (sd >= 0) {
         const T key = sd == 0 ? s : -s;
         unsigned long long ge = 0;
-        for (int j = 0; j < K; j++) {
+        for (int j = lane; j < K; j += 32) {
             const T o = out[K + j];
             const bool jin = sd == 0 ? (o >= T(0)) : (o <= T(0));
             ge += jin && ((sd == 0 ? o : -o) >= key);
         }
-        cnt_obs[k] = ge;
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) ge += __shfl_xor_sync(kFullMask, ge, o);
+        if (lane == 0) cnt_obs[k] = ge;
     }
 }
 
@@ -341,8 +350,8 @@ cudaError_t launch_stats_ragged(const T* es, int K, int64_t ld, const int64_t* c
     stats_extrema_kernel<T><<<dim3((unsigned)((p_fwer + 127) / 128), (K + kExtremaSets - 1) / kExtremaSets), 128, 0,
                               st>>>(es, K, ld, p_fwer, fac, mx, mn);
     stats_fwer_kernel<T><<<(K + wpb - 1) / wpb, wpb * 32, 0, st>>>(K, p_fwer, mx, mn, stats);
-    stats_fdr_obs_kernel<T><<<(K + 127) / 128, 128, 0, st>>>(K, stats, cnt_obs, lcount, sorted_pos, sorted_neg,
-                                                              totals);
+    stats_fdr_obs_kernel<T><<<(K + wpb - 1) / wpb, wpb * 32, 0, st>>>(K, stats, cnt_obs, lcount, sorted_pos,
+                                                                       sorted_neg, totals);
     if (ld > 1) {
         const int64_t need = (ld - 1 + kHistCols - 1) / kHistCols;
         const unsigned chunks = (unsigned)(need < 65535 ? need : 65535);
