@@ -136,3 +136,38 @@ def test_no_cpu_fallback_without_gpu():
     with pytest.raises(N.GseaError) as e:
         api.GSEA(t, [0, 0, 1, 1], {"a": ["g0", "g1"]}, 10, "twopass_signal2noise")
     assert e.value.status in (3, 5)
+
+
+def test_new_entry_points_check_arguments_without_a_gpu():
+    """Host-side validation of the batch, set-mapping, tuning and allocator
+    entry points (no device touched)."""
+    L = N.lib()
+    cfgs = (N.Config * 2)()
+    for c in cfgs:
+        L.gsea_config_init(ctypes.byref(c))
+        c.num_genes, c.num_samples, c.num_sets, c.num_perms = 100, 10, 3, 5
+    cfgs[1].precision = 64
+    h = ctypes.c_void_p()
+    assert L.gsea_batch_create(2, cfgs, 0, ctypes.byref(h)) == 1       # mixed precision
+    cfgs[1].precision = 32
+    cfgs[1].num_genes = 70000
+    assert L.gsea_batch_create(2, cfgs, 0, ctypes.byref(h)) == 7       # G > 65,536: unsupported
+    assert L.gsea_batch_create(0, cfgs, 0, ctypes.byref(h)) == 1
+    assert L.gsea_batch_execute(None, None) == 1
+    # set mapping: bad offsets are rejected before any device work
+    genes = (ctypes.c_char_p * 2)(b"a", b"b")
+    mem = (ctypes.c_char_p * 2)(b"a", b"x")
+    off = np.array([0, 2, 1], np.int64)
+    out = np.empty(3, np.int64)
+    assert L.gsea_map_sets(2, genes, 2, N.ptr(off), mem, N.ptr(out), None, 0, None) == 9
+    assert L.gsea_map_sets(0, genes, 0, None, None, N.ptr(out), None, 0, None) == 1
+    # tuning / adaptive defaults
+    t = N.Tuning()
+    L.gsea_tuning_init(ctypes.byref(t))
+    assert (t.metric_pb, t.chosen_tile, t.sort_variant, t.es_warps, t.es_stage) == (0, 0, 0, 0, -1)
+    assert L.gsea_plan_set_tuning(None, ctypes.byref(t)) == 1
+    ap = N.AdaptiveParams()
+    L.gsea_adaptive_params_init(ctypes.byref(ap))
+    assert ap.pilot_perms == 1000 and ap.growth == 2.0 and ap.z == 3.0 and ap.q_call == 0.25
+    assert L.gsea_plan_execute_adaptive(None, None, ctypes.byref(ap), None, None) == 1
+    assert L.gsea_model_train(None, None, None, 0, 1, 1, ctypes.c_float(1e-3), None) == 1
