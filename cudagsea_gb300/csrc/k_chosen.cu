@@ -327,24 +327,53 @@ class_stats_kernel(const unsigned char* __restrict__ A1, const unsigned char* __
 // ---------------------------------------------------------------------------
 // operand preparation
 
-// per gene: mean over all samples and the centred totals (FP64)
+// per gene: the mean over all samples (FP64, kept as FP32: mu_f) and the
+// totals of x - mu_f and (x - mu_f)^2 in FP64 -- centred at the same mu_f as
+// the GEMM operands, so class B = totals - class A is exact up to the
+// accumulation.  Block of 256 threads = 32 genes x 8 sample groups: a warp
+// reads 32 consecutive genes of one sample (coalesced); the 8 partial sums of
+// a gene are added in group order.
 template <class T>
-__global__ void gene_moments_kernel(const T* __restrict__ X, int G, int S, float* __restrict__ mu_f,
-                                    double* __restrict__ t1, double* __restrict__ t2) {
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= G) return;
+__global__ void __launch_bounds__(256) gene_moments_kernel(const T* __restrict__ X, int G, int S,
+                                                           float* __restrict__ mu_f, double* __restrict__ t1,
+                                                           double* __restrict__ t2) {
+    __shared__ double part[8][32], part2[8][32];
+    __shared__ float s_mu[32];
+    const int gi = threadIdx.x & 31, j = threadIdx.x >> 5;
+    const int g = blockIdx.x * 32 + gi;
+    const bool gv = g < G;
     double s = 0.0;
-    for (int i = 0; i < S; i++) s += (double)X[(size_t)i * G + g];
-    const double mu = s / S;
-    double a = 0.0, b = 0.0;
-    for (int i = 0; i < S; i++) {
-        const double d = (double)X[(size_t)i * G + g] - mu;
-        a += d;
-        b += d * d;
+    if (gv)
+        for (int i = j; i < S; i += 8) s += (double)X[(size_t)i * G + g];
+    part[j][gi] = s;
+    __syncthreads();
+    if (j == 0) {
+        double tot = 0.0;
+        for (int k = 0; k < 8; k++) tot += part[k][gi];
+        s_mu[gi] = (float)(tot / S);
     }
-    mu_f[g] = (float)mu;
-    t1[g] = a;
-    t2[g] = b;
+    __syncthreads();
+    const double mu = (double)s_mu[gi];
+    double a = 0.0, b = 0.0;
+    if (gv)
+        for (int i = j; i < S; i += 8) {
+            const double d = (double)X[(size_t)i * G + g] - mu;
+            a += d;
+            b += d * d;
+        }
+    part[j][gi] = a;
+    part2[j][gi] = b;
+    __syncthreads();
+    if (j == 0 && gv) {
+        double ta = 0.0, tb = 0.0;
+        for (int k = 0; k < 8; k++) {
+            ta += part[k][gi];
+            tb += part2[k][gi];
+        }
+        mu_f[g] = s_mu[gi];
+        t1[g] = ta;
+        t2[g] = tb;
+    }
 }
 
 __device__ __forceinline__ void split3(double v, __nv_bfloat16& hi, __nv_bfloat16& mid, __nv_bfloat16& lo) {
@@ -355,26 +384,51 @@ __device__ __forceinline__ void split3(double v, __nv_bfloat16& hi, __nv_bfloat1
     lo = __double2bfloat16(r2);
 }
 
+__device__ __forceinline__ uint4 pack8(const __nv_bfloat16 (&a)[8]) {
+    auto w = [&](int i) {
+        return (uint32_t)__bfloat16_as_ushort(a[i]) | ((uint32_t)__bfloat16_as_ushort(a[i + 1]) << 16);
+    };
+    return make_uint4(w(0), w(2), w(4), w(6));
+}
+
 // A1 (x') and A2 (x'^2) in chunked core-matrix layout; K index = part*S + s.
-// One thread per (gene, sample); the buffers are zeroed beforehand.
+// One thread per (gene, 8 consecutive samples): the 8 values of a part are
+// one 16-byte row segment of a core matrix when part*S + s0 is a multiple of
+// 8 (always when S is), written with one vector store per operand and part;
+// otherwise element by element.  The buffers are zeroed beforehand.
 template <class T>
 __global__ void split_operands_kernel(const T* __restrict__ X, int G, int S, int chunks,
                                       const float* __restrict__ mu_f, unsigned char* __restrict__ A1,
                                       unsigned char* __restrict__ A2) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    const int s = blockIdx.y;
+    const int s0 = blockIdx.y * 8;
     if (g >= G) return;
-    const double d = (double)X[(size_t)s * G + g] - (double)mu_f[g];
-    __nv_bfloat16 p[3], q[3];
-    split3(d, p[0], p[1], p[2]);
-    split3(d * d, q[0], q[1], q[2]);
+    const double mu = (double)mu_f[g];
+    __nv_bfloat16 p[3][8], q[3][8];
+    const int ns = S - s0 < 8 ? S - s0 : 8;
+#pragma unroll
+    for (int e = 0; e < 8; e++) {
+        const double d = e < ns ? (double)X[(size_t)(s0 + e) * G + g] - mu : 0.0;
+        split3(d, p[0][e], p[1][e], p[2][e]);
+        split3(d * d, q[0][e], q[1][e], q[2][e]);
+    }
     const int gt = g / BM, row = g % BM;
     for (int part = 0; part < 3; part++) {
-        const int k = part * S + s;
-        const int c = k / BK, kk = k % BK;
-        const size_t off = ((size_t)gt * chunks + c) * A_CHUNK + core_offset(row, kk);
-        *reinterpret_cast<__nv_bfloat16*>(A1 + off) = p[part];
-        *reinterpret_cast<__nv_bfloat16*>(A2 + off) = q[part];
+        const int k0 = part * S + s0;
+        if ((k0 & 7) == 0 && ns == 8) {
+            const int c = k0 / BK, kk = k0 % BK;
+            const size_t off = ((size_t)gt * chunks + c) * A_CHUNK + core_offset(row, kk);
+            *reinterpret_cast<uint4*>(A1 + off) = pack8(p[part]);  // off is 16-byte aligned (kk % 8 == 0)
+            *reinterpret_cast<uint4*>(A2 + off) = pack8(q[part]);
+        } else {
+            for (int e = 0; e < ns; e++) {
+                const int k = k0 + e;
+                const int c = k / BK, kk = k % BK;
+                const size_t off = ((size_t)gt * chunks + c) * A_CHUNK + core_offset(row, kk);
+                *reinterpret_cast<__nv_bfloat16*>(A1 + off) = p[part][e];
+                *reinterpret_cast<__nv_bfloat16*>(A2 + off) = q[part][e];
+            }
+        }
     }
 }
 
@@ -414,8 +468,9 @@ cudaError_t launch_chosen_prepare(const T* X, int G, int S, float* mu, double* t
     cudaError_t e = cudaMemsetAsync(A1, 0, ab, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(A2, 0, ab, st);
     if (e != cudaSuccess) return e;
-    chosen::gene_moments_kernel<T><<<(G + 127) / 128, 128, 0, st>>>(X, G, S, mu, t1, t2);
-    chosen::split_operands_kernel<T><<<dim3((G + 127) / 128, S), 128, 0, st>>>(X, G, S, chosen_chunks(S), mu, A1, A2);
+    chosen::gene_moments_kernel<T><<<(G + 31) / 32, 256, 0, st>>>(X, G, S, mu, t1, t2);
+    chosen::split_operands_kernel<T><<<dim3((G + 127) / 128, (S + 7) / 8), 128, 0, st>>>(X, G, S, chosen_chunks(S), mu,
+                                                                                     A1, A2);
     launches_add(2);
     return cudaGetLastError();
 }
