@@ -70,6 +70,9 @@ def parse():
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the adaptive forms (sequential rule with and without the learned prior)")
     ap.add_argument("--pilot", type=int, default=250, help="pilot permutations of the adaptive forms")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the automatic launch configuration (by default each form's plan is autotuned on a "
+                         "sample of its permutations before the warm-up, outside the timed region)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU-baseline sample time")
     return ap.parse_args()
 
@@ -458,6 +461,7 @@ def run_ours(args):
         plan = api.Plan(d.num_genes, d.num_samples, K, P, args.metric, precision=args.precision, form=form,
                         perm_offset=rank * P, device=local)
         plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+        tuning = plan.autotune() if not args.no_autotune else (plan.get_tuning(), None)
         plan.set_profiling(True)
         for _ in range(args.warmup):
             plan.execute(stream.cuda_stream)
@@ -491,7 +495,8 @@ def run_ours(args):
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             mean_ms = float(t.item())
         measured[form_name] = {"mean_ms": mean_ms, "value": world * K * P / (mean_ms / 1e3),
-                               "stages": {k: v / args.steps for k, v in stage_sum.items()}, "launches": launches}
+                               "stages": {k: v / args.steps for k, v in stage_sum.items()}, "launches": launches,
+                               "tuning": tuning[0]}
         plans[form_name] = plan
         if form_name == forms[-1]:
             clk = c
@@ -575,8 +580,8 @@ def run_ours(args):
             "config": {"workload": d.name, "metric_string": args.metric, "form": head,
                        "precision": args.precision, "l2": "256 MB write between timed steps",
                        "parallelism": f"perm-shard x{world}"},
-            "forms": {k: ({"value": v["value"], "ms_per_step": v["mean_ms"], "stages_ms": v["stages"]}
-                          if "stages" in v else v) for k, v in measured.items()},
+            "forms": {k: ({"value": v["value"], "ms_per_step": v["mean_ms"], "stages_ms": v["stages"],
+                           "tuning": v["tuning"]} if "stages" in v else v) for k, v in measured.items()},
             "chosen_over_plain": (measured["chosen"]["value"] / measured["plain"]["value"]
                                   if "chosen" in measured else None),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

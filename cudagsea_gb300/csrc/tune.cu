@@ -204,7 +204,9 @@ int gsea_plan_autotune(gsea_plan p, int64_t sample_perms, gsea_tuning* best, dou
     GSEA_CUDA(cudaSetDevice(p->device), "cudaSetDevice");
     int sms = 1;
     GSEA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device), "device attribute");
-    int64_t n = sample_perms ? sample_perms : 2 * (int64_t)sms;
+    // default sample: the plan's own batch (launch shapes depend on it), at
+    // most 1,024 permutations and at least two per SM
+    int64_t n = sample_perms ? sample_perms : std::max<int64_t>(2 * (int64_t)sms, std::min<int64_t>(p->pb, 1024));
     n = std::min(n, p->pb);
     return p->cfg.precision == 64 ? autotune_t<double>(p, n, kMetric | kSort | kEs, best, ms_out)
                                   : autotune_t<float>(p, n, kMetric | kSort | kEs, best, ms_out);

@@ -238,7 +238,8 @@ void gsea_tuning_init(gsea_tuning* t);
 int gsea_plan_set_tuning(gsea_plan plan, const gsea_tuning* t);
 int gsea_plan_get_tuning(gsea_plan plan, gsea_tuning* t);
 /* Times every candidate of every stage on the plan's inputs (sample_perms
- * permutations, at most one device batch; 0 = 2 x the SM count), keeps the
+ * permutations, at most one device batch; 0 = the plan's device batch up to
+ * 1,024 permutations, at least 2 x the SM count), keeps the
  * fastest of each stage in the plan and returns it in *best (may be NULL).
  * ms_out (may be NULL) receives the fastest time of the metric, sort and ES
  * stages on the sample.  Overwrites the first sample_perms columns of the
