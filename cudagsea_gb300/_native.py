@@ -110,6 +110,10 @@ SIGNATURES = [
                                     ctypes.c_char_p]),
     ("gsea_proxy_run", ctypes.c_int, [ctypes.c_int, _p, _i64, _i64, _p, _p, _i64, _p, _p, ctypes.c_char_p, _i64,
                                       ctypes.c_int, ctypes.c_int, ctypes.c_char_p, _p]),
+    ("gsea_shard_sum", ctypes.c_int, [_p, _i64, _i64, _i64, ctypes.c_int, _p, _p, _p]),
+    ("gsea_shard_head", ctypes.c_int, [_p, _p, _i64, _i64, ctypes.c_int, _p, _p]),
+    ("gsea_shard_partial", ctypes.c_int, [_p, _i64, _i64, _i64, ctypes.c_int, _i64, _p, _p, _p, _p]),
+    ("gsea_shard_finish", ctypes.c_int, [_p, _i64, _i64, ctypes.c_int, _p, _p, _p, _p]),
     ("gsea_map_sets", ctypes.c_int, [_i64, _p, _i64, _p, _p, _p, _p, _i64, ctypes.POINTER(_i64)]),
     ("gsea_plan_create", ctypes.c_int, [ctypes.POINTER(Config), ctypes.POINTER(_p)]),
     ("gsea_plan_destroy", ctypes.c_int, [_p]),

@@ -143,6 +143,31 @@ int gsea_proxy_run(int precision, const void* exprs, int64_t num_genes, int64_t 
                    const char* metric, int64_t num_perms, int sort_direction, int swap_labels,
                    const char* dump_filename, void* result_out);
 
+/* ---- statistics of a run split over ranks (permutation shards) --------
+ *      The reference computes final_statistics once on the whole [K][P]
+ *      matrix (src/include/statistics.cuh:46-117).  A rank holding
+ *      permutations [first, first + count) (device ES columns, row stride ld)
+ *      contributes O(K) partial results instead, and the merged statistics
+ *      are bit-identical to a single run's:
+ *        1. gsea_shard_sum: continues the sequential sum of |ES| over its
+ *           columns from `init` (the previous rank's result; NULL on the rank
+ *           holding permutation 0) -- chained over the ranks in order;
+ *        2. gsea_shard_head: head = [ES, NES, fac] (3K) from the observed
+ *           scores (column 0 of the first rank) and the chained total;
+ *        3. gsea_shard_partial: counts = [NP counts (K), FWER counts (K)] and
+ *           hist = FDR null histograms [2(K+2)] + null totals [2] of its
+ *           columns -- summed over the ranks (integers: exact);
+ *        4. gsea_shard_finish: stats [5K] from head and the summed counts.
+ *      Device pointers; `stream` a cudaStream_t (NULL = default stream).   */
+int gsea_shard_sum(const void* es, int64_t num_sets, int64_t count, int64_t ld, int precision, const void* init,
+                   void* sum, void* stream);
+int gsea_shard_head(const void* es_obs, const void* sum, int64_t num_sets, int64_t num_perms, int precision,
+                    void* head, void* stream);
+int gsea_shard_partial(const void* es, int64_t num_sets, int64_t count, int64_t ld, int precision, int64_t first_perm,
+                       const void* head, uint64_t* counts, double* hist, void* stream);
+int gsea_shard_finish(const void* head, int64_t num_sets, int64_t num_perms, int precision, const uint64_t* counts,
+                      double* hist, void* stats, void* stream);
+
 /* ---- gene-set membership on the device (replaces create_bitmaps,
  *      src/include/create_bitmaps.cuh:13-65, which rebuilds host bitmaps for
  *      every 32/64-set batch of every permutation batch).  Gene symbols are

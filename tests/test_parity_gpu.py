@@ -359,3 +359,42 @@ def test_device_set_mapping_matches_host_rules(gpu):
         exp_off.append(len(exp))
     assert np.array_equal(off, np.array(exp_off))
     assert np.array_equal(gs, np.array(exp, np.int32))
+
+
+@pytest.mark.parametrize("precision,shards", [(32, 3), (64, 2)])
+def test_shard_partial_statistics_on_device(gpu, precision, shards):
+    """The library's shard kernels, ranks emulated in one process (the
+    exchange replaced by passing tensors on): the merged statistics equal the
+    single plan's bit for bit."""
+    import torch
+    from cudagsea_gb300.shard import DeviceOps, shard_range
+    d = synthetic.make(3000, 30, 60, 700, seed=12, n_class_b=14, sd_range=(0.5, 2.0), n_shift=40,
+                       shift_range=(0.3, 1.0), set_min=10, set_max=200, enriched_frac=0.2)
+    P = d.num_perms
+    ref = api.Plan(d.num_genes, d.num_samples, d.num_sets, P, 8, precision=precision)
+    ref.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+    ref.execute()
+    _, st_ref = ref.read(es=False)
+    ref.close()
+    ops = DeviceOps(precision)
+    parts = []
+    for r in range(shards):
+        first, count = shard_range(P, r, shards)
+        plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, count, 8, precision=precision, perm_offset=first)
+        plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+        plan.execute()
+        es, _ = plan.read(stats=False)
+        plan.close()
+        parts.append((first, torch.from_numpy(es).cuda()))
+    total = None
+    for _, es in parts:
+        total = ops.chain_sum(es, total)
+    head = ops.head(ops.observed(parts[0][1]), total, P)
+    counts = hist = None
+    for first, es in parts:
+        c, h = ops.partial(es, first, head)
+        counts = c if counts is None else counts + c
+        hist = h if hist is None else hist + h
+    st = ops.finish(head, P, counts, hist).cpu().numpy()
+    u = np.uint64 if precision == 64 else np.uint32
+    assert np.array_equal(st.view(u), st_ref.view(u))

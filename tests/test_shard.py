@@ -59,3 +59,37 @@ def test_two_rank_gather_equals_single_run(tmp_path, P):
     es_full, st_full = oracle.gsea(8, d.exprs, d.labels, d.set_offsets, d.set_genes, P)
     np.testing.assert_array_equal(merged, es_full)
     np.testing.assert_array_equal(oracle.stats(merged), st_full)
+
+
+def _merge_worker(rank, world, port, P, out_dir):
+    import torch.distributed as dist
+    import oracle
+    from oracle.shard import OracleOps
+    from cudagsea_gb300 import synthetic
+    from cudagsea_gb300.shard import merge_stats, shard_range
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+    d = synthetic.make(400, 16, 12, P, seed=9, n_class_b=8, set_min=5, set_max=40)
+    first, count = shard_range(P, rank, world)
+    keys = oracle.metric(8, d.exprs, d.labels, count, shift=first)
+    sk, order = oracle.sort(keys)
+    es_local = oracle.es(sk, order, d.set_offsets, d.set_genes)
+    st = merge_stats(OracleOps(32), es_local, first, P)
+    np.save(os.path.join(out_dir, f"stats{rank}.npy"), st)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("world,P", [(2, 64), (3, 50)])
+def test_partial_statistics_merge_equals_single_run(tmp_path, world, P):
+    """O(K) merge over gloo ranks (sequential |ES| sum chained rank to rank,
+    counts and FDR histograms summed): every rank gets the single run's
+    statistics bit for bit."""
+    import oracle
+    from cudagsea_gb300 import synthetic
+    mp.start_processes(_merge_worker, args=(world, _free_port(), P, str(tmp_path)), nprocs=world,
+                       start_method="spawn")
+    d = synthetic.make(400, 16, 12, P, seed=9, n_class_b=8, set_min=5, set_max=40)
+    _, st_full = oracle.gsea(8, d.exprs, d.labels, d.set_offsets, d.set_genes, P)
+    for r in range(world):
+        st = np.load(tmp_path / f"stats{r}.npy")
+        np.testing.assert_array_equal(st.view(np.uint32), st_full.view(np.uint32))
