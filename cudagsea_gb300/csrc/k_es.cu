@@ -442,7 +442,7 @@ inline int es_region_words(int G, int wpl) { return wpl > 0 ? wpl * 32 : (G + 31
 inline int es_wpl(int G, bool ranks16) {
     const int need = (((G + 31) >> 5) + 31) >> 5;
     if (!ranks16) return 0;
-    for (int w : {4, 8, 12, 16, 20})
+    for (int w : {4, 8, 12, 16, 20, 24, 32})
         if (need <= w) return w;
     return 0;
 }
@@ -471,16 +471,25 @@ template <class T, class RankT, int WARPS, bool STAGE>
 cudaError_t launch_es_w(const RankT* ranks, const T* sorted_abs, int G, int P, const int64_t* off,
                         const int32_t* genes, const int32_t* order, const T* decay, int K, T* es, int64_t stride,
                         int64_t col0, int grid, cudaStream_t st) {
-    // words per lane for the register-resident list procedure (u16 positions)
-    switch (es_wpl(G, sizeof(RankT) == 2)) {
-        case 4: return launch_es_v<T, RankT, WARPS, STAGE, 4>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-        case 8: return launch_es_v<T, RankT, WARPS, STAGE, 8>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-        case 12: return launch_es_v<T, RankT, WARPS, STAGE, 12>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-        case 16: return launch_es_v<T, RankT, WARPS, STAGE, 16>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-        case 20: return launch_es_v<T, RankT, WARPS, STAGE, 20>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-        default: break;
+    // words per lane for the register-resident list procedure (u16 positions);
+    // 32-bit ranks (G > 65,536) always take the general procedure
+    if constexpr (sizeof(RankT) == 4) {
+        return launch_es_v<T, RankT, WARPS, STAGE, 0>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride,
+                                                      col0, grid, st);
+    } else {
+        switch (es_wpl(G, true)) {
+            case 4: return launch_es_v<T, RankT, WARPS, STAGE, 4>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+            case 8: return launch_es_v<T, RankT, WARPS, STAGE, 8>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+            case 12: return launch_es_v<T, RankT, WARPS, STAGE, 12>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+            case 16: return launch_es_v<T, RankT, WARPS, STAGE, 16>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+            case 20: return launch_es_v<T, RankT, WARPS, STAGE, 20>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+            case 24: return launch_es_v<T, RankT, WARPS, STAGE, 24>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+            case 32: return launch_es_v<T, RankT, WARPS, STAGE, 32>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+            default: break;
+        }
+        return launch_es_v<T, RankT, WARPS, STAGE, 0>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride,
+                                                      col0, grid, st);
     }
-    return launch_es_v<T, RankT, WARPS, STAGE, 0>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
 }
 
 template <class T, class RankT>
@@ -549,6 +558,8 @@ cudaError_t launch_es_batch_w(const EsTask<T>* tasks, const int64_t* item_end, i
         case 12: return launch_es_batch_v<T, WARPS, STAGE, 12>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
         case 16: return launch_es_batch_v<T, WARPS, STAGE, 16>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
         case 20: return launch_es_batch_v<T, WARPS, STAGE, 20>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
+        case 24: return launch_es_batch_v<T, WARPS, STAGE, 24>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
+        case 32: return launch_es_batch_v<T, WARPS, STAGE, 32>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
         case 0: return launch_es_batch_v<T, WARPS, STAGE, 0>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
         default: return cudaErrorInvalidValue;
     }
