@@ -125,6 +125,13 @@ void free_plan_buffers(gsea_plan_s* p) {
     p->feat = p->pred = nullptr;
 }
 
+void drop_graph(gsea_plan_s* p) {
+    if (p->graph_exec) cudaGraphExecDestroy(p->graph_exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    p->graph_exec = nullptr;
+    p->graph = nullptr;
+}
+
 template <class Ptr>
 int dev_alloc(Ptr** ptr, size_t bytes, const char* what) {
     if (injected("alloc")) return fail(GSEA_ERR_INJECTED, std::string("injected allocation failure: ") + what);
@@ -156,6 +163,7 @@ int upload_sets(gsea_plan_s* p, const int64_t* off, const int32_t* genes, cudaSt
         if (off[k + 1] < off[k]) return fail(GSEA_ERR_INVALID_INPUT, "set_offsets must be non-decreasing");
     const int64_t nnz = off[K];
     if (nnz > p->nnz_cap) {
+        drop_graph(p);  // the captured launches point at the old buffer
         if (p->set_genes) cudaFree(p->set_genes);
         p->set_genes = nullptr;
         int rc = dev_alloc(&p->set_genes, sizeof(int32_t) * (size_t)nnz, "set genes");
@@ -279,21 +287,49 @@ int run_range_t(gsea_plan_s* p, cudaStream_t st, int64_t lo, int64_t hi, const i
 }
 
 template <class T>
-int execute_t(gsea_plan_s* p, cudaStream_t st) {
-    const gsea_config& c = p->cfg;
-    const int K = (int)c.num_sets;
-    const int64_t P = c.num_perms;
-    if (injected("launch")) return fail(GSEA_ERR_INJECTED, "injected launch failure");
-    gsea::launches_take();
-    p->events_used = 0;
+int record_t(gsea_plan_s* p, cudaStream_t st) {
+    const int K = (int)p->cfg.num_sets;
+    const int64_t P = p->cfg.num_perms;
     int rc = mark(p, -1, st);
     if (rc) return rc;
     if ((rc = run_range_t<T>(p, st, 0, P, p->set_order, K))) return rc;
     GSEA_CUDA(gsea::launch_stats<T>(static_cast<const T*>(p->es), K, P, static_cast<T*>(p->stats),
                                     p->stats_scratch, st),
               "statistics kernels");
-    if ((rc = mark(p, 4, st))) return rc;
-    p->last_launches = gsea::launches_take();
+    return mark(p, 4, st);
+}
+
+// One execute.  With stage profiling off, the launches are captured into a
+// CUDA graph on the plan's stream the first time and the graph is replayed
+// on `st` afterwards (one launch instead of ~12).
+template <class T>
+int execute_t(gsea_plan_s* p, cudaStream_t st) {
+    if (injected("launch")) return fail(GSEA_ERR_INJECTED, "injected launch failure");
+    gsea::launches_take();
+    p->events_used = 0;
+    if (p->profile || !p->use_graph) {
+        drop_graph(p);
+        const int rc = record_t<T>(p, st);
+        p->last_launches = gsea::launches_take();
+        return rc;
+    }
+    if (!p->graph_exec) {
+        GSEA_CUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        const int rc = record_t<T>(p, p->stream);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(p->stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            return rc;
+        }
+        GSEA_CUDA(e, "end capture");
+        p->graph = g;
+        p->graph_launches = gsea::launches_take();
+        GSEA_CUDA(cudaGraphInstantiate(&p->graph_exec, g, 0), "graph instantiate");
+    }
+    GSEA_CUDA(cudaGraphLaunch(p->graph_exec, st), "graph launch");
+    p->last_launches = p->graph_launches;
     return GSEA_OK;
 }
 
@@ -324,6 +360,7 @@ int plan_run_range(gsea_plan_s* p, cudaStream_t st, int64_t lo, int64_t hi, cons
                                   : run_range_t<float>(p, st, lo, hi, set_list, n_sets);
 }
 int plan_dev_alloc(void** ptr, size_t bytes, const char* what) { return dev_alloc(ptr, bytes, what); }
+void plan_drop_graph(gsea_plan_s* p) { drop_graph(p); }
 int plan_run_stage1(gsea_plan_s* p, cudaStream_t st) {
     return p->cfg.precision == 64 ? run_range_t<double>(p, st, 0, p->cfg.num_perms, nullptr, 0, false)
                                   : run_range_t<float>(p, st, 0, p->cfg.num_perms, nullptr, 0, false);
@@ -521,6 +558,7 @@ int gsea_plan_destroy(gsea_plan p) {
     cudaSetDevice(p->device);
     cudaStreamSynchronize(p->stream);
     for (cudaEvent_t e : p->events) cudaEventDestroy(e);
+    drop_graph(p);
     free_plan_buffers(p);
     cudaStreamDestroy(p->stream);
     delete p;
@@ -652,6 +690,7 @@ int gsea_plan_set_debug(gsea_plan p, int keep) {
     int rc = use_device(p);
     if (rc) return rc;
     p->debug = keep != 0;
+    drop_graph(p);
     if (p->debug) return alloc_order(p);
     return GSEA_OK;
 }

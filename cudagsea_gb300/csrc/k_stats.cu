@@ -216,13 +216,24 @@ constexpr int kHistCols = kHistThreads * 8;  // null columns per block
 template <class T>
 __global__ void __launch_bounds__(kHistThreads)
 stats_fdr_hist_kernel(const T* __restrict__ es, int64_t ld, const int64_t* __restrict__ counts,
-                      const T* __restrict__ fac, const T* __restrict__ sorted_pos, const T* __restrict__ sorted_neg,
-                      double* __restrict__ hpos, double* __restrict__ hneg, unsigned long long* __restrict__ totals) {
+                      const T* __restrict__ fac, const T* sorted_pos, const T* sorted_neg,
+                      double* __restrict__ hpos, double* __restrict__ hneg, unsigned long long* __restrict__ totals,
+                      bool stage_obs) {
+    extern __shared__ __align__(16) unsigned char hist_smem[];  // [2K] T when staged (dynamic size > 0)
     const int64_t k = blockIdx.x;
     const int64_t n = counts ? counts[k] : ld;
     if (n < 2) return;
     const double w = counts ? (double)(ld - 1) / (double)(n - 1) : 1.0;
     const unsigned npos = (unsigned)totals[2], nneg = (unsigned)totals[3];
+    if (stage_obs) {  // the binary searches then run in shared memory
+        T* s_pos = reinterpret_cast<T*>(hist_smem);
+        T* s_neg = s_pos + npos;
+        for (unsigned i = threadIdx.x; i < npos; i += kHistThreads) s_pos[i] = sorted_pos[i];
+        for (unsigned i = threadIdx.x; i < nneg; i += kHistThreads) s_neg[i] = sorted_neg[i];
+        __syncthreads();
+        sorted_pos = s_pos;
+        sorted_neg = s_neg;
+    }
     const T f = fac[k];
     const T* row = es + k * ld;
     double* wtot = reinterpret_cast<double*>(totals + 4);
@@ -355,8 +366,12 @@ cudaError_t launch_stats_ragged(const T* es, int K, int64_t ld, const int64_t* c
     if (ld > 1) {
         const int64_t need = (ld - 1 + kHistCols - 1) / kHistCols;
         const unsigned chunks = (unsigned)(need < 65535 ? need : 65535);
-        stats_fdr_hist_kernel<T><<<dim3((unsigned)K, chunks), kHistThreads, 0, st>>>(
-            es, ld, counts, fac, sorted_pos, sorted_neg, hpos, hneg, totals);
+        // the sorted observed keys (at most 2K values) in shared memory when
+        // they fit the default 48 KB
+        const size_t obs_bytes = 2 * sizeof(T) * (size_t)K;
+        const bool stage = obs_bytes <= 48 * 1024;
+        stats_fdr_hist_kernel<T><<<dim3((unsigned)K, chunks), kHistThreads, stage ? obs_bytes : 0, st>>>(
+            es, ld, counts, fac, sorted_pos, sorted_neg, hpos, hneg, totals, stage);
     }
     stats_fdr_suffix_kernel<<<2, 1024, 0, st>>>(hpos, hneg, totals);
     stats_fdr_final_kernel<T><<<(K + 255) / 256, 256, 0, st>>>(K, cnt_obs, lcount, hpos, hneg, totals, stats);

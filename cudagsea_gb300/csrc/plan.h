@@ -75,6 +75,12 @@ struct gsea_plan_s {
     void* stats = nullptr;
     void* stats_scratch = nullptr;
     size_t stats_scratch_bytes = 0;
+    // the execute captured as a CUDA graph (replayed until buffers, tuning or
+    // debug change)
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    int64_t graph_launches = 0;
+    bool use_graph = true;
     // adaptive allocation / model features
     double* moments = nullptr;         // mean, sd, skewness of the observed ranking metric
     int32_t* active = nullptr;         // [K] set list of the current adaptive round
@@ -97,6 +103,8 @@ namespace gsea {
 // (row stride num_perms).  No statistics.
 int plan_run_range(gsea_plan_s* p, cudaStream_t st, int64_t lo, int64_t hi, const int32_t* set_list, int n_sets);
 int plan_dev_alloc(void** ptr, size_t bytes, const char* what);
+// forget the captured execute graph (buffers, tuning or debug changed)
+void plan_drop_graph(gsea_plan_s* p);
 // permutation, metric and sort of every permutation (one device batch) without
 // the enrichment kernel; and the statistics of the plan's ES matrix
 int plan_run_stage1(gsea_plan_s* p, cudaStream_t st);

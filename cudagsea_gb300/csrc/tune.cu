@@ -144,6 +144,7 @@ int autotune_t(gsea_plan_s* p, int64_t n64, unsigned stages, gsea_tuning* best_o
     if ((ebest >= 1e30f && (stages & kEs)) || sbest >= 1e30f || mbest >= 1e30f)
         return fail(GSEA_ERR_CUDA, "no launch configuration ran");
     p->tuning = best;
+    gsea::plan_drop_graph(p);
     if (best_out) *best_out = best;
     if (ms_out) {
         ms_out[0] = mbest;
@@ -188,6 +189,7 @@ int gsea_plan_set_tuning(gsea_plan p, const gsea_tuning* t) {
     if (!p || !t) return fail(GSEA_ERR_INVALID_ARGUMENT, "null argument");
     if (!valid(t)) return fail(GSEA_ERR_INVALID_ARGUMENT, "invalid tuning value");
     p->tuning = *t;
+    gsea::plan_drop_graph(p);
     return GSEA_OK;
 }
 

@@ -91,3 +91,28 @@ def test_autotune_keeps_results(gpu, data, form):
     es, st = plan.read()
     assert same(es, ref[1]) and same(st, ref[2])
     plan.close()
+
+
+def test_graph_replay_matches_direct_launches(gpu, data):
+    """An execute is captured into a CUDA graph and replayed (profiling off);
+    replays, re-captures after a tuning change and direct launches (profiling
+    on) all give the same results bit for bit."""
+    import torch
+    plan = api.Plan(data.num_genes, data.num_samples, data.num_sets, data.num_perms, "twopass_signal2noise")
+    plan.set_inputs(data.exprs, data.labels, data.set_offsets, data.set_genes)
+    outs = []
+    plan.execute()
+    outs.append(plan.read())
+    s = torch.cuda.Stream()
+    plan.execute(s.cuda_stream)  # replay on another stream
+    outs.append(plan.read())
+    plan.set_tuning(es_warps=16)  # re-capture
+    plan.execute()
+    outs.append(plan.read())
+    plan.set_profiling(True)      # direct launches
+    plan.execute()
+    outs.append(plan.read())
+    assert plan.last_launches() > 5
+    plan.close()
+    for es, st in outs[1:]:
+        assert same(es, outs[0][0]) and same(st, outs[0][1])
