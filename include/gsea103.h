@@ -181,14 +181,20 @@ int gsea_map_sets(int64_t num_genes, const char* const* gene_symbols, int64_t nu
                   const int64_t* set_symbol_offsets, const char* const* set_symbols, int64_t* set_offsets_out,
                   int32_t* set_genes_out, int64_t capacity, int64_t* nnz_out);
 
-/* ---- plan API: device-resident inputs, repeated execution --------------- */
+/* ---- plan API: device-resident inputs, repeated execution.  Splits
+ *      gsea_proxy<> (src/cudaGSEA_wrapper.cu:179-401), which allocates, runs
+ *      and frees per call (:229-372), into create / set_inputs / execute /
+ *      read, so inputs and buffers stay resident across executes. -------- */
 int gsea_plan_create(const gsea_config* cfg, gsea_plan* out);
 int gsea_plan_destroy(gsea_plan plan);
 /* copy inputs from host memory (synchronous) */
 int gsea_plan_set_inputs(gsea_plan plan, const void* exprs, const uint8_t* labels,
                          const int64_t* set_offsets, const int32_t* set_genes);
 /* run permutation -> metric -> sort -> ES -> statistics on `stream`
- * (a cudaStream_t, NULL = the plan's own stream); asynchronous */
+ * (a cudaStream_t, NULL = the plan's own stream); asynchronous.  The first
+ * execute (and the first after new set buffers, a tuning or debug change)
+ * captures the launches into a CUDA graph on the plan's stream; later ones
+ * replay it.  With stage profiling on, the launches are issued directly. */
 int gsea_plan_execute(gsea_plan plan, void* stream);
 /* one call = upload of all inputs from host + execute + download of the
  * results to host, ordered on the plan's stream and synchronised at the end
