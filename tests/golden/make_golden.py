@@ -23,7 +23,8 @@ Fixtures (compressed .npz):
   tiny.npz             37 genes x 5 samples, 3 sets, 3 permutations
   cli_result_*.txt     "RESULT:" lines of the reference CLI (-cpu) on .gct /
                        .cls / .gmt files of the 2,000 x 40 workload (256
-                       permutations, twopass_signal2noise)
+                       permutations, twopass_signal2noise; single, double and
+                       single with -order ascending)
 """
 from __future__ import annotations
 
@@ -122,12 +123,14 @@ def main():
     d = synthetic.small(num_perms=256)
     with tempfile.TemporaryDirectory() as tmp:
         gct, cls, gmt = broad.write_dataset(os.path.join(tmp, "small"), d)
-        for prec in ("single", "double"):
+        runs = [("single", [], "cli_result_single.txt"), ("double", [], "cli_result_double.txt"),
+                ("single", ["-order", "ascending"], "cli_result_ascending_single.txt")]
+        for prec, extra, fname in runs:
             out = subprocess.run([os.path.join(oracle.REF_DIR, "cudaGSEA_cpu"), "-res", gct, "-cls", cls, "-gmx",
                                   gmt, "-nperm", "256", "-metric", "twopass_signal2noise", "-precision", prec,
-                                  "-cpu"], capture_output=True, text=True, check=True).stdout
+                                  "-cpu"] + extra, capture_output=True, text=True, check=True).stdout
             lines = [l for l in out.splitlines() if l.startswith("RESULT:")]
-            with open(os.path.join(HERE, f"cli_result_{prec}.txt"), "w") as f:
+            with open(os.path.join(HERE, fname), "w") as f:
                 f.write("\n".join(lines) + "\n")
     print("golden fixtures written to", HERE)
 

@@ -66,16 +66,19 @@ def test_reference_error_cases(tmp_path, case, msg):
     assert e.value.status == 6 and msg in str(e.value)
 
 
-@pytest.mark.parametrize("prec", ["single", "double"])
-def test_oracle_reproduces_reference_cli(tmp_path, prec):
-    """The reference CLI's RESULT lines (golden) from the oracle on our parse."""
+@pytest.mark.parametrize("prec,order", [("single", "descending"), ("double", "descending"),
+                                        ("single", "ascending")])
+def test_oracle_reproduces_reference_cli(tmp_path, prec, order):
+    """The reference CLI's RESULT lines (golden) from the oracle on our parse;
+    `-order ascending` sorts the keys ascending and keeps the labels."""
     d = synthetic.small(num_perms=256)
     gct, cls, gmt = broad.write_dataset(str(tmp_path / "s"), d)
     ds = broad.Dataset(gct, cls, gmt)
     double = prec == "double"
     x, labels, off, genes = ds.arrays(64 if double else 32)
-    es, st = oracle.gsea(8, x, labels, off, genes, 256, double=double)
-    names, ref = broad.parse_result_lines(open(os.path.join(H.GOLDEN, f"cli_result_{prec}.txt")).read())
+    es, st = oracle.gsea(8, x, labels, off, genes, 256, double=double, ascending=order == "ascending")
+    fname = f"cli_result_{prec}.txt" if order == "descending" else f"cli_result_{order}_{prec}.txt"
+    names, ref = broad.parse_result_lines(open(os.path.join(H.GOLDEN, fname)).read())
     assert names == ds.set_names()
     K = d.num_sets
     ours = np.stack([st[:K], st[K:2 * K], st[2 * K:3 * K], st[3 * K:4 * K]], axis=1)

@@ -13,17 +13,19 @@ pytestmark = pytest.mark.gpu
 CLI = os.path.join(os.path.dirname(build.LIB), "gsea103")
 
 
-@pytest.mark.parametrize("prec", ["single", "double"])
-def test_cli_matches_reference_result_lines(gpu, tmp_path, prec):
+@pytest.mark.parametrize("prec,order", [("single", "descending"), ("double", "descending"),
+                                        ("single", "ascending")])
+def test_cli_matches_reference_result_lines(gpu, tmp_path, prec, order):
     d = synthetic.small(num_perms=256)
     gct, cls, gmt = broad.write_dataset(str(tmp_path / "s"), d)
     dump = str(tmp_path / "dump")
     out = subprocess.run([CLI, "-res", gct, "-cls", cls, "-gmx", gmt, "-nperm", "256", "-metric",
-                          "twopass_signal2noise", "-precision", prec, "-dump", dump],
+                          "twopass_signal2noise", "-precision", prec, "-order", order, "-dump", dump],
                          capture_output=True, text=True, timeout=300)
     assert out.returncode == 0, out.stdout + out.stderr
     names, ours = broad.parse_result_lines(out.stdout)
-    rnames, ref = broad.parse_result_lines(open(os.path.join(H.GOLDEN, f"cli_result_{prec}.txt")).read())
+    fname = f"cli_result_{prec}.txt" if order == "descending" else f"cli_result_{order}_{prec}.txt"
+    rnames, ref = broad.parse_result_lines(open(os.path.join(H.GOLDEN, fname)).read())
     assert names == rnames
     np.testing.assert_allclose(ours[:, :2], ref[:, :2], atol=1e-5)   # ES, NES
     np.testing.assert_allclose(ours[:, 2:], ref[:, 2:], atol=2.0 / 256)  # NP, FWER
