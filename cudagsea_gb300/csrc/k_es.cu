@@ -22,22 +22,25 @@
 // Work per (set, permutation) is O(G/32 + n) instead of O(G):
 //   * one CTA per permutation stages the rank of every gene and the weight at
 //     every position in shared memory;
-//   * a warp takes the next set from a CTA-wide counter (largest sets first)
-//     and marks its members' ranks in a per-warp bitmap (duplicates collapse);
-//   * the hits are compacted into a rank-ordered list: each lane loads its
-//     own range of bitmap words into registers, a warp scan of their
-//     popcounts places each lane's hits, and the list overwrites the bitmap;
-//   * every lane then takes an equal contiguous slice of the list: it sums the
-//     slice's weights, one warp scan gives each slice its prefix and N_R, and
-//     a second walk over the slice evaluates the candidates exactly.  No lane
-//     idles while another walks a long run of hits.
-//   Sets larger than twice the bitmap's word count (or very large G) take a
-//   general path in which each lane walks its own word range.
+//   * a warp takes the next set from a CTA-wide counter (largest sets first),
+//     marks its members' ranks in a per-warp bitmap (duplicates collapse) and
+//     sums the weights of the marked ranks (N_R);
+//   * each lane owns a contiguous range of bitmap words: their popcounts and
+//     one warp scan give the global index of the lane's first hit, and the
+//     lane walks its hits once, in rank order, with a lane-local prefix of the
+//     weights; its largest and smallest candidates are shifted afterwards by
+//     the weight of the hits before the lane (a second warp scan);
+//   * a warp reduction picks the winner.
+//   With G > 32,768 (or 32-bit ranks) a general procedure walks each lane's
+//   word range twice from shared memory instead.
 //
 // Rounding: fp32 sums are compensated (Kahan in a lane, float-float across
 // lanes), so the fp32 ES stay within a few ulp of the reference's Kahan
-// running sum; the fp64 path is double throughout.
+// running sum (the shift adds one rounding); the fp64 path is double
+// throughout.
 #include <climits>
+
+#include <math_constants.h>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -116,25 +119,28 @@ __device__ __forceinline__ void consider(T val, int pos, T& best, int& bpos) {
 // Per-set procedures.  Both run on one warp with the set's member ranks marked
 // in the warp's bitmap `bm` (G bits) and leave the bitmap all zero.
 
-// Fast procedure: the lane's bitmap words (at most WPL, a multiple of 4,
-// loaded as 16-byte vectors) are held in registers, the hits are compacted
-// into a rank-ordered list of positions that overwrites the start of the
-// bitmap (needs n <= 2*words), then every lane processes an equal contiguous
-// slice of the list -- no lane waits for another's hits.  The slice length is
-// odd so that the lanes' list reads fall into different banks; the first
-// CACHE weights of a slice stay in registers between the two walks.
-// `w0` = lane*WPL: the lane's first word, 16-byte aligned inside the warp's
-// region of WPL*32 words (bits at positions >= G are never set).
-template <class T, int WPL, int CACHE>
-__device__ __forceinline__ T set_score_list(uint32_t* bm, int w0, const T* wt, const T* __restrict__ decay, int G,
-                                            int lane) {
-    uint32_t wr[WPL];
+// Direct procedure (G <= 1024*WPL): the lane's bitmap words (WPL, a multiple
+// of 4, loaded as 16-byte vectors) give its hit count and a mask of its
+// nonzero words; a warp scan of the counts gives the global index of each
+// lane's first hit.  Every lane then walks its own hits once, in rank order,
+// with a lane-local compensated prefix of the weights, and keeps its largest
+// value after a hit and smallest value before one; the weight of the hits in
+// the lanes before it (a second warp scan, after the walk) shifts both by a
+// constant, which leaves their positions unchanged.  The set's total weight
+// `Wt` (every lane) comes from the marking.  Each word is cleared as it is
+// read.  `w0` = lane*WPL: the lane's first word, 16-byte aligned inside the
+// warp's region of WPL*32 words (bits at positions >= G are never set).
+template <class T, int WPL>
+__device__ __forceinline__ T set_score_direct(uint32_t* bm, int w0, const T* wt, const T* __restrict__ decay, int G,
+                                              int lane, const Acc<T>& Wt) {
+    uint32_t nzm = 0u;  // bit i: word w0 + i holds hits
     int cnt = 0;
 #pragma unroll
     for (int i = 0; i < WPL; i += 4) {
-        const uint4 v = *reinterpret_cast<const uint4*>(bm + w0 + i);  // words padded to WPL*32
-        wr[i] = v.x; wr[i + 1] = v.y; wr[i + 2] = v.z; wr[i + 3] = v.w;
+        const uint4 v = *reinterpret_cast<const uint4*>(bm + w0 + i);
         cnt += __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
+        nzm |= (((v.x != 0u) ? 1u : 0u) | ((v.y != 0u) ? 2u : 0u) | ((v.z != 0u) ? 4u : 0u) |
+                ((v.w != 0u) ? 8u : 0u)) << i;
     }
     int incl = cnt;
 #pragma unroll
@@ -143,88 +149,53 @@ __device__ __forceinline__ T set_score_list(uint32_t* bm, int w0, const T* wt, c
         if (lane >= o) incl += y;
     }
     const int n = __shfl_sync(kFullMask, incl, 31);
-    __syncwarp();  // every lane holds its words: the bitmap may be overwritten
-#pragma unroll
-    for (int i = 0; i < WPL; i += 4) {
-        if (wr[i] | wr[i + 1] | wr[i + 2] | wr[i + 3])
-            *reinterpret_cast<uint4*>(bm + w0 + i) = make_uint4(0u, 0u, 0u, 0u);
-    }
-    __syncwarp();
-    uint16_t* list = reinterpret_cast<uint16_t*>(bm);
-    int j = incl - cnt;
-#pragma unroll
-    for (int i = 0; i < WPL; i++) {
-        uint32_t word = wr[i];
-        while (word) {
-            const int bit = __ffs(word) - 1;
-            word &= word - 1;
-            list[j++] = (uint16_t)(((w0 + i) << 5) + bit);
+    const int excl = incl - cnt;  // hits in the lanes before
+    const T inv = n > 0 ? T(1) / Wt.value() : T(0);
+    const T d = decay[n];
+    Acc<T> Wl;  // weight of this lane's hits so far
+    T mx = -CUDART_INF, mn = CUDART_INF;
+    int pmx = -1, pmn = -1;
+    uint32_t cur = 0u;
+    int wi = 0;
+    for (int t = 0; t < cnt; t++) {
+        if (cur == 0u) {  // next nonzero word of the lane
+            wi = __ffs(nzm) - 1;
+            nzm &= nzm - 1;
+            cur = bm[w0 + wi];
+            bm[w0 + wi] = 0u;
         }
+        const int bit = __ffs(cur) - 1;
+        cur &= cur - 1;
+        const int r = ((w0 + wi) << 5) + bit;
+        const T md = -(T)(r - (excl + t)) * d;  // misses before this hit, times the decay
+        const T before = t > 0 ? Wl.scaled_plus(inv, md) : md;
+        Wl.add(wt[r]);
+        const T after = Wl.scaled_plus(inv, md);
+        if (before < mn) { mn = before; pmn = r - 1; }
+        if (after > mx) { mx = after; pmx = r; }
     }
-    __syncwarp();
-    // balanced slices of the rank-ordered hit list
-    int per = (n + 31) >> 5;
-    per |= 1;
-    const int j0 = min(n, lane * per), j1 = min(n, j0 + per);
-    Acc<T> Wl;
-    T wc[CACHE];
-#pragma unroll
-    for (int c = 0; c < CACHE; c++) {
-        wc[c] = j0 + c < j1 ? wt[list[j0 + c]] : T(0);
-        if (j0 + c < j1) Wl.add(wc[c]);
-    }
-    for (int k = j0 + CACHE; k < j1; k++) Wl.add(wt[list[k]]);
     Acc<T> W_incl = Wl;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const Acc<T> y = W_incl.shfl_up(o);
         if (lane >= o) W_incl.merge(y);
     }
-    Acc<T> W = W_incl.shfl_up(1);  // weight of the hits before this slice
-    if (lane == 0) W = Acc<T>();
-    Acc<T> Wt;                      // weight of all hits
-    Wt.hi = __shfl_sync(kFullMask, W_incl.hi, 31);
-    Wt.lo = __shfl_sync(kFullMask, W_incl.lo, 31);
-    const T N_R = Wt.value();
-    const T inv = n > 0 ? T(1) / N_R : T(0);
-    const T d = decay[n];
-    // The largest value is always just after a hit and the smallest just
-    // before one (or at the end): track the two separately.
-    T mx = T(0), mn = T(0);
-    int pmx = -1, pmn = -1;
-#pragma unroll
-    for (int c = 0; c < CACHE; c++) {
-        const int k = j0 + c;
-        if (k < j1) {
-            const int r = list[k];
-            const T md = -(T)(r - k) * d;  // misses before hit k, times the decay
-            const T before = k > 0 ? W.scaled_plus(inv, md) : md;
-            W.add(wc[c]);
-            const T after = W.scaled_plus(inv, md);
-            if (before < mn) { mn = before; pmn = r - 1; }
-            if (after > mx) { mx = after; pmx = r; }
-        }
-    }
-    for (int k = j0 + CACHE; k < j1; k++) {
-        const int r = list[k];
-        const T md = -(T)(r - k) * d;
-        const T before = k > 0 ? W.scaled_plus(inv, md) : md;
-        W.add(wt[r]);
-        const T after = W.scaled_plus(inv, md);
-        if (before < mn) { mn = before; pmn = r - 1; }
-        if (after > mx) { mx = after; pmx = r; }
-    }
+    const Acc<T> W_pre = W_incl.shfl_up(1);  // weight of the hits before this lane's
+    const T shift = excl > 0 ? W_pre.scaled_plus(inv, T(0)) : T(0);
+    mx += shift;
+    mn += shift;
     if (lane == 31) {  // end of the list, after the trailing misses
         const T tail = -(T)(G - n) * d;
         const T end = n > 0 ? Wt.scaled_plus(inv, tail) : tail;
         if (end < mn) { mn = end; pmn = G - 1; }
     }
+    // the largest value is always just after a hit and the smallest just
+    // before one (or at the end): only a positive maximum and a negative
+    // minimum are candidates
     T best = T(0);
     int bpos = -1;
-    if (pmx >= 0) consider<T>(mx, pmx, best, bpos);
-    if (mn < T(0)) consider<T>(mn, pmn, best, bpos);
-    __syncwarp();
-    for (int k = lane; k < (n + 1) / 2; k += 32) bm[k] = 0u;  // the list's words
+    if (pmx >= 0 && mx > T(0)) consider<T>(mx, pmx, best, bpos);
+    if (pmn >= 0 && mn < T(0)) consider<T>(mn, pmn, best, bpos);
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) {
         const T ob = __shfl_xor_sync(kFullMask, best, o);
@@ -334,7 +305,9 @@ __device__ __forceinline__ void es_one_perm(const RankT* rk, const T* wt, int G,
         if (slot >= K) break;
         const int k = set_order ? set_order[slot] : slot;
         const int64_t a = set_off[k], b = set_off[k + 1];
-        // mark the members' ranks (duplicates and unknown ids fall away)
+        // mark the members' ranks (duplicates and unknown ids fall away); the
+        // direct procedure also sums the weights of the newly marked ranks
+        Acc<T> Wm;
         for (int64_t base = a; base < b; base += 128) {
             int g[4];
 #pragma unroll
@@ -346,17 +319,24 @@ __device__ __forceinline__ void es_one_perm(const RankT* rk, const T* wt, int G,
             for (int i = 0; i < 4; i++) {
                 if (g[i] >= 0 && g[i] < G) {
                     const uint32_t r = (uint32_t)rk[g[i]];
-                    atomicOr(&bm[r >> 5], 1u << (r & 31));
+                    const uint32_t bit = 1u << (r & 31);
+                    if (WPL > 0) {
+                        if (!(atomicOr(&bm[r >> 5], bit) & bit)) Wm.add(wt[r]);
+                    } else {
+                        atomicOr(&bm[r >> 5], bit);
+                    }
                 }
             }
         }
         __syncwarp();
         T score;
-        if (WPL > 0 && b - a <= 2 * (int64_t)words)  // the list fits in the bitmap region
-            score = set_score_list<T, (WPL > 0 ? WPL : 4), (sizeof(T) == 4 ? 10 : 6)>(bm, lane * WPL, wt, decay, G,
-                                                                                    lane);
-        else
+        if (WPL > 0) {
+#pragma unroll
+            for (int o = 16; o >= 1; o >>= 1) Wm.merge(Wm.shfl_xor(o));  // the set's weight, every lane
+            score = set_score_direct<T, (WPL > 0 ? WPL : 4)>(bm, lane * WPL, wt, decay, G, lane, Wm);
+        } else {
             score = set_score_walk<T>(bm, w0, w1, wt, decay, G, lane);
+        }
         if (lane == 0) es_col[(int64_t)k * es_stride] = score;
         __syncwarp();
     }
