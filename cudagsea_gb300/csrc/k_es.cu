@@ -274,7 +274,10 @@ __device__ __noinline__ T set_score_walk(uint32_t* bm, int w0, int w1, const T* 
 }
 
 // One permutation on the calling CTA: stage its ranks and weights (STAGE),
-// then warps take sets from the CTA-wide counter until all K are scored.
+// then warps take sets from the CTA-wide counter until the CTA's share is
+// scored.  The share is parts [part_lo, part_hi) of `parts` interleaved parts
+// of the set order (part j: slots j, j + parts, j + 2*parts, ...), so that
+// every part mixes large and small sets; parts = 1 takes every set.
 // s_w / s_rank: staging (STAGE), bm: this warp's zeroed bitmap region.
 // Begins and ends with the CTA in step (the staging may be reused after).
 template <class T, class RankT, int WARPS, bool STAGE, int WPL>
@@ -282,7 +285,8 @@ __device__ __forceinline__ void es_one_perm(const RankT* rk, const T* wt, int G,
                                             const int32_t* __restrict__ set_genes,
                                             const int32_t* __restrict__ set_order, const T* __restrict__ decay, int K,
                                             T* __restrict__ es_col, int64_t es_stride, T* s_w, RankT* s_rank,
-                                            uint32_t* bm, int* next_set) {
+                                            uint32_t* bm, int* next_set, int part_lo = 0, int part_hi = 1,
+                                            int parts = 1) {
     const int tid = threadIdx.x, lane = tid & 31;
     const int words = (G + 31) >> 5;
     const int wpl = WPL > 0 ? WPL : (words + 31) >> 5;  // bitmap words per lane
@@ -302,6 +306,10 @@ __device__ __forceinline__ void es_one_perm(const RankT* rk, const T* wt, int G,
         int slot = 0;
         if (lane == 0) slot = atomicAdd(next_set, 1);
         slot = __shfl_sync(kFullMask, slot, 0);
+        if (parts > 1) {  // i-th set of the share: slots grow with i
+            const int m = part_hi - part_lo;
+            slot = (slot / m) * parts + part_lo + slot % m;
+        }
         if (slot >= K) break;
         const int k = set_order ? set_order[slot] : slot;
         const int64_t a = set_off[k], b = set_off[k + 1];
@@ -371,10 +379,38 @@ es_kernel(const RankT* __restrict__ ranks, const T* __restrict__ sorted_abs, int
     uint32_t* bm;
     es_smem_layout<T, RankT, STAGE>(smem, G, region, s_w, s_rank, bm);
     for (int w = threadIdx.x & 31; w < region; w += 32) bm[w] = 0u;
-    for (int p = blockIdx.x; p < num_perms; p += gridDim.x)
+    // whole permutations in rounds of gridDim.x ...
+    const int grid = gridDim.x;
+    const int full = num_perms / grid;
+    for (int i = 0; i < full; i++) {
+        const int p = blockIdx.x + i * grid;
         es_one_perm<T, RankT, WARPS, STAGE, WPL>(ranks + (int64_t)p * G, sorted_abs + (int64_t)p * G, G, set_off,
                                                   set_genes, set_order, decay, K, es + col0 + p, es_stride, s_w,
                                                   s_rank, bm, &next_set);
+    }
+    // ... then the rem < gridDim.x left over, each cut into `parts` parts
+    // (parts * rem a multiple of gridDim.x where K allows); every CTA takes an
+    // equal contiguous run of the (permutation, part) items, which spans at
+    // most a few permutations, so the last round ends evenly
+    const int rem = num_perms - full * grid;
+    if (rem == 0) return;
+    int a = rem, b = grid;
+    while (b) { const int t = a % b; a = b; b = t; }
+    const int parts = min(grid / a, K);
+    const int64_t items = (int64_t)rem * parts;
+    int64_t lo = items * blockIdx.x / grid;
+    const int64_t hi = items * (blockIdx.x + 1) / grid;
+    while (lo < hi) {
+        const int64_t q = lo / parts;
+        const int j0 = (int)(lo - q * parts);
+        const int64_t left = hi - lo;
+        const int j1 = left < (int64_t)(parts - j0) ? j0 + (int)left : parts;
+        const int p = full * grid + (int)q;
+        es_one_perm<T, RankT, WARPS, STAGE, WPL>(ranks + (int64_t)p * G, sorted_abs + (int64_t)p * G, G, set_off,
+                                                  set_genes, set_order, decay, K, es + col0 + p, es_stride, s_w,
+                                                  s_rank, bm, &next_set, j0, j1, parts);
+        lo += j1 - j0;
+    }
 }
 
 // Persistent multi-instance form: every CTA takes (instance, permutation)
@@ -442,6 +478,11 @@ cudaError_t launch_es_v(const RankT* ranks, const T* sorted_abs, int G, int P, c
     auto kern = es_kernel<T, RankT, WARPS, STAGE, WPL>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    int per_sm = 0;  // resident CTAs per SM: the grid fills the device once
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, WARPS * 32, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidValue;
+    grid *= per_sm;
     kern<<<grid, WARPS * 32, smem, st>>>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0);
     launches_add(1);
     return cudaGetLastError();
@@ -481,7 +522,7 @@ cudaError_t launch_es_t(const RankT* ranks, const T* sorted_abs, int G, int P, c
     cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const size_t cap = (size_t)max_smem - 64;  // static shared counter
-    const int grid = P < sms ? P : sms;
+    const int grid = sms;  // times the resident CTAs per SM; the last round's permutations are split by sets
     // candidates in the automatic order: most warps first, staged before not
     struct Cand { int warps; bool stage; size_t smem; };
     const Cand cands[] = {{32, true, es_smem_bytes<T, RankT, 32, true>(G)},
