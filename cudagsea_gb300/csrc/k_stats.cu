@@ -50,17 +50,34 @@ __global__ void stats_set_kernel(const T* __restrict__ es, int K, int64_t ld, co
     T sum = T(0);
     unsigned long long np = 0;
     const T aes0 = fabs(es0);
-    for (int64_t p0 = 0; p0 < P; p0 += 32) {
-        const int64_t p = p0 + lane;
-        const T v = p < P ? row[p] : T(0);
-        const T av = fabs(v);
-        if (p < P && av >= aes0) np++;
-        const int n = (int)(P - p0 < 32 ? P - p0 : 32);
-        // sequential sum in index order, as the reference's host loop
-        for (int i = 0; i < n; i++) {
-            const T x = __shfl_sync(kFullMask, av, i);
-            sum = Exact<T>::add(sum, x);
+    // blocks of 4 x 32 columns; the next block's loads are in flight while
+    // this block is summed
+    constexpr int kB = 4;
+    T cur[kB];
+#pragma unroll
+    for (int j = 0; j < kB; j++) cur[j] = j * 32 + lane < P ? row[j * 32 + lane] : T(0);
+    for (int64_t p0 = 0; p0 < P; p0 += kB * 32) {
+        T nxt[kB];
+#pragma unroll
+        for (int j = 0; j < kB; j++) {
+            const int64_t q = p0 + kB * 32 + j * 32 + lane;
+            nxt[j] = q < P ? row[q] : T(0);
         }
+#pragma unroll
+        for (int j = 0; j < kB; j++) {
+            const int64_t b = p0 + j * 32;
+            if (b >= P) break;  // warp-uniform
+            const T av = fabs(cur[j]);
+            if (b + lane < P && av >= aes0) np++;
+            const int n = (int)(P - b < 32 ? P - b : 32);
+            // sequential sum in index order, as the reference's host loop
+            for (int i = 0; i < n; i++) {
+                const T x = __shfl_sync(kFullMask, av, i);
+                sum = Exact<T>::add(sum, x);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < kB; j++) cur[j] = nxt[j];
     }
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) np += __shfl_xor_sync(kFullMask, np, o);
@@ -262,6 +279,98 @@ stats_fdr_hist_kernel(const T* __restrict__ es, int64_t ld, const int64_t* __res
     }
 }
 
+// Dense form (every set has all ld columns, unit weights): block b bins an
+// equal contiguous share of the K x (ld - 1) null scores (row-major, column
+// 0 excluded) into shared-memory integer histograms of both sides, against
+// the sorted observed keys staged beside them, and writes them as row b of
+// `partial` (width 2(K+2) + 2: H_pos | H_neg | #null >= 0 | #null <= 0).
+// stats_fdr_hist_sum_kernel adds the rows up column by column: exact integer
+// counts, no global atomics, the same result in any order.
+constexpr int kDenseHistThreads = 512;
+constexpr size_t kDenseHistPartialBytes = size_t(1) << 20;
+constexpr size_t kDenseHistSmemMax = 96 * 1024;
+template <class T>
+__global__ void __launch_bounds__(kDenseHistThreads)
+stats_fdr_hist_dense_kernel(const T* __restrict__ es, int K, int64_t ld, const T* __restrict__ fac,
+                            const T* __restrict__ sorted_pos, const T* __restrict__ sorted_neg,
+                            const unsigned long long* __restrict__ totals, unsigned* __restrict__ partial) {
+    extern __shared__ __align__(16) unsigned char dense_smem[];
+    const int W = 2 * (K + 2) + 2;
+    unsigned* h = reinterpret_cast<unsigned*>(dense_smem);  // W counters
+    T* s_pos = reinterpret_cast<T*>(dense_smem + (((size_t)W * 4 + 15) & ~(size_t)15));
+    const unsigned npos = (unsigned)totals[2], nneg = (unsigned)totals[3];
+    T* s_neg = s_pos + npos;
+    for (int i = threadIdx.x; i < W; i += kDenseHistThreads) h[i] = 0u;
+    for (unsigned i = threadIdx.x; i < npos; i += kDenseHistThreads) s_pos[i] = sorted_pos[i];
+    for (unsigned i = threadIdx.x; i < nneg; i += kDenseHistThreads) s_neg[i] = sorted_neg[i];
+    __syncthreads();
+    const int64_t cols = ld - 1;
+    const int64_t total = (int64_t)K * cols;
+    const int64_t lo = total * blockIdx.x / gridDim.x, hi = total * (blockIdx.x + 1) / gridDim.x;
+    unsigned cpos = 0, cneg = 0;
+    int64_t k = lo / cols;
+    int64_t c = lo - k * cols;  // column - 1 within row k
+    for (int64_t i = lo; i < hi;) {
+        const int64_t run = (cols - c) < (hi - i) ? (cols - c) : (hi - i);  // rest of row k in the share
+        const T f = fac[k];
+        const T* row = es + k * ld + 1 + c;
+        for (int64_t j = threadIdx.x; j < run; j += kDenseHistThreads) {
+            const T v = Exact<T>::mul(row[j], f);
+            if (v >= T(0)) {
+                cpos++;
+                atomicAdd(&h[upper_bound_t(s_pos, npos, v)], 1u);
+            }
+            if (v <= T(0)) {
+                cneg++;
+                atomicAdd(&h[(K + 2) + upper_bound_t(s_neg, nneg, -v)], 1u);
+            }
+        }
+        i += run;
+        k++;
+        c = 0;
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        cpos += __shfl_xor_sync(kFullMask, cpos, o);
+        cneg += __shfl_xor_sync(kFullMask, cneg, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (cpos) atomicAdd(&h[W - 2], cpos);
+        if (cneg) atomicAdd(&h[W - 1], cneg);
+    }
+    __syncthreads();
+    unsigned* out = partial + (size_t)blockIdx.x * W;
+    for (int i = threadIdx.x; i < W; i += kDenseHistThreads) out[i] = h[i];
+}
+
+// column sums of the partial histograms: H_pos, H_neg (contiguous, 2(K+2)
+// doubles) and the null counts per side (totals[4], [5] as doubles)
+__global__ void stats_fdr_hist_sum_kernel(const unsigned* __restrict__ partial, int rows, int K,
+                                          double* __restrict__ hist, unsigned long long* __restrict__ totals) {
+    const int W = 2 * (K + 2) + 2;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= W) return;
+    unsigned long long s = 0;
+    for (int r = 0; r < rows; r++) s += partial[(size_t)r * W + j];
+    if (j < W - 2) hist[j] = (double)s;
+    else reinterpret_cast<double*>(totals + 4)[j - (W - 2)] = (double)s;
+}
+
+template <class T>
+size_t dense_hist_smem(int K) {
+    const size_t W = 2 * ((size_t)K + 2) + 2;
+    return ((W * 4 + 15) & ~(size_t)15) + 2 * sizeof(T) * (size_t)K;
+}
+// rows of the partial histograms (0: the dense form does not apply)
+template <class T>
+int dense_hist_rows(int K, int sms) {
+    if (dense_hist_smem<T>(K) > kDenseHistSmemMax) return 0;
+    const size_t W = 2 * ((size_t)K + 2) + 2;
+    const size_t cap = kDenseHistPartialBytes / (4 * W);
+    const size_t want = 2 * (size_t)(sms > 0 ? sms : 1);
+    return (int)(cap < want ? cap : want);
+}
+
 // in-place suffix sums of the two histograms (one block each)
 __global__ void stats_fdr_suffix_kernel(double* __restrict__ hpos, double* __restrict__ hneg,
                                         const unsigned long long* __restrict__ totals) {
@@ -326,7 +435,11 @@ __global__ void stats_fdr_final_kernel(int K, const unsigned long long* __restri
 
 template <class T>
 size_t stats_scratch_bytes(int K, int64_t P) {
-    return StatsScratch::bytes(K, P, sizeof(T)) + 256;
+    // + the dense histograms' partial rows (at most kDenseHistPartialBytes)
+    const size_t W = 2 * ((size_t)K + 2) + 2;
+    const size_t dense = dense_hist_smem<T>(K) <= kDenseHistSmemMax
+                             ? (kDenseHistPartialBytes / (4 * W)) * 4 * W + 16 : 0;
+    return StatsScratch::bytes(K, P, sizeof(T)) + 256 + dense;
 }
 template size_t stats_scratch_bytes<float>(int, int64_t);
 template size_t stats_scratch_bytes<double>(int, int64_t);
@@ -352,6 +465,7 @@ cudaError_t launch_stats_ragged(const T* es, int K, int64_t ld, const int64_t* c
     double* hpos = reinterpret_cast<double*>(s + off);
     double* hneg = hpos + (K + 2);
     unsigned long long* totals = reinterpret_cast<unsigned long long*>(hneg + (K + 2));
+    unsigned* partial = reinterpret_cast<unsigned*>(s + align16(off + sizeof(double) * (2 * ((size_t)K + 2) + 8)));
     cudaError_t e = cudaMemsetAsync(hpos, 0, sizeof(double) * (2 * ((size_t)K + 2) + 8), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(mx, 0x00, sizeof(U) * (size_t)p_fwer, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(mn, 0xff, sizeof(U) * (size_t)p_fwer, st);
@@ -363,7 +477,23 @@ cudaError_t launch_stats_ragged(const T* es, int K, int64_t ld, const int64_t* c
     stats_fwer_kernel<T><<<(K + wpb - 1) / wpb, wpb * 32, 0, st>>>(K, p_fwer, mx, mn, stats);
     stats_fdr_obs_kernel<T><<<(K + wpb - 1) / wpb, wpb * 32, 0, st>>>(K, stats, cnt_obs, lcount, sorted_pos,
                                                                        sorted_neg, totals);
-    if (ld > 1) {
+    int rows = 0;
+    if (!counts && ld > 1) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        rows = dense_hist_rows<T>(K, sms);
+    }
+    if (rows > 0) {
+        const size_t smem = dense_hist_smem<T>(K);
+        e = cudaFuncSetAttribute(stats_fdr_hist_dense_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+        if (e != cudaSuccess) return e;
+        stats_fdr_hist_dense_kernel<T><<<rows, kDenseHistThreads, smem, st>>>(es, K, ld, fac, sorted_pos, sorted_neg,
+                                                                            totals, partial);
+        const int W = 2 * (K + 2) + 2;
+        stats_fdr_hist_sum_kernel<<<(W + 255) / 256, 256, 0, st>>>(partial, rows, K, hpos, totals);
+    } else if (ld > 1) {
         const int64_t need = (ld - 1 + kHistCols - 1) / kHistCols;
         const unsigned chunks = (unsigned)(need < 65535 ? need : 65535);
         // the sorted observed keys (at most 2K values) in shared memory when
@@ -375,7 +505,7 @@ cudaError_t launch_stats_ragged(const T* es, int K, int64_t ld, const int64_t* c
     }
     stats_fdr_suffix_kernel<<<2, 1024, 0, st>>>(hpos, hneg, totals);
     stats_fdr_final_kernel<T><<<(K + 255) / 256, 256, 0, st>>>(K, cnt_obs, lcount, hpos, hneg, totals, stats);
-    launches_add(ld > 1 ? 7 : 6);
+    launches_add(rows > 0 ? 8 : (ld > 1 ? 7 : 6));
     return cudaGetLastError();
 }
 template cudaError_t launch_stats_ragged<float>(const float*, int, int64_t, const int64_t*, int64_t, float*, void*,
