@@ -280,6 +280,8 @@ def run_adaptive(args, d, full_plan, stream, flush, local):
                      "scores_per_s": res.report["scores"] / mean_s,
                      "scores_fraction": res.report["scores"] / (K * P), "pilot_perms": args.pilot,
                      "rounds": res.report["rounds"], "stop_p": res.report["stop_p"],
+                     "stopped_after_pilot": res.report["stopped_pilot"], "stopped_by_fdr_bound": res.report["stopped_q"],
+                     "full_sets": res.report["full_sets"],
                      "model_used": res.report["model_used"], "calls": len(calls), "calls_full": len(calls_full),
                      "call_flips": len(calls ^ calls_full)}
         plan.close()
@@ -347,7 +349,8 @@ def run_learned(args):
         res[name] = {"s_per_run": mean, "value_equivalent": K * P / mean, "scores_per_s": r.report["scores"] / mean,
                      "scores_fraction": r.report["scores"] / (K * P), "rounds": r.report["rounds"],
                      "stop_p": r.report["stop_p"], "stopped_after_pilot": r.report["stopped_pilot"],
-                     "full_sets": r.report["full_sets"], "model_used": r.report["model_used"],
+                     "stopped_by_fdr_bound": r.report["stopped_q"], "full_sets": r.report["full_sets"],
+                     "model_used": r.report["model_used"], "prior_sets_agreed": r.report["prior_agreed"],
                      "calls": len(calls), "calls_full": len(calls_full), "call_flips": len(flips),
                      "flip_q_full": [float(full_stats[4][k]) for k in flips[:10]]}
         plan.close()

@@ -70,6 +70,7 @@ class AdaptiveParams(ctypes.Structure):
         ("p_floor", ctypes.c_double),
         ("prior_cap", ctypes.c_double),
         ("fallback_tol", ctypes.c_double),
+        ("q_margin", ctypes.c_double),
     ]
 
 
@@ -82,6 +83,9 @@ class AdaptiveReport(ctypes.Structure):
         ("stop_p", ctypes.c_double),
         ("model_used", ctypes.c_int32),
         ("model_mean_err", ctypes.c_double),
+        ("prior_sets", ctypes.c_int64),
+        ("prior_agreed", ctypes.c_int64),
+        ("stopped_q", ctypes.c_int64),
     ]
 
 
@@ -158,6 +162,7 @@ SIGNATURES = [
                                                   ctypes.POINTER(AdaptiveReport)]),
     ("gsea_adaptive_decide", ctypes.c_int, [_i64, _p, _p, _p, _p, ctypes.c_double, ctypes.c_double, _p]),
     ("gsea_stats_ragged", ctypes.c_int, [_p, _i64, _i64, _p, _i64, ctypes.c_int, _p, _p]),
+    ("gsea_fdr_lower_bound", ctypes.c_int, [_p, _i64, _i64, _p, _i64, _p, ctypes.c_double, ctypes.c_int, _p, _p, _p]),
     ("gsea_dataset_load", ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(_p)]),
     ("gsea_dataset_dims", ctypes.c_int, [_p, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_i64),
                                          ctypes.POINTER(_i64)]),

@@ -197,3 +197,19 @@ def stats_ragged(es, counts, p_fwer: int):
     out = torch.empty(5 * K, dtype=es.dtype, device=es.device)
     N.check(N.lib().gsea_stats_ragged(_vp(es.contiguous()), K, ld, _vp(c), p_fwer, prec, _vp(out), None))
     return out
+
+
+def fdr_lower_bound(es, counts, p_fwer: int, sums, z: float):
+    """(statistics [5K], q lower bounds [K]) of a CUDA ES tensor [K][ld] whose
+    row k holds counts[k] scores; sums [2K]: sum |S| then sum S^2 per set
+    (gsea_fdr_lower_bound)."""
+    torch = _torch()
+    K, ld = es.shape
+    prec = 64 if es.dtype == torch.float64 else 32
+    c = torch.as_tensor(np.ascontiguousarray(counts, np.int64)).to(es.device)
+    sm = torch.as_tensor(np.ascontiguousarray(sums, np.float64)).to(es.device)
+    out = torch.empty(5 * K, dtype=es.dtype, device=es.device)
+    q = torch.empty(K, dtype=torch.float32, device=es.device)
+    N.check(N.lib().gsea_fdr_lower_bound(_vp(es.contiguous()), K, ld, _vp(c), p_fwer, _vp(sm), z, prec, _vp(out),
+                                         _vp(q), None))
+    return out, q

@@ -40,7 +40,8 @@ int ensure_buffers(gsea_plan_s* p) {
     if (!p->counts && (rc = gsea::plan_dev_alloc((void**)&p->counts, sizeof(int64_t) * K, "set counts"))) return rc;
     if (!p->exceed && (rc = gsea::plan_dev_alloc((void**)&p->exceed, sizeof(unsigned long long) * K, "exceedances")))
         return rc;
-    if (!p->sumabs && (rc = gsea::plan_dev_alloc((void**)&p->sumabs, sizeof(double) * K, "score sums"))) return rc;
+    if (!p->sumabs && (rc = gsea::plan_dev_alloc((void**)&p->sumabs, sizeof(double) * 2 * K, "score sums"))) return rc;
+    if (!p->qlow && (rc = gsea::plan_dev_alloc((void**)&p->qlow, sizeof(float) * K, "q bounds"))) return rc;
     if (!p->feat && (rc = gsea::plan_dev_alloc((void**)&p->feat, sizeof(float) * 5 * K, "features"))) return rc;
     if (!p->pred && (rc = gsea::plan_dev_alloc((void**)&p->pred, sizeof(float) * 2 * K, "predictions"))) return rc;
     return GSEA_OK;
@@ -113,6 +114,20 @@ int model_samples_t(gsea_plan_s* p, int queries, int holdout, float* x, float* t
     return GSEA_OK;
 }
 
+}  // namespace
+
+namespace gsea {
+// prior-data conflict check: the observed fraction c / n within z sd of the
+// prior predictive (beta-binomial with mean pm and pm * w + (1 - pm) * w
+// pseudo-counts) keeps the prior for the set
+bool prior_agrees(double pm, double w, double n, double c, double z) {
+    const double sd_pp = std::sqrt(pm * (1.0 - pm) * (w + n) / (n * (w + 1.0)));
+    return std::fabs(c / n - pm) <= z * sd_pp;
+}
+}  // namespace gsea
+
+namespace {
+
 template <class T>
 int execute_adaptive_t(gsea_plan_s* p, gsea_model model, const gsea_adaptive_params& ap, int64_t* counts_out,
                        gsea_adaptive_report* report) {
@@ -126,10 +141,10 @@ int execute_adaptive_t(gsea_plan_s* p, gsea_model model, const gsea_adaptive_par
     gsea::launches_take();
     p->events_used = 0;
     GSEA_CUDA(cudaMemsetAsync(p->exceed, 0, sizeof(unsigned long long) * K, st), "clear exceedances");
-    GSEA_CUDA(cudaMemsetAsync(p->sumabs, 0, sizeof(double) * K, st), "clear sums");
+    GSEA_CUDA(cudaMemsetAsync(p->sumabs, 0, sizeof(double) * 2 * K, st), "clear sums");
     // pilot: every set, permutations [0, P0)
     if ((rc = gsea::plan_run_range(p, st, 0, P0, p->set_order, K))) return rc;
-    GSEA_CUDA(gsea::launch_exceed<T>(es, P, nullptr, K, 0, P0, p->exceed, p->sumabs, st), "exceedance kernel");
+    GSEA_CUDA(gsea::launch_exceed<T>(es, P, K, nullptr, K, 0, P0, p->exceed, p->sumabs, st), "exceedance kernel");
     std::vector<int64_t> counts((size_t)K, P0);
     GSEA_CUDA(cudaMemcpyAsync(p->counts, counts.data(), sizeof(int64_t) * K, cudaMemcpyHostToDevice, st),
               "copy counts");
@@ -193,6 +208,41 @@ int execute_adaptive_t(gsea_plan_s* p, gsea_model model, const gsea_adaptive_par
                                     model_used ? prior.data() : nullptr, stop_p, ap.z, out.data());
     };
     if ((rc = decide(stop))) return rc;
+    // FDR rule: the pilot statistics are current; later rounds recompute them
+    std::vector<float> qlow((size_t)K);
+    int64_t stopped_q = 0;
+    const double q_stop = ap.q_margin * ap.q_call;
+    auto q_rule = [&](std::vector<uint8_t>& st_out, bool fresh_stats) -> int {
+        if (!(ap.q_margin > 0.0)) return GSEA_OK;
+        if (fresh_stats) {
+            GSEA_CUDA(cudaMemcpyAsync(p->counts, counts.data(), sizeof(int64_t) * K, cudaMemcpyHostToDevice, st),
+                      "copy counts");
+            GSEA_CUDA(gsea::launch_stats_ragged<T>(es, K, P, p->counts, P0, static_cast<T*>(p->stats),
+                                                   p->stats_scratch, st),
+                      "round statistics");
+        }
+        GSEA_CUDA(gsea::launch_fdr_bound<T>(K, P0, static_cast<const T*>(p->stats), p->counts, p->sumabs, ap.z,
+                                            p->stats_scratch, p->qlow, st),
+                  "FDR bound kernel");
+        GSEA_CUDA(cudaMemcpyAsync(qlow.data(), p->qlow, sizeof(float) * K, cudaMemcpyDeviceToHost, st), "copy bounds");
+        GSEA_CUDA(cudaStreamSynchronize(st), "stream sync");
+        for (int k = 0; k < K; k++)
+            if (!st_out[k] && counts[k] < P && (double)qlow[k] >= q_stop) {
+                st_out[k] = 1;
+                stopped_q++;
+            }
+        return GSEA_OK;
+    };
+    if ((rc = q_rule(stop, false))) return rc;
+    int64_t prior_sets = 0, prior_agreed = 0;
+    if (model_used) {
+        for (int k = 0; k < K; k++) {
+            if (!(std::isfinite(pm[k]) && std::isfinite(prior[k]) && prior[k] > 0)) continue;
+            prior_sets++;
+            const double v = std::min(std::max((double)pm[k], 1e-6), 1.0 - 1e-6);
+            prior_agreed += gsea::prior_agrees(v, prior[k], (double)P0, (double)exceed[k], ap.z) ? 1 : 0;
+        }
+    }
     int64_t stopped_pilot = 0;
     for (int k = 0; k < K; k++) stopped_pilot += stop[k];
     int64_t cur = P0, rounds = 1;
@@ -208,13 +258,14 @@ int execute_adaptive_t(gsea_plan_s* p, gsea_model model, const gsea_adaptive_par
         GSEA_CUDA(cudaMemcpyAsync(p->active, active.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st),
                   "copy active sets");
         if ((rc = gsea::plan_run_range(p, st, cur, next, p->active, n))) return rc;
-        GSEA_CUDA(gsea::launch_exceed<T>(es, P, p->active, n, cur, next, p->exceed, p->sumabs, st), "exceedances");
+        GSEA_CUDA(gsea::launch_exceed<T>(es, P, K, p->active, n, cur, next, p->exceed, p->sumabs, st), "exceedances");
         GSEA_CUDA(cudaMemcpyAsync(exceed.data(), p->exceed, sizeof(unsigned long long) * K, cudaMemcpyDeviceToHost, st),
                   "copy exceedances");
         GSEA_CUDA(cudaStreamSynchronize(st), "stream sync");
         for (int32_t k : active) counts[k] = next;
         if ((rc = decide(now))) return rc;
         for (int32_t k : active) stop[k] = now[k];
+        if (next < P && (rc = q_rule(stop, true))) return rc;
         cur = next;
         rounds++;
     }
@@ -238,6 +289,9 @@ int execute_adaptive_t(gsea_plan_s* p, gsea_model model, const gsea_adaptive_par
         report->stop_p = stop_p;
         report->model_used = model_used;
         report->model_mean_err = mean_err;
+        report->prior_sets = prior_sets;
+        report->prior_agreed = prior_agreed;
+        report->stopped_q = stopped_q;
     }
     return GSEA_OK;
 }
@@ -256,10 +310,12 @@ void gsea_adaptive_params_init(gsea_adaptive_params* ap) {
     ap->p_floor = 0.01;
     ap->prior_cap = 4.0;
     ap->fallback_tol = 0.25;
+    ap->q_margin = 1.5;
 }
 
 int gsea_adaptive_decide(int64_t num_sets, const int64_t* counts, const int64_t* exceed, const float* p_model,
                          const float* prior, double stop_p, double z, uint8_t* stop) {
+    using gsea::prior_agrees;
     if (num_sets < 0 || (num_sets > 0 && (!counts || !exceed || !stop)))
         return fail(GSEA_ERR_INVALID_ARGUMENT, "invalid arguments");
     for (int64_t k = 0; k < num_sets; k++) {
@@ -271,10 +327,7 @@ int gsea_adaptive_decide(int64_t num_sets, const int64_t* counts, const int64_t*
         double a = 0.5 + c, b = 0.5 + (n - c);
         if (p_model && prior && std::isfinite(p_model[k]) && std::isfinite(prior[k]) && prior[k] > 0) {
             const double pm = std::min(std::max((double)p_model[k], 1e-6), 1.0 - 1e-6), w = prior[k];
-            // prior-data conflict: the observed fraction outside z sd of the
-            // prior predictive (beta-binomial) drops the prior for this set
-            const double sd_pp = std::sqrt(pm * (1.0 - pm) * (w + n) / (n * (w + 1.0)));
-            if (std::fabs(c / n - pm) <= z * sd_pp) {
+            if (prior_agrees(pm, w, n, c, z)) {
                 a += pm * w;
                 b += (1.0 - pm) * w;
             }
@@ -306,7 +359,7 @@ int gsea_plan_execute_adaptive(gsea_plan p, gsea_model model, const gsea_adaptiv
     gsea_adaptive_params_init(&def);
     const gsea_adaptive_params& a = ap ? *ap : def;
     if (a.pilot_perms < 2 || !(a.growth > 1.0) || !(a.z >= 0.0) || !(a.margin > 0.0) || !(a.p_floor >= 0.0) ||
-        !(a.prior_cap >= 0.0) || !(a.q_call > 0.0))
+        !(a.prior_cap >= 0.0) || !(a.q_call > 0.0) || !(a.q_margin >= 0.0))
         return fail(GSEA_ERR_INVALID_ARGUMENT, "invalid adaptive parameters");
     GSEA_CUDA(cudaSetDevice(p->device), "cudaSetDevice");
     return p->cfg.precision == 64 ? execute_adaptive_t<double>(p, model, a, counts, report)
@@ -331,6 +384,37 @@ int gsea_stats_ragged(const void* es, int64_t num_sets, int64_t ld, const int64_
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     cudaFree(scratch);
     GSEA_CUDA(e, "ragged statistics");
+    return GSEA_OK;
+}
+
+int gsea_fdr_lower_bound(const void* es, int64_t num_sets, int64_t ld, const int64_t* counts, int64_t p_fwer,
+                         const double* sums, double z, int precision, void* stats, float* qlow, void* stream) {
+    if (!es || !stats || !counts || !sums || !qlow || num_sets < 1 || num_sets > (int64_t)1 << 30 || ld < 1 ||
+        p_fwer < 1 || p_fwer > ld || !(z >= 0.0) || (precision != 32 && precision != 64))
+        return fail(GSEA_ERR_INVALID_ARGUMENT, "invalid arguments");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int K = (int)num_sets;
+    const size_t bytes = precision == 64 ? gsea::stats_scratch_bytes<double>(K, ld)
+                                         : gsea::stats_scratch_bytes<float>(K, ld);
+    void* scratch = nullptr;
+    GSEA_CUDA(cudaMalloc(&scratch, bytes), "statistics scratch");
+    cudaError_t e;
+    if (precision == 64) {
+        e = gsea::launch_stats_ragged<double>(static_cast<const double*>(es), K, ld, counts, p_fwer,
+                                              static_cast<double*>(stats), scratch, st);
+        if (e == cudaSuccess)
+            e = gsea::launch_fdr_bound<double>(K, p_fwer, static_cast<const double*>(stats), counts, sums, z, scratch,
+                                               qlow, st);
+    } else {
+        e = gsea::launch_stats_ragged<float>(static_cast<const float*>(es), K, ld, counts, p_fwer,
+                                             static_cast<float*>(stats), scratch, st);
+        if (e == cudaSuccess)
+            e = gsea::launch_fdr_bound<float>(K, p_fwer, static_cast<const float*>(stats), counts, sums, z, scratch,
+                                              qlow, st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(scratch);
+    GSEA_CUDA(e, "FDR bound");
     return GSEA_OK;
 }
 

@@ -100,7 +100,7 @@ void free_plan_buffers(gsea_plan_s* p) {
     void* bufs[] = {p->exprs, p->labels, p->set_off, p->set_genes, p->set_order, p->masks, p->fast_ok, p->decay, p->gene_mu,
                     p->gene_t1, p->gene_t2, p->opA1, p->opA2, p->opB, p->dev_error, p->keys,
                     p->ranks, p->sorted, p->order, p->sort_scratch, p->es, p->stats, p->stats_scratch,
-                    p->moments, p->active, p->counts, p->exceed, p->sumabs, p->feat, p->pred};
+                    p->moments, p->active, p->counts, p->exceed, p->sumabs, p->qlow, p->feat, p->pred};
     for (void* b : bufs)
         if (b) cudaFree(b);
     p->exprs = p->labels = nullptr;
@@ -122,6 +122,7 @@ void free_plan_buffers(gsea_plan_s* p) {
     p->counts = nullptr;
     p->exceed = nullptr;
     p->sumabs = nullptr;
+    p->qlow = nullptr;
     p->feat = p->pred = nullptr;
 }
 

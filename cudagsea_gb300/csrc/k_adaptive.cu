@@ -159,10 +159,10 @@ __global__ void model_features_kernel(const T* __restrict__ es, int64_t ld, cons
 }
 
 // warp per listed set: exceed[k] += #{p in [lo, hi): |S_kp| >= |S_k0|},
-// sumabs[k] += sum |S_kp|
+// sumabs[k] += sum |S_kp|, sumabs[K + k] += sum S_kp^2
 template <class T>
 __global__ void exceed_kernel(const T* __restrict__ es, int64_t ld, const int32_t* __restrict__ list, int n_list,
-                              int64_t lo, int64_t hi, unsigned long long* __restrict__ exceed,
+                              int K, int64_t lo, int64_t hi, unsigned long long* __restrict__ exceed,
                               double* __restrict__ sumabs) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= n_list) return;
@@ -170,20 +170,23 @@ __global__ void exceed_kernel(const T* __restrict__ es, int64_t ld, const int32_
     const T* row = es + k * ld;
     const T a0 = fabs(row[0]);
     unsigned long long c = 0;
-    double s = 0.0;
+    double s = 0.0, s2 = 0.0;
     for (int64_t p = lo + lane; p < hi; p += 32) {
         const T a = fabs(row[p]);
         c += a >= a0;
         s += (double)a;
+        s2 += (double)a * (double)a;
     }
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) {
         c += __shfl_xor_sync(kFullMask, c, o);
         s += __shfl_xor_sync(kFullMask, s, o);
+        s2 += __shfl_xor_sync(kFullMask, s2, o);
     }
     if (lane == 0) {
         exceed[k] += c;
         sumabs[k] += s;
+        sumabs[K + k] += s2;
     }
 }
 
@@ -241,16 +244,16 @@ template cudaError_t launch_model_features<double>(const double*, int64_t, const
                                                    const double*, int64_t, float*, cudaStream_t);
 
 template <class T>
-cudaError_t launch_exceed(const T* es, int64_t ld, const int32_t* list, int n_list, int64_t lo, int64_t hi,
+cudaError_t launch_exceed(const T* es, int64_t ld, int K, const int32_t* list, int n_list, int64_t lo, int64_t hi,
                           unsigned long long* exceed, double* sumabs, cudaStream_t st) {
     if (n_list <= 0 || hi <= lo) return cudaSuccess;
-    exceed_kernel<T><<<(n_list + 7) / 8, 256, 0, st>>>(es, ld, list, n_list, lo, hi, exceed, sumabs);
+    exceed_kernel<T><<<(n_list + 7) / 8, 256, 0, st>>>(es, ld, list, n_list, K, lo, hi, exceed, sumabs);
     launches_add(1);
     return cudaGetLastError();
 }
-template cudaError_t launch_exceed<float>(const float*, int64_t, const int32_t*, int, int64_t, int64_t,
+template cudaError_t launch_exceed<float>(const float*, int64_t, int, const int32_t*, int, int64_t, int64_t,
                                           unsigned long long*, double*, cudaStream_t);
-template cudaError_t launch_exceed<double>(const double*, int64_t, const int32_t*, int, int64_t, int64_t,
+template cudaError_t launch_exceed<double>(const double*, int64_t, int, const int32_t*, int, int64_t, int64_t,
                                            unsigned long long*, double*, cudaStream_t);
 
 }  // namespace gsea

@@ -57,9 +57,13 @@ __device__ __forceinline__ void load_params(const __nv_bfloat16* __restrict__ wq
     for (int i = threadIdx.x; i < NPARAM; i += blockDim.x) w[i] = __bfloat162float(wq[i]);
 }
 
+// standardised inputs, clamped to +-kInputClamp training standard deviations
+// (a feature that did not vary in training has scale 0 and drops out)
+constexpr float kInputClamp = 8.f;
 __device__ __forceinline__ void normalise(const float* __restrict__ x, const Norm& nm, float* xin) {
 #pragma unroll
-    for (int d = 0; d < IN; d++) xin[d] = (x[d] - nm.x_mean[d]) * nm.x_scale[d];
+    for (int d = 0; d < IN; d++)
+        xin[d] = fminf(fmaxf((x[d] - nm.x_mean[d]) * nm.x_scale[d], -kInputClamp), kInputClamp);
 }
 
 // forward pass of one sample; h1 kept in registers, h2 handed to `sink(j, h2_j)`
@@ -461,20 +465,25 @@ int gsea_model_train(gsea_model m, const float* x, const float* t, int64_t n, in
     std::vector<float> hx((size_t)n * IN), ht((size_t)n * 2);
     GSEA_CUDA(cudaMemcpy(hx.data(), x, sizeof(float) * hx.size(), cudaMemcpyDeviceToHost), "copy samples");
     GSEA_CUDA(cudaMemcpy(ht.data(), t, sizeof(float) * ht.size(), cudaMemcpyDeviceToHost), "copy targets");
+    // two passes (mean, then squared deviations): a feature that is constant
+    // over the samples -- a property of the calibration data set, e.g. the
+    // metric's moments -- gets an exact zero spread and scale 0, so the
+    // network ignores it instead of amplifying rounding noise
     for (int d = 0; d <= IN; d++) {
-        double s = 0, s2 = 0;
-        for (int64_t i = 0; i < n; i++) {
-            const double v = d < IN ? hx[(size_t)i * IN + d] : ht[(size_t)i * 2 + 1];
-            s += v;
-            s2 += v * v;
-        }
-        const double mean = s / n, var = std::max(s2 / n - mean * mean, 0.0), sd = std::sqrt(var);
+        auto val = [&](int64_t i) { return d < IN ? (double)hx[(size_t)i * IN + d] : (double)ht[(size_t)i * 2 + 1]; };
+        double s = 0;
+        for (int64_t i = 0; i < n; i++) s += val(i);
+        const double mean = s / n;
+        double ss = 0;
+        for (int64_t i = 0; i < n; i++) ss += (val(i) - mean) * (val(i) - mean);
+        const double sd = std::sqrt(ss / n);
+        const bool varies = sd > 1e-5 * std::max(1.0, std::fabs(mean));
         if (d < IN) {
             m->norms[d] = (float)mean;
-            m->norms[IN + d] = sd > 1e-6 ? (float)(1.0 / sd) : 1.f;
+            m->norms[IN + d] = varies ? (float)(1.0 / sd) : 0.f;
         } else {
             m->norms[2 * IN] = (float)mean;
-            m->norms[2 * IN + 1] = sd > 1e-6 ? (float)sd : 1.f;
+            m->norms[2 * IN + 1] = varies ? (float)sd : 1.f;
         }
     }
     m->norms[2 * IN + 4] = 0.f;

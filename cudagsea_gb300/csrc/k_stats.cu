@@ -431,7 +431,109 @@ __global__ void stats_fdr_final_kernel(int K, const unsigned long long* __restri
     out[4 * K + k] = q;
 }
 
+// the statistics scratch of K sets with FWER over p_fwer columns
+template <class T>
+struct RaggedLayout {
+    using U = typename RadixKey<T>::U;
+    T* fac;
+    U* mx;
+    U* mn;
+    unsigned long long* cnt_obs;
+    unsigned long long* lcount;
+    T* sorted_pos;
+    T* sorted_neg;
+    double* hpos;
+    double* hneg;
+    unsigned long long* totals;
+    unsigned* partial;
+    RaggedLayout(void* scratch, int K, int64_t p_fwer) {
+        unsigned char* s = static_cast<unsigned char*>(scratch);
+        auto align16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
+        fac = reinterpret_cast<T*>(s);
+        mx = reinterpret_cast<U*>(fac + K);
+        mn = mx + p_fwer;
+        size_t off = align16(sizeof(T) * ((size_t)K + 2 * (size_t)p_fwer));
+        cnt_obs = reinterpret_cast<unsigned long long*>(s + off);
+        lcount = cnt_obs + K;
+        off = align16(off + sizeof(unsigned long long) * 2 * (size_t)K);
+        sorted_pos = reinterpret_cast<T*>(s + off);
+        sorted_neg = sorted_pos + K;
+        off = align16(off + sizeof(T) * 2 * (size_t)K);
+        hpos = reinterpret_cast<double*>(s + off);
+        hneg = hpos + (K + 2);
+        totals = reinterpret_cast<unsigned long long*>(hneg + (K + 2));
+        partial = reinterpret_cast<unsigned*>(s + align16(off + sizeof(double) * (2 * ((size_t)K + 2) + 8)));
+    }
+};
+
+// Lower bound of every set's FDR q after the statistics (adaptive stopping):
+// the set's |NES| may lie anywhere in [|NES|, key], key = |NES| (1 + z cv /
+// sqrt(n)) -- z standard errors of its normalising mean, cv the coefficient
+// of variation of its n scores |S| (sums[k] = sum |S|, sums[K + k] = sum
+// S^2).  q(x) = (null weight >= x / null weight of the side) / (#observed >=
+// x / m) is not monotone in x, so the bound takes the least numerator and
+// the largest denominator over the interval: with i_up observed keys below
+// key, at least S[i_up + 1] null weight lies at or above key (the nulls at or
+// above the next observed key); with i_lo observed keys below |NES|, at most
+// m - i_lo observed keys lie at or above |NES|:
+//   q >= (S[i_up + 1] / null weight of the side) / (max(m - i_lo, 1) / m).
+// NaN or zero NES: 0 (no bound).
+template <class T>
+__global__ void stats_fdr_bound_kernel(int K, const T* __restrict__ stats, const int64_t* __restrict__ counts,
+                                       const double* __restrict__ sums, double z, const T* __restrict__ sorted_pos,
+                                       const T* __restrict__ sorted_neg, const double* __restrict__ spos,
+                                       const double* __restrict__ sneg, const unsigned long long* __restrict__ totals,
+                                       float* __restrict__ qlow) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= K) return;
+    const double s = (double)stats[K + k];
+    float out = 0.f;
+    const double n = (double)counts[k];
+    if (s == s && s != 0.0 && n > 0) {
+        const bool up = s > 0.0;
+        const double m = sums[k] / n;
+        const double var = fmax(sums[K + k] / n - m * m, 0.0);
+        const double cv = m > 0.0 ? sqrt(var) / m : INFINITY;
+        const double key = fabs(s) * (1.0 + z * cv / sqrt(n));
+        const unsigned mcount = (unsigned)(up ? totals[2] : totals[3]);
+        if (key < INFINITY && mcount > 0) {
+            const T* keys = up ? sorted_pos : sorted_neg;
+            auto below = [&](double x) {  // #{keys < x}
+                unsigned lo = 0, hi = mcount;
+                while (lo < hi) {
+                    const unsigned mid = (lo + hi) >> 1;
+                    if ((double)keys[mid] < x) lo = mid + 1; else hi = mid;
+                }
+                return lo;
+            };
+            const unsigned i_up = below(key), i_lo = below(fabs(s));
+            const double c_null = i_up + 1 <= mcount ? (up ? spos : sneg)[i_up + 1] : 0.0;
+            const double wtot = reinterpret_cast<const double*>(totals + 4)[up ? 0 : 1];
+            const double fn = wtot > 0.0 ? c_null / wtot : 0.0;
+            const double obs = (double)(mcount - i_lo > 0 ? mcount - i_lo : 1u);
+            const double r = fn / (obs / (double)mcount);
+            out = (float)(r < 1.0 ? r : 1.0);
+        }
+    }
+    qlow[k] = out;
+}
+
 }  // namespace
+
+template <class T>
+cudaError_t launch_fdr_bound(int K, int64_t p_fwer, const T* stats, const int64_t* counts, const double* sums,
+                             double z, const void* scratch, float* qlow, cudaStream_t st) {
+    if (K <= 0) return cudaSuccess;
+    const RaggedLayout<T> L(const_cast<void*>(scratch), K, p_fwer);
+    stats_fdr_bound_kernel<T><<<(K + 255) / 256, 256, 0, st>>>(K, stats, counts, sums, z, L.sorted_pos, L.sorted_neg,
+                                                               L.hpos, L.hneg, L.totals, qlow);
+    launches_add(1);
+    return cudaGetLastError();
+}
+template cudaError_t launch_fdr_bound<float>(int, int64_t, const float*, const int64_t*, const double*, double,
+                                             const void*, float*, cudaStream_t);
+template cudaError_t launch_fdr_bound<double>(int, int64_t, const double*, const int64_t*, const double*, double,
+                                              const void*, float*, cudaStream_t);
 
 template <class T>
 size_t stats_scratch_bytes(int K, int64_t P) {
@@ -448,24 +550,19 @@ template <class T>
 cudaError_t launch_stats_ragged(const T* es, int K, int64_t ld, const int64_t* counts, int64_t p_fwer, T* stats,
                                 void* scratch, cudaStream_t st) {
     if (K <= 0 || ld <= 0 || p_fwer <= 0 || p_fwer > ld) return K <= 0 ? cudaSuccess : cudaErrorInvalidValue;
-    unsigned char* s = static_cast<unsigned char*>(scratch);
-    auto align16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
-    size_t off = 0;
     using U = typename RadixKey<T>::U;
-    T* fac = reinterpret_cast<T*>(s + off);
-    U* mx = reinterpret_cast<U*>(fac + K);
-    U* mn = mx + p_fwer;
-    off = align16(sizeof(T) * ((size_t)K + 2 * (size_t)p_fwer));
-    unsigned long long* cnt_obs = reinterpret_cast<unsigned long long*>(s + off);
-    unsigned long long* lcount = cnt_obs + K;
-    off = align16(off + sizeof(unsigned long long) * 2 * (size_t)K);
-    T* sorted_pos = reinterpret_cast<T*>(s + off);
-    T* sorted_neg = sorted_pos + K;
-    off = align16(off + sizeof(T) * 2 * (size_t)K);
-    double* hpos = reinterpret_cast<double*>(s + off);
-    double* hneg = hpos + (K + 2);
-    unsigned long long* totals = reinterpret_cast<unsigned long long*>(hneg + (K + 2));
-    unsigned* partial = reinterpret_cast<unsigned*>(s + align16(off + sizeof(double) * (2 * ((size_t)K + 2) + 8)));
+    const RaggedLayout<T> L(scratch, K, p_fwer);
+    T* fac = L.fac;
+    U* mx = L.mx;
+    U* mn = L.mn;
+    unsigned long long* cnt_obs = L.cnt_obs;
+    unsigned long long* lcount = L.lcount;
+    T* sorted_pos = L.sorted_pos;
+    T* sorted_neg = L.sorted_neg;
+    double* hpos = L.hpos;
+    double* hneg = L.hneg;
+    unsigned long long* totals = L.totals;
+    unsigned* partial = L.partial;
     cudaError_t e = cudaMemsetAsync(hpos, 0, sizeof(double) * (2 * ((size_t)K + 2) + 8), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(mx, 0x00, sizeof(U) * (size_t)p_fwer, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(mn, 0xff, sizeof(U) * (size_t)p_fwer, st);

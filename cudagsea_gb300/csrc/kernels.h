@@ -137,9 +137,15 @@ cudaError_t launch_model_samples(const T* es, int64_t ld, int64_t P, const int64
 template <class T>
 cudaError_t launch_model_features(const T* es, int64_t ld, const int64_t* off, int K, const double* mom,
                                   const double* sumabs, int64_t n, float* x, cudaStream_t st);
+// sumabs: [2K], sum of |S| then sum of S^2 per set
 template <class T>
-cudaError_t launch_exceed(const T* es, int64_t ld, const int32_t* list, int n_list, int64_t lo, int64_t hi,
+cudaError_t launch_exceed(const T* es, int64_t ld, int K, const int32_t* list, int n_list, int64_t lo, int64_t hi,
                           unsigned long long* exceed, double* sumabs, cudaStream_t st);
+// after launch_stats_ragged with the same (K, p_fwer, scratch): a lower bound
+// of every set's FDR q with its NES pushed z standard errors outward
+template <class T>
+cudaError_t launch_fdr_bound(int K, int64_t p_fwer, const T* stats, const int64_t* counts, const double* sums,
+                             double z, const void* scratch, float* qlow, cudaStream_t st);
 
 // number of kernel launches issued by the launchers above since the last reset
 int64_t launches_take();

@@ -86,7 +86,8 @@ struct gsea_plan_s {
     int32_t* active = nullptr;         // [K] set list of the current adaptive round
     int64_t* counts = nullptr;         // [K] scores held per set (ragged statistics)
     unsigned long long* exceed = nullptr;  // [K] #{|S| >= |ES|} per set
-    double* sumabs = nullptr;          // [K] sum of |S| per set
+    double* sumabs = nullptr;          // [2K] sum of |S| per set, then sum of S^2 per set
+    float* qlow = nullptr;             // [K] lower bound of each set's FDR q (adaptive stopping)
     float* feat = nullptr;             // [K][5] model features
     float* pred = nullptr;             // [K][2] model predictions
     // stage timing (gsea_plan_set_profiling): events recorded at every stage

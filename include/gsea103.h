@@ -327,7 +327,9 @@ int gsea_batch_info(gsea_batch b, int64_t* graph_nodes, int64_t* es_classes, int
 #define GSEA_MODEL_OUTPUTS 2
 /* parameter vector: W1[64][5] b1[64] W2[64][64] b2[64] W3[2][64] b3[2] */
 #define GSEA_MODEL_PARAMS 4674
-/* normaliser vector: x_mean[5] x_scale[5] (x_n = (x - mean) * scale),
+/* normaliser vector: x_mean[5] x_scale[5] (x_n = (x - mean) * scale,
+ * clamped to [-8, 8]; training sets scale 0 for a feature that is constant
+ * over its samples),
  * y_mean y_std (log null mean = z1 * y_std + y_mean), sigma_tail (sd of the
  * logit error of the tail on held-out sets), sigma_mean (sd of the log error
  * of the null mean), trained (0/1) */
@@ -379,6 +381,8 @@ typedef struct gsea_adaptive_params {
     double p_floor;      /* lower bound of stop_p (0.01) */
     double prior_cap;    /* prior pseudo-permutations <= prior_cap * pilot_perms (4) */
     double fallback_tol; /* model dropped if its median |log m~ - log m^| on the pilot exceeds (0.25) */
+    double q_margin;     /* also stop a set once a lower bound of its FDR q (NES pushed z standard
+                            errors outward) is >= q_margin * q_call; 0 turns this rule off (1.5) */
 } gsea_adaptive_params;
 void gsea_adaptive_params_init(gsea_adaptive_params* ap);
 typedef struct gsea_adaptive_report {
@@ -389,6 +393,9 @@ typedef struct gsea_adaptive_report {
     double stop_p;           /* p threshold of the stopping rule */
     int32_t model_used;      /* 1 if the model's prior was applied */
     double model_mean_err;   /* median |log m~ - log m^| on the pilot */
+    int64_t prior_sets;      /* sets with a finite model prior (model_used) */
+    int64_t prior_agreed;    /* of those, sets whose pilot agreed with the prior (kept at the pilot decision) */
+    int64_t stopped_q;       /* sets stopped by the FDR bound (q_margin), any round */
 } gsea_adaptive_report;
 /* Adaptive permutation test on the plan's inputs, num_perms permutations at
  * most per set: a pilot of pilot_perms permutations for every set, then
@@ -413,6 +420,14 @@ int gsea_adaptive_decide(int64_t num_sets, const int64_t* counts, const int64_t*
  * first p_fwer columns.  Allocates its scratch; synchronous.               */
 int gsea_stats_ragged(const void* es, int64_t num_sets, int64_t ld, const int64_t* counts, int64_t p_fwer,
                       int precision, void* stats, void* stream);
+/* The adaptive test's FDR stopping bound on its own: the ragged statistics
+ * (as gsea_stats_ragged, into stats) and, per set, a lower bound of its FDR
+ * q with |NES| pushed z standard errors outward (qlow, device float [K]).
+ * sums: device double [2K], sum |S| then sum S^2 over each set's counts[k]
+ * scores.  With z = 0 and untied NES the bound is the FDR q itself.
+ * Allocates its scratch; synchronous.                                      */
+int gsea_fdr_lower_bound(const void* es, int64_t num_sets, int64_t ld, const int64_t* counts, int64_t p_fwer,
+                         const double* sums, double z, int precision, void* stats, float* qlow, void* stream);
 
 /* ---- Broad files (replace read_gct / read_cls / read_gmt,
  *      src/include/read_data_files.cuh:46-321, and the loader proxies

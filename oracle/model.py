@@ -37,9 +37,12 @@ def unpack(p):
             p[OFF_W3:OFF_B3].reshape(OUT, H), p[OFF_B3:NPARAM])
 
 
+INPUT_CLAMP = 8.0  # standardised inputs are clamped to +-8 (k_model.cu kInputClamp)
+
+
 def normalise(x, norms):
     n = np.asarray(norms, np.float64)
-    return (np.asarray(x, np.float64) - n[:IN]) * n[IN:2 * IN]
+    return np.clip((np.asarray(x, np.float64) - n[:IN]) * n[IN:2 * IN], -INPUT_CLAMP, INPUT_CLAMP)
 
 
 def forward(p, norms, x):
@@ -189,3 +192,52 @@ def stats_ragged(es, counts, p_fwer, dtype=np.float32):
             fo = np.count_nonzero(oneg <= s) / oneg.size
         out[4, k] = T(min(fn / fo, 1.0))
     return out.ravel()
+
+
+def fdr_bound(es, counts, p_fwer, sums, z, dtype=np.float32):
+    """Lower bound of every set's FDR q over |NES| in [|NES|, key], key =
+    |NES| (1 + z cv / sqrt(n)) (k_stats.cu stats_fdr_bound_kernel), cv from
+    sums (sum |S| then sum S^2 per set): the null weight at or above the
+    observed key next above key (i_up keys below key) over the side's null
+    weight, divided by max(m - i_lo, 1) / m (i_lo keys below |NES|), capped at
+    1.  NaN or zero NES: 0.  Returns (statistics, bounds float32)."""
+    T = dtype
+    es = np.asarray(es, T)
+    K, ld = es.shape
+    counts = np.asarray(counts, np.int64)
+    sums = np.asarray(sums, np.float64)
+    st = stats_ragged(es, counts, p_fwer, dtype).reshape(5, K)
+    fac = np.zeros(K, T)
+    for k in range(K):
+        n = counts[k]
+        fac[k] = T(n) / np.cumsum(np.abs(es[k, :n]), dtype=T)[-1]
+    vals, wts = [], []
+    for k in range(K):
+        n = counts[k]
+        if n >= 2:
+            vals.append((es[k, 1:n] * fac[k]).astype(np.float64))
+            wts.append(np.full(n - 1, (ld - 1) / (n - 1)))
+    v = np.concatenate(vals) if vals else np.zeros(0)
+    w = np.concatenate(wts) if wts else np.zeros(0)
+    obs = st[1].astype(np.float64)
+    sides = {True: (np.sort(obs[obs >= 0]), v >= 0, v), False: (np.sort(-obs[obs <= 0]), v <= 0, -v)}
+    q = np.zeros(K, np.float32)
+    for k in range(K):
+        s, n = obs[k], float(counts[k])
+        if not (s == s) or s == 0.0 or n <= 0:
+            continue
+        m = sums[k] / n
+        var = max(sums[K + k] / n - m * m, 0.0)
+        cv = np.sqrt(var) / m if m > 0 else np.inf
+        key = abs(s) * (1.0 + z * cv / np.sqrt(n))
+        keys, on_side, nv = sides[s > 0]
+        mc = keys.size
+        if not np.isfinite(key) or mc == 0:
+            continue
+        i_up = int(np.count_nonzero(keys < key))
+        i_lo = int(np.count_nonzero(keys < abs(s)))
+        c_null = w[on_side & (nv >= keys[i_up])].sum() if i_up < mc else 0.0
+        wtot = w[on_side].sum()
+        fn = c_null / wtot if wtot > 0 else 0.0
+        q[k] = np.float32(min(fn / (max(mc - i_lo, 1) / mc), 1.0))
+    return st.ravel(), q

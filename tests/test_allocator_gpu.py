@@ -248,3 +248,44 @@ def test_adaptive_single_set_and_invalid_parameters(gpu):
     with pytest.raises(N.GseaError):
         allocator.execute_adaptive(plan, None, growth=1.0)
     plan.close()
+
+
+def test_fdr_bound_matches_oracle(gpu):
+    """gsea_fdr_lower_bound against the numpy restatement: ragged counts,
+    z = 0 (the FDR q itself) and z = 3."""
+    import torch
+    rs = np.random.RandomState(3)
+    K, ld = 40, 300
+    es = rs.normal(0, 0.3, (K, ld)).astype(np.float32)
+    es[:, 0] += rs.normal(0, 0.6, K).astype(np.float32)
+    counts = rs.randint(50, ld + 1, K).astype(np.int64)
+    counts[0] = ld
+    a = np.abs(es.astype(np.float64))
+    sums = np.concatenate([[a[k, :counts[k]].sum() for k in range(K)],
+                           [(a[k, :counts[k]] ** 2).sum() for k in range(K)]])
+    p_fwer = int(counts.min())
+    for z in (0.0, 3.0):
+        st, q = allocator.fdr_lower_bound(torch.as_tensor(es).cuda(), counts, p_fwer, sums, z)
+        st_o, q_o = M.fdr_bound(es, counts, p_fwer, sums, z)
+        np.testing.assert_allclose(q.cpu().numpy(), q_o, rtol=1e-5, atol=1e-7)
+        if z == 0.0:
+            np.testing.assert_allclose(q.cpu().numpy(), st.cpu().numpy().reshape(5, -1)[4], rtol=1e-6)
+
+
+def test_fdr_rule_saves_scores_with_the_full_tests_calls(gpu):
+    """Stopping sets whose FDR q is clearly above the call level: the full
+    test's calls, fewer scores than the p rule alone."""
+    d = case(seed=77)
+    plan_f, es_f, st_f = full_run(d)
+    plan_f.close()
+    scores, reports = {}, {}
+    for qm in (0.0, 1.5):
+        plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, P_MAX, "twopass_signal2noise")
+        plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+        res = allocator.execute_adaptive(plan, None, pilot_perms=250, q_margin=qm)
+        scores[qm] = check_against_full(d, res, es_f, st_f, plan)
+        reports[qm] = res.report
+        plan.close()
+    assert reports[0.0]["stopped_q"] == 0
+    assert reports[1.5]["stopped_q"] > 0
+    assert scores[1.5] < scores[0.0], scores

@@ -169,5 +169,7 @@ def test_new_entry_points_check_arguments_without_a_gpu():
     ap = N.AdaptiveParams()
     L.gsea_adaptive_params_init(ctypes.byref(ap))
     assert ap.pilot_perms == 1000 and ap.growth == 2.0 and ap.z == 3.0 and ap.q_call == 0.25
+    assert ap.q_margin == 1.5
+    assert L.gsea_fdr_lower_bound(None, 1, 1, None, 1, None, 0.0, 32, None, None, None) == 1
     assert L.gsea_plan_execute_adaptive(None, None, ctypes.byref(ap), None, None) == 1
     assert L.gsea_model_train(None, None, None, 0, 1, 1, ctypes.c_float(1e-3), None) == 1

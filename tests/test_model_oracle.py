@@ -93,3 +93,42 @@ def test_ragged_oracle_reduces_to_dense_statistics(double):
     st = st.reshape(5, -1)
     assert np.array_equal(r[:4].view(np.uint64 if double else np.uint32), st[:4].view(np.uint64 if double else np.uint32))
     np.testing.assert_allclose(r[4], st[4], rtol=1e-6 if not double else 1e-12)
+
+
+def _ragged_case(seed=3, K=40, ld=300):
+    rs = np.random.RandomState(seed)
+    es = rs.normal(0, 0.3, (K, ld)).astype(np.float32)
+    es[:, 0] += rs.normal(0, 0.6, K).astype(np.float32)
+    counts = rs.randint(50, ld + 1, K).astype(np.int64)
+    counts[0] = ld
+    a = np.abs(es.astype(np.float64))
+    sums = np.concatenate([[a[k, :counts[k]].sum() for k in range(K)],
+                           [(a[k, :counts[k]] ** 2).sum() for k in range(K)]])
+    return es, counts, sums
+
+
+def test_fdr_bound_oracle_is_q_at_z0_and_below_q_otherwise():
+    """The adaptive test's FDR stopping bound: at z = 0 it is the set's own
+    FDR q (no ties here); a wider interval only lowers it, and it never
+    exceeds q at any |NES| inside the interval (checked at the observed keys
+    the interval covers)."""
+    es, counts, sums = _ragged_case()
+    p_fwer = int(counts.min())
+    st, q0 = M.fdr_bound(es, counts, p_fwer, sums, 0.0)
+    q = st.reshape(5, -1)[4]
+    np.testing.assert_allclose(q0, q, rtol=1e-6)
+    _, q1 = M.fdr_bound(es, counts, p_fwer, sums, 1.0)
+    _, q3 = M.fdr_bound(es, counts, p_fwer, sums, 3.0)
+    assert np.all(q1 <= q0) and np.all(q3 <= q1)
+    assert np.any(q3 < q0)
+    # q(x) at every observed key x inside [|NES_k|, key_k] is >= the bound
+    K = es.shape[0]
+    nes = st.reshape(5, -1)[1].astype(np.float64)
+    for k in range(K):
+        n = counts[k]
+        m = sums[k] / n
+        cv = np.sqrt(max(sums[K + k] / n - m * m, 0.0)) / m
+        key = abs(nes[k]) * (1 + 3.0 * cv / np.sqrt(n))
+        same = [j for j in range(K) if np.sign(nes[j]) == np.sign(nes[k]) and abs(nes[k]) <= abs(nes[j]) <= key]
+        for j in same:
+            assert q3[k] <= q[j] + 1e-6, (k, j, q3[k], q[j])
