@@ -19,7 +19,11 @@ statistics) over the whole workload.
                  gsea_plan_run_host copies the inputs in, runs the pipeline
                  and copies ES + statistics out, every step.
 * roofline       the dominant stage's algorithmic bytes per launch / its
-                 average device time, against MEASURED_PEAKS.json.
+                 average device time, against MEASURED_PEAKS.json; `limiter`
+                 adds the kernel's issue-slot utilisation from its ncu summary
+                 under profiles/ (the stage is instruction bound: its data
+                 stay in shared memory, so the HBM fraction is small by
+                 construction).
 * forms.adaptive / forms.learned
                  the adaptive permutation test (tensor-core form) without
                  and with the learned prior: wall time of the whole adaptive
@@ -154,6 +158,29 @@ def peaks():
         return float(p["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+STAGE_PROFILES = {"es": "es_kernel_full_20000x200_K1000_152perms.md",
+                  "sort": "sort_regs_kernel_full_20000x200_152perms.md",
+                  "metric": "class_stats_kernel_full_20000x200_152perms.md"}
+
+
+def issue_limiter(stage):
+    """Issue-slot utilisation of the stage's kernel from its committed ncu
+    summary (the `issue active %` row), or None."""
+    name = STAGE_PROFILES.get(stage)
+    if not name:
+        return None
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        for line in open(path):
+            cells = [c.strip() for c in line.strip().strip("|").split("|")]
+            if len(cells) == 2 and cells[0] == "issue active %":
+                return {"kind": "instruction issue", "issue_active": float(cells[1]) / 100.0,
+                        "source": "profiles/" + name}
+    except Exception:
+        return None
+    return None
 
 
 def traffic_record():
@@ -570,6 +597,9 @@ def run_ours(args):
     roof = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": tr, "peak_source": peak_kind,
             "algorithmic_bytes": sb[dominant], "avg_ms": stage_avg[dominant]}
+    lim = issue_limiter(dominant)
+    if lim is not None:
+        roof["limiter"] = lim
 
     out = None
     if rank == 0:
