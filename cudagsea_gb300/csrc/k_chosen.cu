@@ -54,7 +54,11 @@ constexpr int BN = 256;          // permutations per CTA (the default tile; 128 
 constexpr int BK = 64;           // K elements per chunk
 constexpr int A_CHUNK = BM * BK * 2;   // 16 KB
 constexpr int B_CHUNK = BN * BK * 2;   // 32 KB (a 128-permutation tile uses half)
-constexpr int STAGES = 3;
+// pipeline stages: 3 for the 256-permutation tile (192 KB, one CTA per SM);
+// 2 for the 128-permutation tile (96 KB and 256 TMEM columns: two CTAs per
+// SM, so one CTA's epilogue runs beside the other's loads and MMAs)
+template <int TN>
+constexpr int stages() { return TN == 128 ? 2 : 3; }
 template <int TN>
 constexpr int stage_bytes() { return 2 * A_CHUNK + TN * BK * 2; }
 constexpr int THREADS = 256;     // 8 warps: two per TMEM lane quarter in the epilogue
@@ -181,12 +185,13 @@ __device__ __forceinline__ float variance(float ms, float m) {
 }
 
 template <int COMB, bool FP64SUB, int TN>
-__global__ void __launch_bounds__(THREADS, 1)
+__global__ void __launch_bounds__(THREADS, TN == 128 ? 2 : 1)
 class_stats_kernel(const unsigned char* __restrict__ A1, const unsigned char* __restrict__ A2,
                    const unsigned char* __restrict__ B, int chunks, int G, int num_perms,
                    const float* __restrict__ gene_mu, const double* __restrict__ gene_t1,
                    const double* __restrict__ gene_t2, float nA, float nB, float* __restrict__ keys,
                    int* __restrict__ error_flag) {
+    constexpr int STAGES = stages<TN>();
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ __align__(8) uint64_t bar_full[STAGES];
     __shared__ __align__(8) uint64_t bar_done[STAGES];
@@ -490,7 +495,7 @@ cudaError_t launch_chosen_tn(int comb, bool fp64_variance, const uint32_t* masks
     if (e != cudaSuccess) return e;
     label_operand_kernel<TN><<<dim3((num_perms + 127) / 128, S), 128, 0, st>>>(masks, words, S, num_perms, chunks, Bm);
     const dim3 grid((G + BM - 1) / BM, (num_perms + TN - 1) / TN);
-    const size_t smem = (size_t)STAGES * stage_bytes<TN>();
+    const size_t smem = (size_t)stages<TN>() * stage_bytes<TN>();
 #define GSEA_CHOSEN(C)                                                                                        \
     {                                                                                                         \
         auto kern = fp64_variance ? class_stats_kernel<C, true, TN> : class_stats_kernel<C, false, TN>;      \
