@@ -523,10 +523,11 @@ cudaError_t launch_chosen_metric(int metric, bool fp64_variance, const uint32_t*
                                  unsigned char* Bm, float* keys, int* error_flag, cudaStream_t st, int tile_n) {
     const int comb = metric == 0 || metric == 3 ? 0 : metric == 1 || metric == 4 ? 1 : metric == 2 || metric == 5 ? 2
                    : (metric == 6 || metric == 8 || metric == 10 || metric == 12) ? 3 : 4;
-    if (tile_n == 128)
+    // default (0): the 128-permutation tile, two CTAs per SM
+    if (tile_n == 0 || tile_n == 128)
         return launch_chosen_tn<128>(comb, fp64_variance, masks, words, G, S, num_perms, nA, nB, mu, t1, t2, A1, A2,
                                      Bm, keys, error_flag, st);
-    if (tile_n != 0 && tile_n != 256) return cudaErrorInvalidValue;
+    if (tile_n != 256) return cudaErrorInvalidValue;
     return launch_chosen_tn<256>(comb, fp64_variance, masks, words, G, S, num_perms, nA, nB, mu, t1, t2, A1, A2, Bm,
                                  keys, error_flag, st);
 }
