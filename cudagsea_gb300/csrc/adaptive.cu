@@ -82,6 +82,7 @@ int model_samples_t(gsea_plan_s* p, int queries, int holdout, float* x, float* t
     cudaStream_t st = p->stream;
     int rc = ensure_buffers(p);
     if (rc || (rc = compute_moments<T>(p, st))) return rc;
+    p->moments_ready = true;
     GSEA_CUDA(gsea::launch_set_means<T>(static_cast<const T*>(p->es), P, P, K, p->sumabs, st), "set means");
     std::vector<double> means((size_t)K);
     GSEA_CUDA(cudaMemcpyAsync(means.data(), p->sumabs, sizeof(double) * K, cudaMemcpyDeviceToHost, st), "copy means");
@@ -150,6 +151,18 @@ int execute_adaptive_t(gsea_plan_s* p, gsea_model model, const gsea_adaptive_par
               "copy counts");
     GSEA_CUDA(gsea::launch_stats_ragged<T>(es, K, P, p->counts, P0, static_cast<T*>(p->stats), p->stats_scratch, st),
               "pilot statistics");
+    // FDR rule: lower bounds of the sets' q from the statistics just computed
+    // (launched before the host synchronises, copied back with the rest)
+    const bool q_on = ap.q_margin > 0.0;
+    std::vector<float> qlow((size_t)K);
+    auto launch_bound = [&]() -> int {
+        GSEA_CUDA(gsea::launch_fdr_bound<T>(K, P0, static_cast<const T*>(p->stats), p->counts, p->sumabs, ap.z,
+                                            p->stats_scratch, p->qlow, st),
+                  "FDR bound kernel");
+        GSEA_CUDA(cudaMemcpyAsync(qlow.data(), p->qlow, sizeof(float) * K, cudaMemcpyDeviceToHost, st), "copy bounds");
+        return GSEA_OK;
+    };
+    if (q_on && P0 < P && (rc = launch_bound())) return rc;
     std::vector<T> stats((size_t)5 * K);
     std::vector<unsigned long long> exceed((size_t)K);
     std::vector<double> sumabs((size_t)K);
@@ -172,7 +185,10 @@ int execute_adaptive_t(gsea_plan_s* p, gsea_model model, const gsea_adaptive_par
         float norms[GSEA_MODEL_NORMS];
         if ((rc = gsea_model_get(model, nullptr, norms))) return rc;
         if (norms[14] != 0.f) {
-            if ((rc = compute_moments<T>(p, st))) return rc;
+            if (!p->moments_ready) {  // a property of the inputs: computed once per upload
+                if ((rc = compute_moments<T>(p, st))) return rc;
+                p->moments_ready = true;
+            }
             GSEA_CUDA(gsea::launch_model_features<T>(es, P, p->set_off, K, p->moments, p->sumabs, P0, p->feat, st),
                       "features");
             if ((rc = gsea_model_predict(model, p->feat, K, p->pred, st))) return rc;
@@ -208,32 +224,16 @@ int execute_adaptive_t(gsea_plan_s* p, gsea_model model, const gsea_adaptive_par
                                     model_used ? prior.data() : nullptr, stop_p, ap.z, out.data());
     };
     if ((rc = decide(stop))) return rc;
-    // FDR rule: the pilot statistics are current; later rounds recompute them
-    std::vector<float> qlow((size_t)K);
     int64_t stopped_q = 0;
     const double q_stop = ap.q_margin * ap.q_call;
-    auto q_rule = [&](std::vector<uint8_t>& st_out, bool fresh_stats) -> int {
-        if (!(ap.q_margin > 0.0)) return GSEA_OK;
-        if (fresh_stats) {
-            GSEA_CUDA(cudaMemcpyAsync(p->counts, counts.data(), sizeof(int64_t) * K, cudaMemcpyHostToDevice, st),
-                      "copy counts");
-            GSEA_CUDA(gsea::launch_stats_ragged<T>(es, K, P, p->counts, P0, static_cast<T*>(p->stats),
-                                                   p->stats_scratch, st),
-                      "round statistics");
-        }
-        GSEA_CUDA(gsea::launch_fdr_bound<T>(K, P0, static_cast<const T*>(p->stats), p->counts, p->sumabs, ap.z,
-                                            p->stats_scratch, p->qlow, st),
-                  "FDR bound kernel");
-        GSEA_CUDA(cudaMemcpyAsync(qlow.data(), p->qlow, sizeof(float) * K, cudaMemcpyDeviceToHost, st), "copy bounds");
-        GSEA_CUDA(cudaStreamSynchronize(st), "stream sync");
+    auto apply_bound = [&](std::vector<uint8_t>& st_out) {  // after the synchronisation that brought qlow
         for (int k = 0; k < K; k++)
             if (!st_out[k] && counts[k] < P && (double)qlow[k] >= q_stop) {
                 st_out[k] = 1;
                 stopped_q++;
             }
-        return GSEA_OK;
     };
-    if ((rc = q_rule(stop, false))) return rc;
+    if (q_on && P0 < P) apply_bound(stop);
     int64_t prior_sets = 0, prior_agreed = 0;
     if (model_used) {
         for (int k = 0; k < K; k++) {
@@ -259,13 +259,22 @@ int execute_adaptive_t(gsea_plan_s* p, gsea_model model, const gsea_adaptive_par
                   "copy active sets");
         if ((rc = gsea::plan_run_range(p, st, cur, next, p->active, n))) return rc;
         GSEA_CUDA(gsea::launch_exceed<T>(es, P, K, p->active, n, cur, next, p->exceed, p->sumabs, st), "exceedances");
+        for (int32_t k : active) counts[k] = next;
+        const bool bound_now = q_on && next < P;
+        if (bound_now) {  // statistics at the new counts, then the bounds: one synchronisation per round
+            GSEA_CUDA(cudaMemcpyAsync(p->counts, counts.data(), sizeof(int64_t) * K, cudaMemcpyHostToDevice, st),
+                      "copy counts");
+            GSEA_CUDA(gsea::launch_stats_ragged<T>(es, K, P, p->counts, P0, static_cast<T*>(p->stats),
+                                                   p->stats_scratch, st),
+                      "round statistics");
+            if ((rc = launch_bound())) return rc;
+        }
         GSEA_CUDA(cudaMemcpyAsync(exceed.data(), p->exceed, sizeof(unsigned long long) * K, cudaMemcpyDeviceToHost, st),
                   "copy exceedances");
         GSEA_CUDA(cudaStreamSynchronize(st), "stream sync");
-        for (int32_t k : active) counts[k] = next;
         if ((rc = decide(now))) return rc;
         for (int32_t k : active) stop[k] = now[k];
-        if (next < P && (rc = q_rule(stop, true))) return rc;
+        if (bound_now) apply_bound(stop);
         cur = next;
         rounds++;
     }

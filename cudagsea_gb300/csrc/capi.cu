@@ -580,6 +580,7 @@ int gsea_plan_set_inputs(gsea_plan p, const void* exprs, const uint8_t* labels, 
     if ((rc = check_inputs(p, p->stream))) return rc;
     GSEA_CUDA(cudaStreamSynchronize(p->stream), "stream sync");
     p->inputs_set = true;
+    p->moments_ready = false;
     return GSEA_OK;
 }
 
@@ -632,6 +633,7 @@ int gsea_plan_run_host(gsea_plan p, const void* exprs, const uint8_t* labels, co
     if ((rc = upload_sets(p, set_offsets, set_genes, st, true))) return rc;
     if ((rc = check_inputs(p, st))) return rc;
     p->inputs_set = true;
+    p->moments_ready = false;
     rc = p->cfg.precision == 64 ? execute_t<double>(p, st) : execute_t<float>(p, st);
     if (rc) return rc;
     if (injected("d2h")) return fail(GSEA_ERR_INJECTED, "injected device-to-host failure");

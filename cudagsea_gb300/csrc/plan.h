@@ -83,6 +83,7 @@ struct gsea_plan_s {
     bool use_graph = true;
     // adaptive allocation / model features
     double* moments = nullptr;         // mean, sd, skewness of the observed ranking metric
+    bool moments_ready = false;        // moments hold the current inputs' values
     int32_t* active = nullptr;         // [K] set list of the current adaptive round
     int64_t* counts = nullptr;         // [K] scores held per set (ragged statistics)
     unsigned long long* exceed = nullptr;  // [K] #{|S| >= |ES|} per set
