@@ -24,6 +24,11 @@ statistics) over the whole workload.
                  under profiles/ (the stage is instruction bound: its data
                  stay in shared memory, so the HBM fraction is small by
                  construction).
+* pipeline_roofline
+                 the whole step against its compulsory HBM bytes, e*G*S +
+                 P*(2*e*G + 8*G + e*K): the expression table once, per
+                 permutation the metric keys and u32 ranks written and read
+                 back and the ES column written.
 * forms.adaptive / forms.learned
                  the adaptive permutation test (tensor-core form) without
                  and with the learned prior: wall time of the whole adaptive
@@ -600,6 +605,14 @@ def run_ours(args):
     lim = issue_limiter(dominant)
     if lim is not None:
         roof["limiter"] = lim
+    # the whole pipeline against its compulsory bytes: X once, then per
+    # permutation the metric keys written + read, the u32 ranks written +
+    # read and the ES column written
+    Gd, Sd = d.num_genes, d.num_samples
+    pipe_bytes = esize * Gd * Sd + P * (2 * esize * Gd + 8 * Gd + esize * K)
+    pipe_gbs = pipe_bytes / (mean_ms / 1e3) / 1e9
+    pipeline_roof = {"bound": "hbm", "algorithmic_bytes": pipe_bytes, "achieved": pipe_gbs, "peak": peak,
+                     "unit": "GB/s", "frac": pipe_gbs / peak}
 
     out = None
     if rank == 0:
@@ -625,6 +638,7 @@ def run_ours(args):
                                   if "chosen" in measured else None),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": roof,
+            "pipeline_roofline": pipeline_roof,
             "stages_ms": stage_avg,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
