@@ -264,12 +264,14 @@ def test_fdr_bound_matches_oracle(gpu):
     sums = np.concatenate([[a[k, :counts[k]].sum() for k in range(K)],
                            [(a[k, :counts[k]] ** 2).sum() for k in range(K)]])
     p_fwer = int(counts.min())
-    for z in (0.0, 3.0):
-        st, q = allocator.fdr_lower_bound(torch.as_tensor(es).cuda(), counts, p_fwer, sums, z)
-        st_o, q_o = M.fdr_bound(es, counts, p_fwer, sums, z)
-        np.testing.assert_allclose(q.cpu().numpy(), q_o, rtol=1e-5, atol=1e-7)
-        if z == 0.0:
-            np.testing.assert_allclose(q.cpu().numpy(), st.cpu().numpy().reshape(5, -1)[4], rtol=1e-6)
+    for dt in (np.float32, np.float64):
+        e = es.astype(dt)
+        for z in (0.0, 3.0):
+            st, q = allocator.fdr_lower_bound(torch.as_tensor(e).cuda(), counts, p_fwer, sums, z)
+            st_o, q_o = M.fdr_bound(e, counts, p_fwer, sums, z, dtype=dt)
+            np.testing.assert_allclose(q.cpu().numpy(), q_o, rtol=1e-5, atol=1e-7)
+            if z == 0.0:
+                np.testing.assert_allclose(q.cpu().numpy(), st.cpu().numpy().reshape(5, -1)[4], rtol=1e-6)
 
 
 def test_fdr_rule_saves_scores_with_the_full_tests_calls(gpu):
@@ -289,3 +291,35 @@ def test_fdr_rule_saves_scores_with_the_full_tests_calls(gpu):
     assert reports[0.0]["stopped_q"] == 0
     assert reports[1.5]["stopped_q"] > 0
     assert scores[1.5] < scores[0.0], scores
+
+
+def test_adaptive_double_precision_matches_full_test(gpu):
+    """doublePrecision: the adaptive test (both rules) in FP64 -- every score a
+    set received is the full FP64 run's, sets run to completion keep their
+    ES / NES / NP, and the calls are the full test's outside the band."""
+    d = case(seed=91, K=200)
+    x = d.exprs.astype(np.float64)
+    full = api.Plan(d.num_genes, d.num_samples, d.num_sets, P_MAX, "twopass_signal2noise", precision=64)
+    full.set_inputs(x, d.labels, d.set_offsets, d.set_genes)
+    full.execute()
+    es_f, st_f = full.read()
+    st_f = st_f.reshape(5, -1)
+    full.close()
+    plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, P_MAX, "twopass_signal2noise", precision=64)
+    plan.set_inputs(x, d.labels, d.set_offsets, d.set_genes)
+    res = allocator.execute_adaptive(plan, None, pilot_perms=250)
+    es_a, st_a = plan.read()
+    st_a = st_a.reshape(5, -1)
+    plan.close()
+    counts = res.counts
+    assert counts.min() >= 250 and counts.max() <= P_MAX and res.report["scores"] < d.num_sets * P_MAX
+    for k in range(d.num_sets):
+        assert np.array_equal(es_a[k, :counts[k]].view(np.uint64), es_f[k, :counts[k]].view(np.uint64)), k
+    fullk = counts == P_MAX
+    for r in (0, 1, 2):
+        assert np.array_equal(st_a[r, fullk].view(np.uint64), st_f[r, fullk].view(np.uint64))
+    calls_f = set(np.where(st_f[4] < Q_CALL)[0])
+    calls = set(np.where(st_a[4] < Q_CALL)[0])
+    for k in sorted(calls ^ calls_f):
+        assert abs(st_f[4][k] - Q_CALL) <= Q_BAND, (k, st_f[4][k], st_a[4][k])
+    assert np.all(counts[sorted(calls)] == P_MAX)
