@@ -332,61 +332,88 @@ class_stats_kernel(const unsigned char* __restrict__ A1, const unsigned char* __
 // ---------------------------------------------------------------------------
 // operand preparation
 
-// per gene: the mean over all samples (FP64, kept as FP32: mu_f) and the
-// totals of x - mu_f and (x - mu_f)^2 in FP64 -- centred at the same mu_f as
-// the GEMM operands, so class B = totals - class A is exact up to the
-// accumulation.  Block of 256 threads = 32 genes x 8 sample groups: a warp
-// reads 32 consecutive genes of one sample (coalesced); the 8 partial sums of
-// a gene are added in group order.
+// Float-float arithmetic (value = h + l, |l| <= ulp(h)/2) on the FP32 pipe:
+// error-free two-sum and two-product (FMA), so sums of a few hundred terms
+// and the operand splits keep ~44 bits -- more than the FP32 results need --
+// without the FP64 pipe.
+struct FF {
+    float h, l;
+};
+__device__ __forceinline__ FF two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ FF fast_two_sum(float a, float b) {  // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+    const FF s = two_sum(a.h, b.h);
+    return fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ FF ff_sq(FF a) {  // (h + l)^2, the l^2 term dropped
+    const float p = __fmul_rn(a.h, a.h);
+    const float e = __fmaf_rn(a.h, a.h, -p);
+    return fast_two_sum(p, __fmaf_rn(__fadd_rn(a.h, a.h), a.l, e));
+}
+__device__ __forceinline__ double ff_value(FF a) { return (double)a.h + (double)a.l; }
+
+// per gene: the mean over all samples (kept as FP32: mu_f) and the totals of
+// x - mu_f and (x - mu_f)^2 -- centred at the same mu_f as the GEMM operands,
+// so class B = totals - class A is exact up to the accumulation.  Sums in
+// float-float; x - mu_f is exact as a float-float.  Block of 256 threads =
+// 32 genes x 8 sample groups: a warp reads 32 consecutive genes of one sample
+// (coalesced); the 8 partial sums of a gene are added in group order.
 template <class T>
 __global__ void __launch_bounds__(256) gene_moments_kernel(const T* __restrict__ X, int G, int S,
                                                            float* __restrict__ mu_f, double* __restrict__ t1,
                                                            double* __restrict__ t2) {
-    __shared__ double part[8][32], part2[8][32];
+    __shared__ FF part[8][32], part2[8][32];
     __shared__ float s_mu[32];
     const int gi = threadIdx.x & 31, j = threadIdx.x >> 5;
     const int g = blockIdx.x * 32 + gi;
     const bool gv = g < G;
-    double s = 0.0;
+    FF s = {0.f, 0.f};
     if (gv)
-        for (int i = j; i < S; i += 8) s += (double)X[(size_t)i * G + g];
+        for (int i = j; i < S; i += 8) s = ff_add(s, FF{(float)X[(size_t)i * G + g], 0.f});
     part[j][gi] = s;
     __syncthreads();
     if (j == 0) {
-        double tot = 0.0;
-        for (int k = 0; k < 8; k++) tot += part[k][gi];
-        s_mu[gi] = (float)(tot / S);
+        FF tot = {0.f, 0.f};
+        for (int k = 0; k < 8; k++) tot = ff_add(tot, part[k][gi]);
+        s_mu[gi] = (float)(ff_value(tot) / S);
     }
     __syncthreads();
-    const double mu = (double)s_mu[gi];
-    double a = 0.0, b = 0.0;
+    const float mu = s_mu[gi];
+    FF a = {0.f, 0.f}, b = {0.f, 0.f};
     if (gv)
         for (int i = j; i < S; i += 8) {
-            const double d = (double)X[(size_t)i * G + g] - mu;
-            a += d;
-            b += d * d;
+            const FF d = two_sum((float)X[(size_t)i * G + g], -mu);
+            a = ff_add(a, d);
+            b = ff_add(b, ff_sq(d));
         }
     part[j][gi] = a;
     part2[j][gi] = b;
     __syncthreads();
     if (j == 0 && gv) {
-        double ta = 0.0, tb = 0.0;
+        FF ta = {0.f, 0.f}, tb = {0.f, 0.f};
         for (int k = 0; k < 8; k++) {
-            ta += part[k][gi];
-            tb += part2[k][gi];
+            ta = ff_add(ta, part[k][gi]);
+            tb = ff_add(tb, part2[k][gi]);
         }
         mu_f[g] = s_mu[gi];
-        t1[g] = ta;
-        t2[g] = tb;
+        t1[g] = ff_value(ta);
+        t2[g] = ff_value(tb);
     }
 }
 
-__device__ __forceinline__ void split3(double v, __nv_bfloat16& hi, __nv_bfloat16& mid, __nv_bfloat16& lo) {
-    hi = __double2bfloat16(v);
-    const double r1 = v - (double)__bfloat162float(hi);
-    mid = __double2bfloat16(r1);
-    const double r2 = r1 - (double)__bfloat162float(mid);
-    lo = __double2bfloat16(r2);
+// v = hi + mid + lo, three BF16 values: hi = bf16(v.h); v.h - hi and
+// r1 - mid are exact (Sterbenz), so the parts carry v to ~2^-25 relative
+__device__ __forceinline__ void split3(FF v, __nv_bfloat16& hi, __nv_bfloat16& mid, __nv_bfloat16& lo) {
+    hi = __float2bfloat16_rn(v.h);
+    const float r1 = __fadd_rn(__fsub_rn(v.h, __bfloat162float(hi)), v.l);
+    mid = __float2bfloat16_rn(r1);
+    lo = __float2bfloat16_rn(__fsub_rn(r1, __bfloat162float(mid)));
 }
 
 __device__ __forceinline__ uint4 pack8(const __nv_bfloat16 (&a)[8]) {
@@ -408,14 +435,14 @@ __global__ void split_operands_kernel(const T* __restrict__ X, int G, int S, int
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int s0 = blockIdx.y * 8;
     if (g >= G) return;
-    const double mu = (double)mu_f[g];
+    const float mu = mu_f[g];
     __nv_bfloat16 p[3][8], q[3][8];
     const int ns = S - s0 < 8 ? S - s0 : 8;
 #pragma unroll
     for (int e = 0; e < 8; e++) {
-        const double d = e < ns ? (double)X[(size_t)(s0 + e) * G + g] - mu : 0.0;
+        const FF d = e < ns ? two_sum((float)X[(size_t)(s0 + e) * G + g], -mu) : FF{0.f, 0.f};
         split3(d, p[0][e], p[1][e], p[2][e]);
-        split3(d * d, q[0][e], q[1][e], q[2][e]);
+        split3(ff_sq(d), q[0][e], q[1][e], q[2][e]);
     }
     const int gt = g / BM, row = g % BM;
     for (int part = 0; part < 3; part++) {
