@@ -6,24 +6,26 @@
 // contractions
 //     SA [g][p] = sum_s x'[s][g]   * L[s][p]
 //     SA2[g][p] = sum_s x'[s][g]^2 * L[s][p]
-// over centred values x' = x - mean_g (the gene mean over all samples, FP64);
-// class B follows from the per-gene totals (T1 - SA, T2 - SA2).
+// over centred values x' = x - mean_g (the gene mean over all samples, kept
+// as FP32; x' exact as a float-float); class B follows from the per-gene
+// totals (T1 - SA, T2 - SA2).
 //
 // Operands: x' and x'^2 are split into three BF16 parts each (hi + mid + lo
 // carries ~24 significant bits) stacked along K, the labels are exact 0/1 in
 // BF16 and repeated for each part, so one BF16 x BF16 -> FP32 GEMM of depth
-// 3*S gives each sum.  A CTA owns 128 genes x 256 permutations:
-//   * two FP32 accumulators in tensor memory (columns 0-255: SA,
-//     256-511: SA2), allocated with tcgen05.alloc;
+// 3*S gives each sum.  A CTA owns 128 genes x 128 (two CTAs per SM, 2
+// stages, the default) or 256 permutations (one CTA per SM, 3 stages):
+//   * two FP32 accumulators in tensor memory (SA in the first TN columns,
+//     SA2 in the next TN), allocated with tcgen05.alloc;
 //   * the operands are pre-arranged in the canonical no-swizzle K-major
 //     layout (8x8 core matrices of 128 bytes), 64 K-elements per chunk, so a
 //     chunk of A (16 KB), A2 (16 KB) and B (32 KB) is one contiguous 1-D TMA
-//     bulk copy each (cp.async.bulk) completing on an mbarrier; three stages
-//     in flight, a stage refilled as soon as the MMAs of its chunk retired;
-//   * one thread issues tcgen05.mma (M=128, N=256, K=16) with shared-memory
-//     descriptors and tcgen05.commit to the stage's mbarrier (the tile may be
-//     tuned to 128 permutations: N=128, 256 TMEM columns, 16 KB of B per
-//     chunk; the sums are the same MMA chain per element either way);
+//     bulk copy each (cp.async.bulk) completing on an mbarrier; two or three
+//     stages in flight, a stage refilled as soon as the MMAs of its chunk
+//     retired;
+//   * one thread issues tcgen05.mma (M=128, N=TN, K=16) with shared-memory
+//     descriptors and tcgen05.commit to the stage's mbarrier (the sums are
+//     the same MMA chain per element for either tile);
 //   * eight warps read the accumulators with tcgen05.ld (a warp reads its
 //     lane quarter, 32 lanes x 16 columns at a time, over half of the
 //     columns), finalise the metric and store the keys.
