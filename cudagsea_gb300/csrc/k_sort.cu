@@ -12,10 +12,13 @@
 //     counter; ranks across warps from a digit-major scan of the per-warp
 //     counters.
 //
-// Two variants:
+// Variants:
 //   sort_regs_kernel   the whole segment lives in registers (1024 threads x
 //                      ITEMS keys); each pass exchanges keys and gene ids
 //                      through one shared-memory buffer.  fp32, G <= 20,480.
+//   sort_cluster_kernel the same over a cluster of two CTAs (two SMs), the
+//                      exchange through distributed shared memory.  fp32,
+//                      20,480 < G <= 40,960.
 //   sort_tiled_kernel  any key width and any G: the segment ping-pongs
 //                      between two per-CTA global (L2-resident) buffers and
 //                      each pass streams it in tiles of 4,096 items.
@@ -23,8 +26,12 @@
 // Outputs per permutation: ranks[g] (position of gene g), sorted_abs[r]
 // (|metric| of the gene at position r, the running-sum weight of
 // enrichment_scores.cuh:146,183) and optionally order[r] (gene at position r).
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 #include "kernels.h"
+
+namespace cg = cooperative_groups;
 
 namespace gsea {
 namespace {
@@ -224,6 +231,161 @@ size_t regs_smem_bytes() {
 }
 
 // ---------------------------------------------------------------------------
+// Two-CTA cluster form (fp32, 20,480 < G <= 2 x 1024 x ITEMS): one cluster
+// of two CTAs per permutation, CTA r holding the items of positions
+// [r*TILE, (r+1)*TILE) in registers as sort_regs_kernel does.  A pass ranks
+// items inside each warp as there, then the two CTAs' digit totals are
+// exchanged through distributed shared memory: an item's destination is
+//   sum over digits < d of both CTAs' totals + (CTA 1: CTA 0's total of d)
+//   + the earlier warps of its CTA + its rank in its warp,
+// stable because CTA 0 holds the earlier positions.  Keys, then gene ids,
+// are scattered into the exchange buffer of the CTA that owns the
+// destination (local or remote shared-memory stores) and gathered back in
+// position order.  Cluster barriers separate the phases; nothing spins.
+template <class T, class RankT, int ITEMS>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
+sort_cluster_kernel(const T* __restrict__ keys, int G, int num_perms, bool descending,
+                    RankT* __restrict__ ranks, T* __restrict__ sorted_abs, uint32_t* __restrict__ order) {
+    using U = typename RadixKey<T>::U;
+    constexpr int TILE = kThreads * ITEMS;
+    extern __shared__ __align__(16) unsigned char smem[];
+    U* exch = reinterpret_cast<U*>(smem);                                   // [TILE]
+    uint16_t* dst16 = reinterpret_cast<uint16_t*>(smem + sizeof(U) * TILE);  // [TILE]
+    uint32_t(*cnt)[256] = reinterpret_cast<uint32_t(*)[256]>(smem + (sizeof(U) + 2) * TILE);
+    uint32_t* tot = reinterpret_cast<uint32_t*>(cnt + kWarps);  // this CTA's digit totals
+    uint32_t* base = tot + 256;                                  // destination base per digit
+    uint32_t* warp_sums = base + 256;                            // [8]
+
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank = (int)cluster.block_rank();
+    const int peer = rank ^ 1;
+    U* const peer_exch = cluster.map_shared_rank(exch, peer);
+    U* const buf0 = rank == 0 ? exch : peer_exch;  // positions [0, TILE)
+    U* const buf1 = rank == 0 ? peer_exch : exch;  // positions [TILE, 2*TILE)
+    const uint32_t* peer_tot = cluster.map_shared_rank(tot, peer);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t lt = lanemask_lt();
+    const int my0 = warp * 32 * ITEMS + lane;  // slot of item i: my0 + 32*i
+    const int first = rank * TILE;              // global position of slot 0
+    const int clusters = gridDim.x >> 1;
+
+    for (int p = blockIdx.x >> 1; p < num_perms; p += clusters) {
+        const T* kp = keys + (int64_t)p * G;
+        U key[ITEMS];
+        uint32_t val[ITEMS];
+#pragma unroll
+        for (int i = 0; i < ITEMS; i++) {
+            const int pos = first + my0 + 32 * i;
+            key[i] = pos < G ? RadixKey<T>::from(kp[pos], descending) : ~U(0);
+            val[i] = (uint32_t)pos;
+        }
+        for (int shift = 0; shift < 8 * (int)sizeof(U); shift += 8) {
+            for (int d = lane; d < 256; d += 32) cnt[warp][d] = 0;
+            __syncwarp();
+#pragma unroll
+            for (int i = 0; i < ITEMS; i++) {
+                const uint32_t dig = digit_of(key[i], shift);
+                const uint32_t peers = match_digit<8>(dig);
+                const int leader = __ffs(peers) - 1;
+                uint32_t before = 0;
+                if (lane == leader) before = atomicAdd(&cnt[warp][dig], (uint32_t)__popc(peers));
+                before = __shfl_sync(kFullMask, before, leader);
+                dst16[my0 + 32 * i] = (uint16_t)(before + __popc(peers & lt));
+            }
+            __syncthreads();
+            // exclusive over the warps, per digit; this CTA's totals
+            if (threadIdx.x < 256) {
+                uint32_t run = 0;
+                for (int w = 0; w < kWarps; w++) {
+                    const uint32_t c = cnt[w][threadIdx.x];
+                    cnt[w][threadIdx.x] = run;
+                    run += c;
+                }
+                tot[threadIdx.x] = run;
+            }
+            cluster.sync();  // both CTAs' totals visible
+            bool skip = false;
+            if (threadIdx.x < 256) {
+                const int d = threadIdx.x;
+                const uint32_t t0 = rank == 0 ? tot[d] : peer_tot[d];
+                const uint32_t t1 = rank == 0 ? peer_tot[d] : tot[d];
+                const uint32_t both = t0 + t1;
+                uint32_t incl = both;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(kFullMask, incl, o);
+                    if (lane >= o) incl += y;
+                }
+                if (lane == 31) warp_sums[d >> 5] = incl;
+                base[d] = incl - both + (rank == 1 ? t0 : 0u);  // warp part; the earlier warps added below
+                skip = both == (uint32_t)(2 * TILE);
+            }
+            // every key has the same digit (both CTAs see the same totals)
+            const bool all_same = __syncthreads_or(skip) != 0;
+            if (threadIdx.x < 256) {
+                uint32_t before = 0;
+                for (int w = 0; w < (threadIdx.x >> 5); w++) before += warp_sums[w];
+                base[threadIdx.x] += before;
+            }
+            cluster.sync();  // the peer has read this CTA's totals
+            if (all_same) continue;
+            if (threadIdx.x < 256) {
+                const uint32_t b = base[threadIdx.x];
+                for (int w = 0; w < kWarps; w++) cnt[w][threadIdx.x] += b;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < ITEMS; i++) {
+                const uint32_t dig = digit_of(key[i], shift);
+                const uint32_t d = cnt[warp][dig] + dst16[my0 + 32 * i];  // global destination < 2*TILE
+                dst16[my0 + 32 * i] = (uint16_t)d;
+                if (d >= (uint32_t)TILE) buf1[d - TILE] = key[i]; else buf0[d] = key[i];
+            }
+            cluster.sync();
+#pragma unroll
+            for (int i = 0; i < ITEMS; i++) key[i] = exch[my0 + 32 * i];
+            cluster.sync();  // both CTAs gathered their keys: the buffers take the gene ids
+#pragma unroll
+            for (int i = 0; i < ITEMS; i++) {
+                const uint32_t d = dst16[my0 + 32 * i];
+                if (d >= (uint32_t)TILE) reinterpret_cast<uint32_t*>(buf1)[d - TILE] = val[i];
+                else reinterpret_cast<uint32_t*>(buf0)[d] = val[i];
+            }
+            cluster.sync();
+#pragma unroll
+            for (int i = 0; i < ITEMS; i++) val[i] = reinterpret_cast<uint32_t*>(exch)[my0 + 32 * i];
+            cluster.sync();  // the buffers are free for the next pass
+        }
+        // outputs: weights (and gene ids) at their positions, coalesced; the
+        // rank of gene g staged in the shared memory of the CTA owning g
+        const int64_t obase = (int64_t)p * G;
+#pragma unroll
+        for (int i = 0; i < ITEMS; i++) {
+            const int pos = first + my0 + 32 * i;
+            if (val[i] < (uint32_t)G) {
+                const uint32_t v = val[i];
+                if (v >= (uint32_t)TILE) reinterpret_cast<RankT*>(buf1)[v - TILE] = (RankT)pos;
+                else reinterpret_cast<RankT*>(buf0)[v] = (RankT)pos;
+                sorted_abs[obase + pos] = cuabs(value_of<T>(key[i], descending));
+                if (order) order[obase + pos] = v;
+            }
+        }
+        cluster.sync();
+        const RankT* s_rk = reinterpret_cast<const RankT*>(exch);
+        const int g_end = min(G, first + TILE);
+        for (int g = first + threadIdx.x; g < g_end; g += kThreads) ranks[obase + g] = s_rk[g - first];
+        cluster.sync();  // the staging is reused by the next permutation
+    }
+}
+
+template <class T, int ITEMS>
+size_t cluster_smem_bytes() {
+    using U = typename RadixKey<T>::U;
+    return (sizeof(U) + 2) * (size_t)kThreads * ITEMS + sizeof(uint32_t) * (kWarps * 256 + 256 + 256 + 8);
+}
+
+// ---------------------------------------------------------------------------
 constexpr int kTileItems = 4;
 constexpr int kTile = kThreads * kTileItems;
 
@@ -371,15 +533,33 @@ cudaError_t launch_regs(const T* keys, int G, int P, bool desc, const SortBuffer
     return cudaGetLastError();
 }
 
+template <class T, class RankT, int ITEMS>
+cudaError_t launch_cluster(const T* keys, int G, int P, bool desc, const SortBuffers& o, cudaStream_t st) {
+    const size_t smem = cluster_smem_bytes<T, ITEMS>();
+    auto kern = sort_cluster_kernel<T, RankT, ITEMS>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int pairs = num_sms() / 2 > 0 ? num_sms() / 2 : 1;
+    const int clusters = P < pairs ? P : pairs;
+    kern<<<2 * clusters, kThreads, smem, st>>>(keys, G, P, desc, static_cast<RankT*>(o.ranks),
+                                               static_cast<T*>(o.sorted_abs), o.order);
+    launches_add(1);
+    return cudaGetLastError();
+}
+
 template <class T, class RankT>
 cudaError_t launch_sort_t(const T* keys, int G, int P, bool desc, const SortBuffers& o, cudaStream_t st) {
-    if (o.variant == 1 && !(sizeof(T) == 4 && G <= kThreads * 20)) return cudaErrorInvalidValue;
-    if (sizeof(T) == 4 && o.variant != 2) {
+    if (o.variant == 1 && !(sizeof(T) == 4 && G <= 2 * kThreads * 20)) return cudaErrorInvalidValue;
+    if constexpr (sizeof(T) == 4) {
+      if (o.variant != 2) {
         if (G <= kThreads * 4) return launch_regs<T, RankT, 4>(keys, G, P, desc, o, st);
         if (G <= kThreads * 8) return launch_regs<T, RankT, 8>(keys, G, P, desc, o, st);
         if (G <= kThreads * 12) return launch_regs<T, RankT, 12>(keys, G, P, desc, o, st);
         if (G <= kThreads * 16) return launch_regs<T, RankT, 16>(keys, G, P, desc, o, st);
         if (G <= kThreads * 20) return launch_regs<T, RankT, 20>(keys, G, P, desc, o, st);
+        if (G <= 2 * kThreads * 16) return launch_cluster<T, RankT, 16>(keys, G, P, desc, o, st);
+        if (G <= 2 * kThreads * 20) return launch_cluster<T, RankT, 20>(keys, G, P, desc, o, st);
+      }
     }
     const int grid = P < num_sms() ? P : num_sms();
     if (o.scratch_bytes < sort_scratch_bytes<T>(G, P)) return cudaErrorInvalidValue;

@@ -35,7 +35,7 @@ struct SortBuffers {
     uint32_t* order;      // optional
     void* scratch;        // per-CTA ping-pong buffers for the tiled variant
     size_t scratch_bytes;
-    int variant = 0;      // 0 automatic, 1 register radix sort (fp32, G <= 20,480), 2 tiled
+    int variant = 0;      // 0 automatic, 1 register radix sort (fp32, G <= 40,960; two-CTA clusters above 20,480), 2 tiled
 };
 template <class T>
 size_t sort_scratch_bytes(int G, int num_perms);

@@ -261,7 +261,8 @@ typedef struct gsea_tuning {
     int32_t metric_pb;    /* plain fp32 metric: permutations per thread, 4 or 8 */
     int32_t chosen_tile;  /* tensor-core form: permutations per tile, 128 (two CTAs per SM, the
                              automatic choice) or 256 (one CTA per SM) */
-    int32_t sort_variant; /* 1 register radix sort (fp32, G <= 20,480), 2 tiled */
+    int32_t sort_variant; /* 1 register radix sort (fp32, G <= 40,960: one CTA up to 20,480, a two-CTA
+                             cluster exchanging through distributed shared memory beyond), 2 tiled */
     int32_t es_warps;     /* warps per CTA of the enrichment kernel: 8, 16 or 32 */
     int32_t es_stage;     /* 1 stage the permutation in shared memory, 0 read it from L2, -1 automatic */
 } gsea_tuning;
