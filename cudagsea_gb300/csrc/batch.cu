@@ -225,7 +225,7 @@ int autotune_b(gsea_batch_s* b, int64_t n) {
         float best = 1e30f;
         gsea::EsTuning pick;
         for (int w : {32, 16, 8}) {
-            for (int stage : {1, 0}) {
+            for (int stage : {1, 2, 0}) {
                 gsea::EsTuning t;
                 t.warps = w;
                 t.stage = stage;

@@ -273,14 +273,16 @@ __device__ __noinline__ T set_score_walk(uint32_t* bm, int w0, int w1, const T* 
     return best;
 }
 
-// One permutation on the calling CTA: stage its ranks and weights (STAGE),
+// One permutation on the calling CTA: stage its ranks and weights (STAGE 1),
+// its ranks only (STAGE 2, the weights then gathered through L1 / L2) or
+// nothing (STAGE 0),
 // then warps take sets from the CTA-wide counter until the CTA's share is
 // scored.  The share is parts [part_lo, part_hi) of `parts` interleaved parts
 // of the set order (part j: slots j, j + parts, j + 2*parts, ...), so that
 // every part mixes large and small sets; parts = 1 takes every set.
 // s_w / s_rank: staging (STAGE), bm: this warp's zeroed bitmap region.
 // Begins and ends with the CTA in step (the staging may be reused after).
-template <class T, class RankT, int WARPS, bool STAGE, int WPL>
+template <class T, class RankT, int WARPS, int STAGE, int WPL>
 __device__ __forceinline__ void es_one_perm(const RankT* rk, const T* wt, int G, const int64_t* __restrict__ set_off,
                                             const int32_t* __restrict__ set_genes,
                                             const int32_t* __restrict__ set_order, const T* __restrict__ decay, int K,
@@ -295,11 +297,11 @@ __device__ __forceinline__ void es_one_perm(const RankT* rk, const T* wt, int G,
     if (tid == 0) *next_set = 0;
     if (STAGE) {
         for (int i = tid; i < G; i += WARPS * 32) {
-            s_w[i] = wt[i];
+            if (STAGE == 1) s_w[i] = wt[i];
             s_rank[i] = rk[i];
         }
         rk = s_rank;
-        wt = s_w;
+        if (STAGE == 1) wt = s_w;
     }
     __syncthreads();
     while (true) {
@@ -350,21 +352,27 @@ __device__ __forceinline__ void es_one_perm(const RankT* rk, const T* wt, int G,
     }
 }
 
+// bytes of a CTA's staging: weights + ranks (1), ranks (2), none (0)
+template <class T, class RankT, int STAGE>
+__host__ __device__ __forceinline__ size_t es_stage_bytes(int G) {
+    return STAGE == 1 ? (sizeof(T) + sizeof(RankT)) * (size_t)G : STAGE == 2 ? sizeof(RankT) * (size_t)G : 0;
+}
+
 // shared memory of a CTA: staging for G genes (STAGE) + WARPS bitmap regions
-template <class T, class RankT, bool STAGE>
+template <class T, class RankT, int STAGE>
 __device__ __forceinline__ void es_smem_layout(unsigned char* smem, int G, int region, T*& s_w, RankT*& s_rank,
                                                uint32_t*& bm) {
     const int warp = threadIdx.x >> 5;
     s_w = reinterpret_cast<T*>(smem);
-    s_rank = reinterpret_cast<RankT*>(smem + (STAGE ? sizeof(T) * (size_t)G : 0));
-    size_t bm_off = STAGE ? (sizeof(T) + sizeof(RankT)) * (size_t)G : 0;
+    s_rank = reinterpret_cast<RankT*>(smem + (STAGE == 1 ? sizeof(T) * (size_t)G : 0));
+    size_t bm_off = es_stage_bytes<T, RankT, STAGE>(G);
     bm_off = (bm_off + 15) & ~(size_t)15;
     bm = reinterpret_cast<uint32_t*>(smem + bm_off) + (size_t)warp * region;
 }
 
 // WPL > 0: bitmap words per lane held in registers by the list procedure
 // (G <= 1024*WPL, ranks < 65536); WPL == 0: general procedure only.
-template <class T, class RankT, int WARPS, bool STAGE, int WPL>
+template <class T, class RankT, int WARPS, int STAGE, int WPL>
 __global__ void __launch_bounds__(WARPS * 32)
 es_kernel(const RankT* __restrict__ ranks, const T* __restrict__ sorted_abs, int G, int num_perms,
           const int64_t* __restrict__ set_off, const int32_t* __restrict__ set_genes,
@@ -419,7 +427,7 @@ es_kernel(const RankT* __restrict__ ranks, const T* __restrict__ sorted_abs, int
 // in order.  item_end[t] = items of tasks 0..t; Gmax sizes the staging and
 // the bitmap regions of the size class (every task: G <= Gmax, and
 // G <= 1024*WPL for WPL > 0).
-template <class T, class RankT, int WARPS, bool STAGE, int WPL>
+template <class T, class RankT, int WARPS, int STAGE, int WPL>
 __global__ void __launch_bounds__(WARPS * 32)
 es_batch_kernel(const EsTask<T>* __restrict__ tasks, const int64_t* __restrict__ item_end, int ntasks,
                 int64_t nitems, unsigned long long* __restrict__ counter, int Gmax) {
@@ -463,14 +471,14 @@ inline int es_wpl(int G, bool ranks16) {
     return 0;
 }
 
-template <class T, class RankT, int WARPS, bool STAGE>
+template <class T, class RankT, int WARPS, int STAGE>
 size_t es_smem_bytes(int G) {
     const int region = es_region_words(G, es_wpl(G, sizeof(RankT) == 2));
-    size_t s = STAGE ? (((sizeof(T) + sizeof(RankT)) * (size_t)G + 15) & ~(size_t)15) : 0;
+    const size_t s = (es_stage_bytes<T, RankT, STAGE>(G) + 15) & ~(size_t)15;
     return s + sizeof(uint32_t) * (size_t)region * WARPS;
 }
 
-template <class T, class RankT, int WARPS, bool STAGE, int WPL>
+template <class T, class RankT, int WARPS, int STAGE, int WPL>
 cudaError_t launch_es_v(const RankT* ranks, const T* sorted_abs, int G, int P, const int64_t* off,
                         const int32_t* genes, const int32_t* order, const T* decay, int K, T* es, int64_t stride,
                         int64_t col0, int grid, cudaStream_t st) {
@@ -488,15 +496,22 @@ cudaError_t launch_es_v(const RankT* ranks, const T* sorted_abs, int G, int P, c
     return cudaGetLastError();
 }
 
-template <class T, class RankT, int WARPS, bool STAGE>
+template <class T, class RankT, int WARPS, int STAGE>
 cudaError_t launch_es_w(const RankT* ranks, const T* sorted_abs, int G, int P, const int64_t* off,
                         const int32_t* genes, const int32_t* order, const T* decay, int K, T* es, int64_t stride,
                         int64_t col0, int grid, cudaStream_t st) {
     // words per lane for the register-resident list procedure (u16 positions);
     // 32-bit ranks (G > 65,536) always take the general procedure
     if constexpr (sizeof(RankT) == 4) {
+        if (STAGE == 2) return cudaErrorInvalidValue;
         return launch_es_v<T, RankT, WARPS, STAGE, 0>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride,
                                                       col0, grid, st);
+    } else if constexpr (STAGE == 2) {  // ranks-only staging: the large-G classes
+        switch (es_wpl(G, true)) {
+            case 24: return launch_es_v<T, RankT, WARPS, 2, 24>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+            case 32: return launch_es_v<T, RankT, WARPS, 2, 32>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+            default: return cudaErrorInvalidValue;
+        }
     } else {
         switch (es_wpl(G, true)) {
             case 4: return launch_es_v<T, RankT, WARPS, STAGE, 4>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
@@ -523,32 +538,40 @@ cudaError_t launch_es_t(const RankT* ranks, const T* sorted_abs, int G, int P, c
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const size_t cap = (size_t)max_smem - 64;  // static shared counter
     const int grid = sms;  // times the resident CTAs per SM; the last round's permutations are split by sets
-    // candidates in the automatic order: most warps first, staged before not
-    struct Cand { int warps; bool stage; size_t smem; };
-    const Cand cands[] = {{32, true, es_smem_bytes<T, RankT, 32, true>(G)},
-                          {16, true, es_smem_bytes<T, RankT, 16, true>(G)},
-                          {8, true, es_smem_bytes<T, RankT, 8, true>(G)},
-                          {32, false, es_smem_bytes<T, RankT, 32, false>(G)},
-                          {16, false, es_smem_bytes<T, RankT, 16, false>(G)},
-                          {8, false, es_smem_bytes<T, RankT, 8, false>(G)}};
+    // candidates in the automatic order: full staging with the most warps,
+    // then ranks-only staging (weights through L1 / L2; the large-G classes,
+    // 24 or 32 bitmap words per lane), then none
+    struct Cand { int warps; int stage; size_t smem; };
+    const Cand cands[] = {{32, 1, es_smem_bytes<T, RankT, 32, 1>(G)},
+                          {16, 1, es_smem_bytes<T, RankT, 16, 1>(G)},
+                          {32, 2, es_smem_bytes<T, RankT, 32, 2>(G)},
+                          {8, 1, es_smem_bytes<T, RankT, 8, 1>(G)},
+                          {16, 2, es_smem_bytes<T, RankT, 16, 2>(G)},
+                          {32, 0, es_smem_bytes<T, RankT, 32, 0>(G)},
+                          {16, 0, es_smem_bytes<T, RankT, 16, 0>(G)},
+                          {8, 0, es_smem_bytes<T, RankT, 8, 0>(G)}};
+    const int wpl = es_wpl(G, sizeof(RankT) == 2);
     for (const Cand& c : cands) {
         if (c.smem > cap) continue;
+        if (c.stage == 2 && wpl != 24 && wpl != 32) continue;
         if (tune.warps && tune.warps != c.warps) continue;
-        if (tune.stage >= 0 && (tune.stage != 0) != c.stage) continue;
+        if (tune.stage >= 0 && tune.stage != c.stage) continue;
 #define GSEA_ES(W, S) \
     return launch_es_w<T, RankT, W, S>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st)
-        if (c.warps == 32 && c.stage) GSEA_ES(32, true);
-        if (c.warps == 16 && c.stage) GSEA_ES(16, true);
-        if (c.warps == 8 && c.stage) GSEA_ES(8, true);
-        if (c.warps == 32) GSEA_ES(32, false);
-        if (c.warps == 16) GSEA_ES(16, false);
-        GSEA_ES(8, false);
+        if (c.warps == 32 && c.stage == 1) GSEA_ES(32, 1);
+        if (c.warps == 16 && c.stage == 1) GSEA_ES(16, 1);
+        if (c.warps == 8 && c.stage == 1) GSEA_ES(8, 1);
+        if (c.warps == 32 && c.stage == 2) GSEA_ES(32, 2);
+        if (c.warps == 16 && c.stage == 2) GSEA_ES(16, 2);
+        if (c.warps == 32) GSEA_ES(32, 0);
+        if (c.warps == 16) GSEA_ES(16, 0);
+        GSEA_ES(8, 0);
 #undef GSEA_ES
     }
     return cudaErrorInvalidValue;  // the requested configuration does not fit
 }
 
-template <class T, int WARPS, bool STAGE, int WPL>
+template <class T, int WARPS, int STAGE, int WPL>
 cudaError_t launch_es_batch_v(const EsTask<T>* tasks, const int64_t* item_end, int ntasks, int64_t nitems,
                               unsigned long long* counter, int Gmax, cudaStream_t st) {
     const size_t smem = es_smem_bytes<T, uint16_t, WARPS, STAGE>(Gmax);
@@ -570,9 +593,16 @@ cudaError_t launch_es_batch_v(const EsTask<T>* tasks, const int64_t* item_end, i
     return cudaGetLastError();
 }
 
-template <class T, int WARPS, bool STAGE>
+template <class T, int WARPS, int STAGE>
 cudaError_t launch_es_batch_w(const EsTask<T>* tasks, const int64_t* item_end, int ntasks, int64_t nitems,
                               unsigned long long* counter, int Gmax, int wpl, cudaStream_t st) {
+    if constexpr (STAGE == 2) {
+        switch (wpl) {
+            case 24: return launch_es_batch_v<T, WARPS, 2, 24>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
+            case 32: return launch_es_batch_v<T, WARPS, 2, 32>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
+            default: return cudaErrorInvalidValue;
+        }
+    } else {
     switch (wpl) {
         case 4: return launch_es_batch_v<T, WARPS, STAGE, 4>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
         case 8: return launch_es_batch_v<T, WARPS, STAGE, 8>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
@@ -583,6 +613,7 @@ cudaError_t launch_es_batch_w(const EsTask<T>* tasks, const int64_t* item_end, i
         case 32: return launch_es_batch_v<T, WARPS, STAGE, 32>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
         case 0: return launch_es_batch_v<T, WARPS, STAGE, 0>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
         default: return cudaErrorInvalidValue;
+    }
     }
 }
 
@@ -599,24 +630,29 @@ cudaError_t launch_es_batch(const EsTask<T>* tasks, const int64_t* item_end, int
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     const size_t cap = (size_t)max_smem - 64;
-    struct Cand { int warps; bool stage; size_t smem; };
-    const Cand cands[] = {{32, true, es_smem_bytes<T, uint16_t, 32, true>(Gmax)},
-                          {16, true, es_smem_bytes<T, uint16_t, 16, true>(Gmax)},
-                          {8, true, es_smem_bytes<T, uint16_t, 8, true>(Gmax)},
-                          {32, false, es_smem_bytes<T, uint16_t, 32, false>(Gmax)},
-                          {16, false, es_smem_bytes<T, uint16_t, 16, false>(Gmax)},
-                          {8, false, es_smem_bytes<T, uint16_t, 8, false>(Gmax)}};
+    struct Cand { int warps; int stage; size_t smem; };
+    const Cand cands[] = {{32, 1, es_smem_bytes<T, uint16_t, 32, 1>(Gmax)},
+                          {16, 1, es_smem_bytes<T, uint16_t, 16, 1>(Gmax)},
+                          {32, 2, es_smem_bytes<T, uint16_t, 32, 2>(Gmax)},
+                          {8, 1, es_smem_bytes<T, uint16_t, 8, 1>(Gmax)},
+                          {16, 2, es_smem_bytes<T, uint16_t, 16, 2>(Gmax)},
+                          {32, 0, es_smem_bytes<T, uint16_t, 32, 0>(Gmax)},
+                          {16, 0, es_smem_bytes<T, uint16_t, 16, 0>(Gmax)},
+                          {8, 0, es_smem_bytes<T, uint16_t, 8, 0>(Gmax)}};
     for (const Cand& c : cands) {
         if (c.smem > cap) continue;
+        if (c.stage == 2 && wpl != 24 && wpl != 32) continue;
         if (tune.warps && tune.warps != c.warps) continue;
-        if (tune.stage >= 0 && (tune.stage != 0) != c.stage) continue;
+        if (tune.stage >= 0 && tune.stage != c.stage) continue;
 #define GSEA_ESB(W, S) return launch_es_batch_w<T, W, S>(tasks, item_end, ntasks, nitems, counter, Gmax, wpl, st)
-        if (c.warps == 32 && c.stage) GSEA_ESB(32, true);
-        if (c.warps == 16 && c.stage) GSEA_ESB(16, true);
-        if (c.warps == 8 && c.stage) GSEA_ESB(8, true);
-        if (c.warps == 32) GSEA_ESB(32, false);
-        if (c.warps == 16) GSEA_ESB(16, false);
-        GSEA_ESB(8, false);
+        if (c.warps == 32 && c.stage == 1) GSEA_ESB(32, 1);
+        if (c.warps == 16 && c.stage == 1) GSEA_ESB(16, 1);
+        if (c.warps == 8 && c.stage == 1) GSEA_ESB(8, 1);
+        if (c.warps == 32 && c.stage == 2) GSEA_ESB(32, 2);
+        if (c.warps == 16 && c.stage == 2) GSEA_ESB(16, 2);
+        if (c.warps == 32) GSEA_ESB(32, 0);
+        if (c.warps == 16) GSEA_ESB(16, 0);
+        GSEA_ESB(8, 0);
 #undef GSEA_ESB
     }
     return cudaErrorInvalidValue;

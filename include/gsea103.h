@@ -264,7 +264,9 @@ typedef struct gsea_tuning {
     int32_t sort_variant; /* 1 register radix sort (fp32, G <= 40,960: one CTA up to 20,480, a two-CTA
                              cluster exchanging through distributed shared memory beyond), 2 tiled */
     int32_t es_warps;     /* warps per CTA of the enrichment kernel: 8, 16 or 32 */
-    int32_t es_stage;     /* 1 stage the permutation in shared memory, 0 read it from L2, -1 automatic */
+    int32_t es_stage;     /* 1 stage the permutation's ranks and weights in shared memory, 2 its ranks
+                             only (24 or 32 bitmap words per lane: 20,481-32,768 genes), 0 read it
+                             from L2, -1 automatic */
 } gsea_tuning;
 /* all automatic */
 void gsea_tuning_init(gsea_tuning* t);
