@@ -31,7 +31,7 @@
 //     weights; its largest and smallest candidates are shifted afterwards by
 //     the weight of the hits before the lane (a second warp scan);
 //   * a warp reduction picks the winner.
-//   With G > 32,768 (or 32-bit ranks) a general procedure walks each lane's
+//   With G > 49,152 (or 32-bit ranks) a general procedure walks each lane's
 //   word range twice from shared memory instead.
 //
 // Rounding: fp32 sums are compensated (Kahan in a lane, float-float across
@@ -39,6 +39,7 @@
 // running sum (the shift adds one rounding); the fp64 path is double
 // throughout.
 #include <climits>
+#include <type_traits>
 
 #include <math_constants.h>
 
@@ -133,14 +134,15 @@ __device__ __forceinline__ void consider(T val, int pos, T& best, int& bpos) {
 template <class T, int WPL>
 __device__ __forceinline__ T set_score_direct(uint32_t* bm, int w0, const T* wt, const T* __restrict__ decay, int G,
                                               int lane, const Acc<T>& Wt) {
-    uint32_t nzm = 0u;  // bit i: word w0 + i holds hits
+    using Mask = typename std::conditional<(WPL > 32), unsigned long long, uint32_t>::type;
+    Mask nzm = 0;  // bit i: word w0 + i holds hits
     int cnt = 0;
 #pragma unroll
     for (int i = 0; i < WPL; i += 4) {
         const uint4 v = *reinterpret_cast<const uint4*>(bm + w0 + i);
         cnt += __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
-        nzm |= (((v.x != 0u) ? 1u : 0u) | ((v.y != 0u) ? 2u : 0u) | ((v.z != 0u) ? 4u : 0u) |
-                ((v.w != 0u) ? 8u : 0u)) << i;
+        nzm |= (Mask)(((v.x != 0u) ? 1u : 0u) | ((v.y != 0u) ? 2u : 0u) | ((v.z != 0u) ? 4u : 0u) |
+                      ((v.w != 0u) ? 8u : 0u)) << i;
     }
     int incl = cnt;
 #pragma unroll
@@ -159,7 +161,7 @@ __device__ __forceinline__ T set_score_direct(uint32_t* bm, int w0, const T* wt,
     int wi = 0;
     for (int t = 0; t < cnt; t++) {
         if (cur == 0u) {  // next nonzero word of the lane
-            wi = __ffs(nzm) - 1;
+            wi = (WPL > 32 ? __ffsll((long long)nzm) : __ffs((int)nzm)) - 1;
             nzm &= nzm - 1;
             cur = bm[w0 + wi];
             bm[w0 + wi] = 0u;
@@ -466,7 +468,7 @@ inline int es_region_words(int G, int wpl) { return wpl > 0 ? wpl * 32 : (G + 31
 inline int es_wpl(int G, bool ranks16) {
     const int need = (((G + 31) >> 5) + 31) >> 5;
     if (!ranks16) return 0;
-    for (int w : {4, 8, 12, 16, 20, 24, 32})
+    for (int w : {4, 8, 12, 16, 20, 24, 32, 40, 48})
         if (need <= w) return w;
     return 0;
 }
@@ -510,6 +512,8 @@ cudaError_t launch_es_w(const RankT* ranks, const T* sorted_abs, int G, int P, c
         switch (es_wpl(G, true)) {
             case 24: return launch_es_v<T, RankT, WARPS, 2, 24>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
             case 32: return launch_es_v<T, RankT, WARPS, 2, 32>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+            case 40: return launch_es_v<T, RankT, WARPS, 2, 40>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+            case 48: return launch_es_v<T, RankT, WARPS, 2, 48>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
             default: return cudaErrorInvalidValue;
         }
     } else {
@@ -521,6 +525,12 @@ cudaError_t launch_es_w(const RankT* ranks, const T* sorted_abs, int G, int P, c
             case 20: return launch_es_v<T, RankT, WARPS, STAGE, 20>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
             case 24: return launch_es_v<T, RankT, WARPS, STAGE, 24>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
             case 32: return launch_es_v<T, RankT, WARPS, STAGE, 32>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+            case 40:  // the staging of ranks and weights never fits beside these regions
+                if constexpr (STAGE == 0) return launch_es_v<T, RankT, WARPS, 0, 40>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+                return cudaErrorInvalidValue;
+            case 48:
+                if constexpr (STAGE == 0) return launch_es_v<T, RankT, WARPS, 0, 48>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+                return cudaErrorInvalidValue;
             default: break;
         }
         return launch_es_v<T, RankT, WARPS, STAGE, 0>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride,
@@ -540,7 +550,7 @@ cudaError_t launch_es_t(const RankT* ranks, const T* sorted_abs, int G, int P, c
     const int grid = sms;  // times the resident CTAs per SM; the last round's permutations are split by sets
     // candidates in the automatic order: full staging with the most warps,
     // then ranks-only staging (weights through L1 / L2; the large-G classes,
-    // 24 or 32 bitmap words per lane), then none
+    // 24-48 bitmap words per lane), then none
     struct Cand { int warps; int stage; size_t smem; };
     const Cand cands[] = {{32, 1, es_smem_bytes<T, RankT, 32, 1>(G)},
                           {16, 1, es_smem_bytes<T, RankT, 16, 1>(G)},
@@ -553,7 +563,8 @@ cudaError_t launch_es_t(const RankT* ranks, const T* sorted_abs, int G, int P, c
     const int wpl = es_wpl(G, sizeof(RankT) == 2);
     for (const Cand& c : cands) {
         if (c.smem > cap) continue;
-        if (c.stage == 2 && wpl != 24 && wpl != 32) continue;
+        if (c.stage == 2 && wpl < 24) continue;
+        if (c.stage == 1 && wpl >= 40) continue;
         if (tune.warps && tune.warps != c.warps) continue;
         if (tune.stage >= 0 && tune.stage != c.stage) continue;
 #define GSEA_ES(W, S) \
@@ -600,6 +611,8 @@ cudaError_t launch_es_batch_w(const EsTask<T>* tasks, const int64_t* item_end, i
         switch (wpl) {
             case 24: return launch_es_batch_v<T, WARPS, 2, 24>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
             case 32: return launch_es_batch_v<T, WARPS, 2, 32>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
+            case 40: return launch_es_batch_v<T, WARPS, 2, 40>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
+            case 48: return launch_es_batch_v<T, WARPS, 2, 48>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
             default: return cudaErrorInvalidValue;
         }
     } else {
@@ -611,6 +624,12 @@ cudaError_t launch_es_batch_w(const EsTask<T>* tasks, const int64_t* item_end, i
         case 20: return launch_es_batch_v<T, WARPS, STAGE, 20>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
         case 24: return launch_es_batch_v<T, WARPS, STAGE, 24>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
         case 32: return launch_es_batch_v<T, WARPS, STAGE, 32>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
+        case 40:
+            if constexpr (STAGE == 0) return launch_es_batch_v<T, WARPS, 0, 40>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
+            return cudaErrorInvalidValue;
+        case 48:
+            if constexpr (STAGE == 0) return launch_es_batch_v<T, WARPS, 0, 48>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
+            return cudaErrorInvalidValue;
         case 0: return launch_es_batch_v<T, WARPS, STAGE, 0>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
         default: return cudaErrorInvalidValue;
     }
@@ -641,7 +660,8 @@ cudaError_t launch_es_batch(const EsTask<T>* tasks, const int64_t* item_end, int
                           {8, 0, es_smem_bytes<T, uint16_t, 8, 0>(Gmax)}};
     for (const Cand& c : cands) {
         if (c.smem > cap) continue;
-        if (c.stage == 2 && wpl != 24 && wpl != 32) continue;
+        if (c.stage == 2 && wpl < 24) continue;
+        if (c.stage == 1 && wpl >= 40) continue;
         if (tune.warps && tune.warps != c.warps) continue;
         if (tune.stage >= 0 && tune.stage != c.stage) continue;
 #define GSEA_ESB(W, S) return launch_es_batch_w<T, W, S>(tasks, item_end, ntasks, nitems, counter, Gmax, wpl, st)
