@@ -1,4 +1,5 @@
-// k_es.cu -- enrichment scores for gene sets x permutations.
+// k_es.cuh -- enrichment scores for gene sets x permutations (included by
+// k_es_f32.cu and k_es_f64.cu, one translation unit per precision).
 //
 // The reference (score_kernel_shared, src/include/enrichment_scores.cuh:91-206)
 // walks the whole ranked list of every (set, permutation) twice: pass 1 sums
@@ -38,6 +39,7 @@
 // lanes), so the fp32 ES stay within a few ulp of the reference's Kahan
 // running sum (the shift adds one rounding); the fp64 path is double
 // throughout.
+#pragma once
 #include <climits>
 #include <type_traits>
 
@@ -638,8 +640,6 @@ cudaError_t launch_es_batch_w(const EsTask<T>* tasks, const int64_t* item_end, i
 
 }  // namespace
 
-int es_size_class(int G) { return es_wpl(G, G <= 65536); }
-
 template <class T>
 cudaError_t launch_es_batch(const EsTask<T>* tasks, const int64_t* item_end, int ntasks, int64_t nitems,
                             unsigned long long* counter, int Gmax, int wpl, EsTuning tune, cudaStream_t st) {
@@ -677,10 +677,6 @@ cudaError_t launch_es_batch(const EsTask<T>* tasks, const int64_t* item_end, int
     }
     return cudaErrorInvalidValue;
 }
-template cudaError_t launch_es_batch<float>(const EsTask<float>*, const int64_t*, int, int64_t, unsigned long long*,
-                                            int, int, EsTuning, cudaStream_t);
-template cudaError_t launch_es_batch<double>(const EsTask<double>*, const int64_t*, int, int64_t,
-                                             unsigned long long*, int, int, EsTuning, cudaStream_t);
 
 template <class T>
 cudaError_t launch_es(const void* ranks, bool ranks16, const T* sorted_abs, int G, int num_perms,
@@ -710,14 +706,6 @@ cudaError_t launch_decay_table(int G, T* decay, cudaStream_t st) {
     launches_add(1);
     return cudaGetLastError();
 }
-template cudaError_t launch_decay_table<float>(int, float*, cudaStream_t);
-template cudaError_t launch_decay_table<double>(int, double*, cudaStream_t);
 
-template cudaError_t launch_es<float>(const void*, bool, const float*, int, int, const int64_t*, const int32_t*,
-                                      const int32_t*, const float*, int, float*, int64_t, int64_t, cudaStream_t,
-                                      EsTuning);
-template cudaError_t launch_es<double>(const void*, bool, const double*, int, int, const int64_t*, const int32_t*,
-                                       const int32_t*, const double*, int, double*, int64_t, int64_t, cudaStream_t,
-                                       EsTuning);
 
 }  // namespace gsea
