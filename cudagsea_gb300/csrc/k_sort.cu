@@ -27,6 +27,7 @@
 // (|metric| of the gene at position r, the running-sum weight of
 // enrichment_scores.cuh:146,183) and optionally order[r] (gene at position r).
 #include <cooperative_groups.h>
+#include <type_traits>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -242,16 +243,23 @@ size_t regs_smem_bytes() {
 // are scattered into the exchange buffer of the CTA that owns the
 // destination (local or remote shared-memory stores) and gathered back in
 // position order.  Cluster barriers separate the phases; nothing spins.
+// pack a key and its gene id into one exchange slot (fp32 keys, at most 16
+// items per thread: the 8-byte buffer then fits beside the rest)
+template <class T, int ITEMS>
+constexpr bool cluster_packed() { return sizeof(typename RadixKey<T>::U) == 4 && ITEMS <= 16; }
+
 template <class T, class RankT, int ITEMS>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
 sort_cluster_kernel(const T* __restrict__ keys, int G, int num_perms, bool descending,
                     RankT* __restrict__ ranks, T* __restrict__ sorted_abs, uint32_t* __restrict__ order) {
     using U = typename RadixKey<T>::U;
+    constexpr bool PACK = cluster_packed<T, ITEMS>();
+    using E = typename std::conditional<PACK, unsigned long long, U>::type;  // exchange slot
     constexpr int TILE = kThreads * ITEMS;
     extern __shared__ __align__(16) unsigned char smem[];
-    U* exch = reinterpret_cast<U*>(smem);                                   // [TILE]
-    uint16_t* dst16 = reinterpret_cast<uint16_t*>(smem + sizeof(U) * TILE);  // [TILE]
-    uint32_t(*cnt)[256] = reinterpret_cast<uint32_t(*)[256]>(smem + (sizeof(U) + 2) * TILE);
+    E* exch = reinterpret_cast<E*>(smem);                                     // [TILE]
+    uint16_t* dst16 = reinterpret_cast<uint16_t*>(smem + sizeof(E) * TILE);  // [TILE]
+    uint32_t(*cnt)[256] = reinterpret_cast<uint32_t(*)[256]>(smem + (sizeof(E) + 2) * TILE);
     uint32_t* tot = reinterpret_cast<uint32_t*>(cnt + kWarps);  // this CTA's digit totals
     uint32_t* base = tot + 256;                                  // destination base per digit
     uint32_t* warp_sums = base + 256;                            // [8]
@@ -259,9 +267,9 @@ sort_cluster_kernel(const T* __restrict__ keys, int G, int num_perms, bool desce
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
     const int peer = rank ^ 1;
-    U* const peer_exch = cluster.map_shared_rank(exch, peer);
-    U* const buf0 = rank == 0 ? exch : peer_exch;  // positions [0, TILE)
-    U* const buf1 = rank == 0 ? peer_exch : exch;  // positions [TILE, 2*TILE)
+    E* const peer_exch = cluster.map_shared_rank(exch, peer);
+    E* const buf0 = rank == 0 ? exch : peer_exch;  // positions [0, TILE)
+    E* const buf1 = rank == 0 ? peer_exch : exch;  // positions [TILE, 2*TILE)
     const uint32_t* peer_tot = cluster.map_shared_rank(tot, peer);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -304,7 +312,8 @@ sort_cluster_kernel(const T* __restrict__ keys, int G, int num_perms, bool desce
                 }
                 tot[threadIdx.x] = run;
             }
-            cluster.sync();  // both CTAs' totals visible
+            // both CTAs' totals visible; the peer finished last pass's gather
+            cluster.sync();
             bool skip = false;
             if (threadIdx.x < 256) {
                 const int d = threadIdx.x;
@@ -323,40 +332,57 @@ sort_cluster_kernel(const T* __restrict__ keys, int G, int num_perms, bool desce
             }
             // every key has the same digit (both CTAs see the same totals)
             const bool all_same = __syncthreads_or(skip) != 0;
+            if (all_same) {
+                cluster.sync();  // the peer has read this CTA's totals before they change
+                continue;
+            }
             if (threadIdx.x < 256) {
                 uint32_t before = 0;
                 for (int w = 0; w < (threadIdx.x >> 5); w++) before += warp_sums[w];
-                base[threadIdx.x] += before;
-            }
-            cluster.sync();  // the peer has read this CTA's totals
-            if (all_same) continue;
-            if (threadIdx.x < 256) {
-                const uint32_t b = base[threadIdx.x];
+                const uint32_t b = base[threadIdx.x] + before;
                 for (int w = 0; w < kWarps; w++) cnt[w][threadIdx.x] += b;
             }
             __syncthreads();
+            if constexpr (PACK) {
+                // key and gene id in one slot: one scatter, one gather
 #pragma unroll
-            for (int i = 0; i < ITEMS; i++) {
-                const uint32_t dig = digit_of(key[i], shift);
-                const uint32_t d = cnt[warp][dig] + dst16[my0 + 32 * i];  // global destination < 2*TILE
-                dst16[my0 + 32 * i] = (uint16_t)d;
-                if (d >= (uint32_t)TILE) buf1[d - TILE] = key[i]; else buf0[d] = key[i];
+                for (int i = 0; i < ITEMS; i++) {
+                    const uint32_t dig = digit_of(key[i], shift);
+                    const uint32_t d = cnt[warp][dig] + dst16[my0 + 32 * i];  // global destination < 2*TILE
+                    const E e = (E)key[i] | ((E)val[i] << 32);
+                    if (d >= (uint32_t)TILE) buf1[d - TILE] = e; else buf0[d] = e;
+                }
+                cluster.sync();  // scattered (the peer read the totals before its scatter)
+#pragma unroll
+                for (int i = 0; i < ITEMS; i++) {
+                    const E e = exch[my0 + 32 * i];
+                    key[i] = (U)(e & 0xFFFFFFFFull);
+                    val[i] = (uint32_t)(e >> 32);
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < ITEMS; i++) {
+                    const uint32_t dig = digit_of(key[i], shift);
+                    const uint32_t d = cnt[warp][dig] + dst16[my0 + 32 * i];  // global destination < 2*TILE
+                    dst16[my0 + 32 * i] = (uint16_t)d;
+                    if (d >= (uint32_t)TILE) buf1[d - TILE] = key[i]; else buf0[d] = key[i];
+                }
+                cluster.sync();
+#pragma unroll
+                for (int i = 0; i < ITEMS; i++) key[i] = exch[my0 + 32 * i];
+                cluster.sync();  // both CTAs gathered their keys: the buffers take the gene ids
+#pragma unroll
+                for (int i = 0; i < ITEMS; i++) {
+                    const uint32_t d = dst16[my0 + 32 * i];
+                    if (d >= (uint32_t)TILE) reinterpret_cast<uint32_t*>(buf1)[d - TILE] = val[i];
+                    else reinterpret_cast<uint32_t*>(buf0)[d] = val[i];
+                }
+                cluster.sync();
+#pragma unroll
+                for (int i = 0; i < ITEMS; i++) val[i] = reinterpret_cast<uint32_t*>(exch)[my0 + 32 * i];
             }
-            cluster.sync();
-#pragma unroll
-            for (int i = 0; i < ITEMS; i++) key[i] = exch[my0 + 32 * i];
-            cluster.sync();  // both CTAs gathered their keys: the buffers take the gene ids
-#pragma unroll
-            for (int i = 0; i < ITEMS; i++) {
-                const uint32_t d = dst16[my0 + 32 * i];
-                if (d >= (uint32_t)TILE) reinterpret_cast<uint32_t*>(buf1)[d - TILE] = val[i];
-                else reinterpret_cast<uint32_t*>(buf0)[d] = val[i];
-            }
-            cluster.sync();
-#pragma unroll
-            for (int i = 0; i < ITEMS; i++) val[i] = reinterpret_cast<uint32_t*>(exch)[my0 + 32 * i];
-            cluster.sync();  // the buffers are free for the next pass
         }
+        cluster.sync();  // both CTAs gathered: the buffers take the ranks
         // outputs: weights (and gene ids) at their positions, coalesced; the
         // rank of gene g staged in the shared memory of the CTA owning g
         const int64_t obase = (int64_t)p * G;
@@ -382,7 +408,8 @@ sort_cluster_kernel(const T* __restrict__ keys, int G, int num_perms, bool desce
 template <class T, int ITEMS>
 size_t cluster_smem_bytes() {
     using U = typename RadixKey<T>::U;
-    return (sizeof(U) + 2) * (size_t)kThreads * ITEMS + sizeof(uint32_t) * (kWarps * 256 + 256 + 256 + 8);
+    const size_t slot = cluster_packed<T, ITEMS>() ? 8 : sizeof(U);
+    return (slot + 2) * (size_t)kThreads * ITEMS + sizeof(uint32_t) * (kWarps * 256 + 256 + 256 + 8);
 }
 
 // ---------------------------------------------------------------------------
