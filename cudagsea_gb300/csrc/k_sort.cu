@@ -131,16 +131,31 @@ __device__ void scan_counters(uint32_t (*cnt)[256], uint32_t* tot, const uint32_
 }
 
 // ---------------------------------------------------------------------------
+// Digit counters of the register sort: 16 bits each (a warp counts at most
+// 32*ITEMS <= 640 items of a digit, a scanned offset is below TILE <= 20,480),
+// two digits to a 32-bit word so that a shifted atomicAdd updates one half
+// without carry into the other.
+__device__ __forceinline__ uint32_t cnt16_add(uint32_t* words, uint32_t dig, uint32_t n) {
+    const uint32_t sh = (dig & 1u) << 4;
+    return (atomicAdd(&words[dig >> 1], n << sh) >> sh) & 0xFFFFu;
+}
+
+// fp32 keys, the whole segment in registers (1024 threads x ITEMS keys).  A
+// pass ranks every key inside its warp (per-bit ballots, one shared atomic
+// per digit group), scans the per-warp digit counters digit-major, and moves
+// each (key, gene id) pair as one 8-byte slot through the exchange buffer:
+// one scatter, one gather, two barriers.
 template <class T, class RankT, int ITEMS>
 __global__ void __launch_bounds__(kThreads, 1)
 sort_regs_kernel(const T* __restrict__ keys, int G, int num_perms, bool descending,
                  RankT* __restrict__ ranks, T* __restrict__ sorted_abs, uint32_t* __restrict__ order) {
     using U = typename RadixKey<T>::U;
+    static_assert(sizeof(U) == 4, "register sort: fp32 keys");
     constexpr int TILE = kThreads * ITEMS;
     extern __shared__ __align__(16) unsigned char smem[];
-    U* exch = reinterpret_cast<U*>(smem);                                   // [TILE]
-    uint16_t* dst16 = reinterpret_cast<uint16_t*>(smem + sizeof(U) * TILE);  // [TILE]
-    uint32_t(*cnt)[256] = reinterpret_cast<uint32_t(*)[256]>(smem + (sizeof(U) + 2) * TILE);
+    unsigned long long* exch = reinterpret_cast<unsigned long long*>(smem);      // [TILE] (key, gene id)
+    uint16_t* dst16 = reinterpret_cast<uint16_t*>(smem + 8 * (size_t)TILE);      // [TILE]
+    uint16_t(*cnt)[256] = reinterpret_cast<uint16_t(*)[256]>(smem + 10 * (size_t)TILE);
     uint32_t* tot = reinterpret_cast<uint32_t*>(cnt + kWarps);
     uint32_t* warp_sums = tot + 256;
     uint32_t* flag = warp_sums + 8;
@@ -148,6 +163,7 @@ sort_regs_kernel(const T* __restrict__ keys, int G, int num_perms, bool descendi
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t lt = lanemask_lt();
     const int my0 = warp * 32 * ITEMS + lane;  // slot of item i: my0 + 32*i
+    uint32_t* wcnt = reinterpret_cast<uint32_t*>(cnt[warp]);  // this warp's 128 counter words
     if (threadIdx.x == 0) *flag = 0u;
     __syncthreads();
 
@@ -162,7 +178,7 @@ sort_regs_kernel(const T* __restrict__ keys, int G, int num_perms, bool descendi
             val[i] = (uint32_t)pos;
         }
         for (int shift = 0; shift < 8 * (int)sizeof(U); shift += 8) {
-            for (int d = lane; d < 256; d += 32) cnt[warp][d] = 0;
+            for (int w = lane; w < 128; w += 32) wcnt[w] = 0u;
             __syncwarp();
             // rank within the warp: the lowest lane of each digit group adds
             // the group's size to the warp's digit counter; the atomics of
@@ -174,15 +190,38 @@ sort_regs_kernel(const T* __restrict__ keys, int G, int num_perms, bool descendi
                 const uint32_t peers = match_digit<8>(dig);
                 const int leader = __ffs(peers) - 1;
                 uint32_t before = 0;
-                if (lane == leader) before = atomicAdd(&cnt[warp][dig], (uint32_t)__popc(peers));
+                if (lane == leader) before = cnt16_add(wcnt, dig, (uint32_t)__popc(peers));
                 before = __shfl_sync(kFullMask, before, leader);
                 dst16[my0 + 32 * i] = (uint16_t)(before + __popc(peers & lt));
             }
             __syncthreads();
-            scan_counters(cnt, tot, nullptr, warp_sums);
-            if (threadIdx.x < 256 && tot[threadIdx.x] == (uint32_t)TILE) *flag = 1u;
+            // digit-major exclusive scan of cnt[w][d] (destinations of this tile)
+            uint32_t run = 0;
+            if (threadIdx.x < 256) {
+                for (int w = 0; w < kWarps; w++) {
+                    const uint32_t c = cnt[w][threadIdx.x];
+                    cnt[w][threadIdx.x] = (uint16_t)run;
+                    run += c;
+                }
+                tot[threadIdx.x] = run;
+                if (run == (uint32_t)TILE) *flag = 1u;
+                uint32_t incl = run;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(kFullMask, incl, o);
+                    if (lane >= o) incl += y;
+                }
+                if (lane == 31) warp_sums[threadIdx.x >> 5] = incl;
+                run = incl - run;  // exclusive within this warp of digits
+            }
             __syncthreads();
             const bool skip = *flag != 0u;
+            if (threadIdx.x < 256 && !skip) {
+                uint32_t before = 0;
+                for (int w = 0; w < (threadIdx.x >> 5); w++) before += warp_sums[w];
+                const uint32_t excl = before + run;
+                for (int w = 0; w < kWarps; w++) cnt[w][threadIdx.x] = (uint16_t)(cnt[w][threadIdx.x] + excl);
+            }
             __syncthreads();
             if (threadIdx.x == 0) *flag = 0u;
             if (skip) continue;  // every item has the same digit: order unchanged
@@ -190,26 +229,22 @@ sort_regs_kernel(const T* __restrict__ keys, int G, int num_perms, bool descendi
             for (int i = 0; i < ITEMS; i++) {
                 const uint32_t dig = digit_of(key[i], shift);
                 const uint32_t d = cnt[warp][dig] + dst16[my0 + 32 * i];
-                dst16[my0 + 32 * i] = (uint16_t)d;
-                exch[d] = key[i];
+                exch[d] = (unsigned long long)key[i] | ((unsigned long long)val[i] << 32);
             }
             __syncthreads();
 #pragma unroll
-            for (int i = 0; i < ITEMS; i++) key[i] = exch[my0 + 32 * i];
-            __syncthreads();
-            uint32_t* exv = reinterpret_cast<uint32_t*>(exch);
-#pragma unroll
-            for (int i = 0; i < ITEMS; i++) exv[dst16[my0 + 32 * i]] = val[i];
-            __syncthreads();
-#pragma unroll
-            for (int i = 0; i < ITEMS; i++) val[i] = exv[my0 + 32 * i];
+            for (int i = 0; i < ITEMS; i++) {
+                const unsigned long long e = exch[my0 + 32 * i];
+                key[i] = (U)(e & 0xFFFFFFFFull);
+                val[i] = (uint32_t)(e >> 32);
+            }
             __syncthreads();
         }
         // weights (and gene ids) at their positions: coalesced; ranks by gene:
         // gathered in shared memory first so the global write is coalesced
         // too (exch is free: every pass ended with a barrier)
         const int64_t base = (int64_t)p * G;
-        RankT* s_rk = reinterpret_cast<RankT*>(exch);  // [G] (exch holds TILE >= G keys)
+        RankT* s_rk = reinterpret_cast<RankT*>(exch);  // [G] (exch holds TILE >= G slots)
 #pragma unroll
         for (int i = 0; i < ITEMS; i++) {
             const int pos = my0 + 32 * i;
@@ -227,8 +262,7 @@ sort_regs_kernel(const T* __restrict__ keys, int G, int num_perms, bool descendi
 
 template <class T, int ITEMS>
 size_t regs_smem_bytes() {
-    using U = typename RadixKey<T>::U;
-    return (sizeof(U) + 2) * (size_t)kThreads * ITEMS + sizeof(uint32_t) * (kWarps * 256 + 256 + 8 + 4);
+    return 10 * (size_t)kThreads * ITEMS + sizeof(uint16_t) * kWarps * 256 + sizeof(uint32_t) * (256 + 8 + 4);
 }
 
 // ---------------------------------------------------------------------------
