@@ -167,13 +167,14 @@ def peaks():
 
 STAGE_PROFILES = {"es": "es_kernel_full_20000x200_K1000_152perms.md",
                   "sort": "sort_regs_kernel_full_20000x200_152perms.md",
-                  "metric": "class_stats_kernel_full_20000x200_152perms.md"}
+                  ("metric", "chosen"): "class_stats_kernel_full_20000x200_152perms.md",
+                  ("metric", "plain"): "metric_fast_kernel_full_20000x200_152perms.md"}
 
 
-def issue_limiter(stage):
-    """Issue-slot utilisation of the stage's kernel from its committed ncu
-    summary (the `issue active %` row), or None."""
-    name = STAGE_PROFILES.get(stage)
+def issue_limiter(stage, form):
+    """Issue-slot utilisation of the stage's kernel (in `form`) from its
+    committed ncu summary (the `issue active %` row), or None."""
+    name = STAGE_PROFILES.get(stage) or STAGE_PROFILES.get((stage, form))
     if not name:
         return None
     path = os.path.join(ROOT, "profiles", name)
@@ -602,7 +603,7 @@ def run_ours(args):
     roof = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": tr, "peak_source": peak_kind,
             "algorithmic_bytes": sb[dominant], "avg_ms": stage_avg[dominant]}
-    lim = issue_limiter(dominant)
+    lim = issue_limiter(dominant, head)
     if lim is not None:
         roof["limiter"] = lim
     # the whole pipeline against its compulsory bytes: X once, then per
