@@ -165,25 +165,27 @@ def peaks():
         return 6800.0, "fallback"
 
 
-STAGE_PROFILES = {"es": "es_kernel_full_20000x200_K1000_152perms.md",
-                  "sort": "sort_regs_kernel_full_20000x200_152perms.md",
-                  ("metric", "chosen"): "class_stats_kernel_full_20000x200_152perms.md",
-                  ("metric", "plain"): "metric_fast_kernel_full_20000x200_152perms.md"}
+# the stage's kernel profile and what bounds it (read off that profile)
+STAGE_PROFILES = {"es": ("es_kernel_full_20000x200_K1000_152perms.md", "instruction issue"),
+                  "sort": ("sort_regs_kernel_full_20000x200_152perms.md", "latency (barriers, ballots)"),
+                  ("metric", "chosen"): ("class_stats_kernel_full_20000x200_152perms.md",
+                                         "latency (epilogue, pipeline)"),
+                  ("metric", "plain"): ("metric_fast_kernel_full_20000x200_152perms.md", "latency (L2 loads)")}
 
 
 def issue_limiter(stage, form):
     """Issue-slot utilisation of the stage's kernel (in `form`) from its
     committed ncu summary (the `issue active %` row), or None."""
-    name = STAGE_PROFILES.get(stage) or STAGE_PROFILES.get((stage, form))
-    if not name:
+    entry = STAGE_PROFILES.get(stage) or STAGE_PROFILES.get((stage, form))
+    if not entry:
         return None
+    name, kind = entry
     path = os.path.join(ROOT, "profiles", name)
     try:
         for line in open(path):
             cells = [c.strip() for c in line.strip().strip("|").split("|")]
             if len(cells) == 2 and cells[0] == "issue active %":
-                return {"kind": "instruction issue", "issue_active": float(cells[1]) / 100.0,
-                        "source": "profiles/" + name}
+                return {"kind": kind, "issue_active": float(cells[1]) / 100.0, "source": "profiles/" + name}
     except Exception:
         return None
     return None
