@@ -32,7 +32,7 @@
 //     weights; its largest and smallest candidates are shifted afterwards by
 //     the weight of the hits before the lane (a second warp scan);
 //   * a warp reduction picks the winner.
-//   With G > 49,152 (or 32-bit ranks) a general procedure walks each lane's
+//   With 32-bit ranks (G > 65,536) a general procedure walks each lane's
 //   word range twice from shared memory instead.
 //
 // Rounding: fp32 sums are compensated (Kahan in a lane, float-float across
@@ -470,7 +470,7 @@ inline int es_region_words(int G, int wpl) { return wpl > 0 ? wpl * 32 : (G + 31
 inline int es_wpl(int G, bool ranks16) {
     const int need = (((G + 31) >> 5) + 31) >> 5;
     if (!ranks16) return 0;
-    for (int w : {4, 8, 12, 16, 20, 24, 32, 40, 48})
+    for (int w : {4, 8, 12, 16, 20, 24, 32, 40, 48, 64})
         if (need <= w) return w;
     return 0;
 }
@@ -516,6 +516,7 @@ cudaError_t launch_es_w(const RankT* ranks, const T* sorted_abs, int G, int P, c
             case 32: return launch_es_v<T, RankT, WARPS, 2, 32>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
             case 40: return launch_es_v<T, RankT, WARPS, 2, 40>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
             case 48: return launch_es_v<T, RankT, WARPS, 2, 48>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+            case 64: return launch_es_v<T, RankT, WARPS, 2, 64>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
             default: return cudaErrorInvalidValue;
         }
     } else {
@@ -532,6 +533,9 @@ cudaError_t launch_es_w(const RankT* ranks, const T* sorted_abs, int G, int P, c
                 return cudaErrorInvalidValue;
             case 48:
                 if constexpr (STAGE == 0) return launch_es_v<T, RankT, WARPS, 0, 48>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+                return cudaErrorInvalidValue;
+            case 64:
+                if constexpr (STAGE == 0) return launch_es_v<T, RankT, WARPS, 0, 64>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
                 return cudaErrorInvalidValue;
             default: break;
         }
@@ -552,7 +556,7 @@ cudaError_t launch_es_t(const RankT* ranks, const T* sorted_abs, int G, int P, c
     const int grid = sms;  // times the resident CTAs per SM; the last round's permutations are split by sets
     // candidates in the automatic order: full staging with the most warps,
     // then ranks-only staging (weights through L1 / L2; the large-G classes,
-    // 24-48 bitmap words per lane), then none
+    // 24-64 bitmap words per lane), then none
     struct Cand { int warps; int stage; size_t smem; };
     const Cand cands[] = {{32, 1, es_smem_bytes<T, RankT, 32, 1>(G)},
                           {16, 1, es_smem_bytes<T, RankT, 16, 1>(G)},
@@ -615,6 +619,7 @@ cudaError_t launch_es_batch_w(const EsTask<T>* tasks, const int64_t* item_end, i
             case 32: return launch_es_batch_v<T, WARPS, 2, 32>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
             case 40: return launch_es_batch_v<T, WARPS, 2, 40>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
             case 48: return launch_es_batch_v<T, WARPS, 2, 48>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
+            case 64: return launch_es_batch_v<T, WARPS, 2, 64>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
             default: return cudaErrorInvalidValue;
         }
     } else {
@@ -631,6 +636,9 @@ cudaError_t launch_es_batch_w(const EsTask<T>* tasks, const int64_t* item_end, i
             return cudaErrorInvalidValue;
         case 48:
             if constexpr (STAGE == 0) return launch_es_batch_v<T, WARPS, 0, 48>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
+            return cudaErrorInvalidValue;
+        case 64:
+            if constexpr (STAGE == 0) return launch_es_batch_v<T, WARPS, 0, 64>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
             return cudaErrorInvalidValue;
         case 0: return launch_es_batch_v<T, WARPS, STAGE, 0>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
         default: return cudaErrorInvalidValue;

@@ -265,7 +265,7 @@ typedef struct gsea_tuning {
                              cluster exchanging through distributed shared memory beyond), 2 tiled */
     int32_t es_warps;     /* warps per CTA of the enrichment kernel: 8, 16 or 32 */
     int32_t es_stage;     /* 1 stage the permutation's ranks and weights in shared memory, 2 its ranks
-                             only (24-48 bitmap words per lane: 20,481-49,152 genes), 0 read it
+                             only (24-64 bitmap words per lane: 20,481-65,536 genes), 0 read it
                              from L2, -1 automatic */
 } gsea_tuning;
 /* all automatic */
