@@ -16,7 +16,7 @@
 //   sort_regs_kernel   the whole segment lives in registers (1024 threads x
 //                      ITEMS keys); each pass exchanges keys and gene ids
 //                      through one shared-memory buffer.  fp32, G <= 20,480.
-//   sort_cluster_kernel the same over a cluster of two CTAs (two SMs), the
+//   sort_cluster_kernel the same over a cluster of two CTAs (SMs), the
 //                      exchange through distributed shared memory.  fp32,
 //                      20,480 < G <= 40,960.
 //   sort_tiled_kernel  any key width and any G: the segment ping-pongs
@@ -266,24 +266,24 @@ size_t regs_smem_bytes() {
 }
 
 // ---------------------------------------------------------------------------
-// Two-CTA cluster form (fp32, 20,480 < G <= 2 x 1024 x ITEMS): one cluster
-// of two CTAs per permutation, CTA r holding the items of positions
+// Cluster form (fp32, 20,480 < G <= CL x 1024 x ITEMS): one cluster of CL
+// CTAs (2 or 4) per permutation, CTA r holding the items of positions
 // [r*TILE, (r+1)*TILE) in registers as sort_regs_kernel does.  A pass ranks
-// items inside each warp as there, then the two CTAs' digit totals are
-// exchanged through distributed shared memory: an item's destination is
-//   sum over digits < d of both CTAs' totals + (CTA 1: CTA 0's total of d)
-//   + the earlier warps of its CTA + its rank in its warp,
-// stable because CTA 0 holds the earlier positions.  Keys, then gene ids,
-// are scattered into the exchange buffer of the CTA that owns the
+// items inside each warp as there, then the CTAs' digit totals are read
+// through distributed shared memory: an item's destination is
+//   sum over digits < d of all CTAs' totals + the totals of d of the CTAs
+//   before its own + the earlier warps of its CTA + its rank in its warp,
+// stable because lower CTAs hold the earlier positions.  Each (key, gene id)
+// pair -- one 8-byte slot at up to 16 items per thread, else keys then gene
+// ids -- is stored into the exchange buffer of the CTA that owns its
 // destination (local or remote shared-memory stores) and gathered back in
 // position order.  Cluster barriers separate the phases; nothing spins.
-// pack a key and its gene id into one exchange slot (fp32 keys, at most 16
-// items per thread: the 8-byte buffer then fits beside the rest)
+//
 template <class T, int ITEMS>
 constexpr bool cluster_packed() { return sizeof(typename RadixKey<T>::U) == 4 && ITEMS <= 16; }
 
-template <class T, class RankT, int ITEMS>
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
+template <class T, class RankT, int ITEMS, int CL>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kThreads, 1)
 sort_cluster_kernel(const T* __restrict__ keys, int G, int num_perms, bool descending,
                     RankT* __restrict__ ranks, T* __restrict__ sorted_abs, uint32_t* __restrict__ order) {
     using U = typename RadixKey<T>::U;
@@ -300,19 +300,16 @@ sort_cluster_kernel(const T* __restrict__ keys, int G, int num_perms, bool desce
 
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
-    const int peer = rank ^ 1;
-    E* const peer_exch = cluster.map_shared_rank(exch, peer);
-    E* const buf0 = rank == 0 ? exch : peer_exch;  // positions [0, TILE)
-    E* const buf1 = rank == 0 ? peer_exch : exch;  // positions [TILE, 2*TILE)
-    const uint32_t* peer_tot = cluster.map_shared_rank(tot, peer);
+    // the exchange buffer holding positions [r*TILE, (r+1)*TILE): CTA r's
+    auto buf = [&](uint32_t r) -> E* { return (int)r == rank ? exch : cluster.map_shared_rank(exch, (int)r); };
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t lt = lanemask_lt();
     const int my0 = warp * 32 * ITEMS + lane;  // slot of item i: my0 + 32*i
     const int first = rank * TILE;              // global position of slot 0
-    const int clusters = gridDim.x >> 1;
+    const int clusters = gridDim.x / CL;
 
-    for (int p = blockIdx.x >> 1; p < num_perms; p += clusters) {
+    for (int p = blockIdx.x / CL; p < num_perms; p += clusters) {
         const T* kp = keys + (int64_t)p * G;
         U key[ITEMS];
         uint32_t val[ITEMS];
@@ -351,18 +348,22 @@ sort_cluster_kernel(const T* __restrict__ keys, int G, int num_perms, bool desce
             bool skip = false;
             if (threadIdx.x < 256) {
                 const int d = threadIdx.x;
-                const uint32_t t0 = rank == 0 ? tot[d] : peer_tot[d];
-                const uint32_t t1 = rank == 0 ? peer_tot[d] : tot[d];
-                const uint32_t both = t0 + t1;
-                uint32_t incl = both;
+                uint32_t all = 0, lower = 0;  // every CTA's count of d; those of the CTAs before this one
+#pragma unroll
+                for (int r = 0; r < CL; r++) {
+                    const uint32_t t = r == rank ? tot[d] : cluster.map_shared_rank(tot, r)[d];
+                    all += t;
+                    if (r < rank) lower += t;
+                }
+                uint32_t incl = all;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
                     const uint32_t y = __shfl_up_sync(kFullMask, incl, o);
                     if (lane >= o) incl += y;
                 }
                 if (lane == 31) warp_sums[d >> 5] = incl;
-                base[d] = incl - both + (rank == 1 ? t0 : 0u);  // warp part; the earlier warps added below
-                skip = both == (uint32_t)(2 * TILE);
+                base[d] = incl - all + lower;  // warp part; the earlier warps added below
+                skip = all == (uint32_t)(CL * TILE);
             }
             // every key has the same digit (both CTAs see the same totals)
             const bool all_same = __syncthreads_or(skip) != 0;
@@ -382,9 +383,9 @@ sort_cluster_kernel(const T* __restrict__ keys, int G, int num_perms, bool desce
 #pragma unroll
                 for (int i = 0; i < ITEMS; i++) {
                     const uint32_t dig = digit_of(key[i], shift);
-                    const uint32_t d = cnt[warp][dig] + dst16[my0 + 32 * i];  // global destination < 2*TILE
+                    const uint32_t d = cnt[warp][dig] + dst16[my0 + 32 * i];  // global destination < CL*TILE
                     const E e = (E)key[i] | ((E)val[i] << 32);
-                    if (d >= (uint32_t)TILE) buf1[d - TILE] = e; else buf0[d] = e;
+                    buf(d / TILE)[d % TILE] = e;
                 }
                 cluster.sync();  // scattered (the peer read the totals before its scatter)
 #pragma unroll
@@ -397,9 +398,9 @@ sort_cluster_kernel(const T* __restrict__ keys, int G, int num_perms, bool desce
 #pragma unroll
                 for (int i = 0; i < ITEMS; i++) {
                     const uint32_t dig = digit_of(key[i], shift);
-                    const uint32_t d = cnt[warp][dig] + dst16[my0 + 32 * i];  // global destination < 2*TILE
+                    const uint32_t d = cnt[warp][dig] + dst16[my0 + 32 * i];  // global destination < CL*TILE
                     dst16[my0 + 32 * i] = (uint16_t)d;
-                    if (d >= (uint32_t)TILE) buf1[d - TILE] = key[i]; else buf0[d] = key[i];
+                    buf(d / TILE)[d % TILE] = key[i];
                 }
                 cluster.sync();
 #pragma unroll
@@ -408,8 +409,7 @@ sort_cluster_kernel(const T* __restrict__ keys, int G, int num_perms, bool desce
 #pragma unroll
                 for (int i = 0; i < ITEMS; i++) {
                     const uint32_t d = dst16[my0 + 32 * i];
-                    if (d >= (uint32_t)TILE) reinterpret_cast<uint32_t*>(buf1)[d - TILE] = val[i];
-                    else reinterpret_cast<uint32_t*>(buf0)[d] = val[i];
+                    reinterpret_cast<uint32_t*>(buf(d / TILE))[d % TILE] = val[i];
                 }
                 cluster.sync();
 #pragma unroll
@@ -425,8 +425,7 @@ sort_cluster_kernel(const T* __restrict__ keys, int G, int num_perms, bool desce
             const int pos = first + my0 + 32 * i;
             if (val[i] < (uint32_t)G) {
                 const uint32_t v = val[i];
-                if (v >= (uint32_t)TILE) reinterpret_cast<RankT*>(buf1)[v - TILE] = (RankT)pos;
-                else reinterpret_cast<RankT*>(buf0)[v] = (RankT)pos;
+                reinterpret_cast<RankT*>(buf(v / TILE))[v % TILE] = (RankT)pos;
                 sorted_abs[obase + pos] = cuabs(value_of<T>(key[i], descending));
                 if (order) order[obase + pos] = v;
             }
@@ -594,16 +593,16 @@ cudaError_t launch_regs(const T* keys, int G, int P, bool desc, const SortBuffer
     return cudaGetLastError();
 }
 
-template <class T, class RankT, int ITEMS>
+template <class T, class RankT, int ITEMS, int CL>
 cudaError_t launch_cluster(const T* keys, int G, int P, bool desc, const SortBuffers& o, cudaStream_t st) {
     const size_t smem = cluster_smem_bytes<T, ITEMS>();
-    auto kern = sort_cluster_kernel<T, RankT, ITEMS>;
+    auto kern = sort_cluster_kernel<T, RankT, ITEMS, CL>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    const int pairs = num_sms() / 2 > 0 ? num_sms() / 2 : 1;
-    const int clusters = P < pairs ? P : pairs;
-    kern<<<2 * clusters, kThreads, smem, st>>>(keys, G, P, desc, static_cast<RankT*>(o.ranks),
-                                               static_cast<T*>(o.sorted_abs), o.order);
+    const int groups = num_sms() / CL > 0 ? num_sms() / CL : 1;
+    const int clusters = P < groups ? P : groups;
+    kern<<<CL * clusters, kThreads, smem, st>>>(keys, G, P, desc, static_cast<RankT*>(o.ranks),
+                                                static_cast<T*>(o.sorted_abs), o.order);
     launches_add(1);
     return cudaGetLastError();
 }
@@ -618,8 +617,10 @@ cudaError_t launch_sort_t(const T* keys, int G, int P, bool desc, const SortBuff
         if (G <= kThreads * 12) return launch_regs<T, RankT, 12>(keys, G, P, desc, o, st);
         if (G <= kThreads * 16) return launch_regs<T, RankT, 16>(keys, G, P, desc, o, st);
         if (G <= kThreads * 20) return launch_regs<T, RankT, 20>(keys, G, P, desc, o, st);
-        if (G <= 2 * kThreads * 16) return launch_cluster<T, RankT, 16>(keys, G, P, desc, o, st);
-        if (G <= 2 * kThreads * 20) return launch_cluster<T, RankT, 20>(keys, G, P, desc, o, st);
+        // two-CTA clusters: a four-CTA cluster ran ~2.4x slower per SM
+        // (four-way barriers, scatters to three peers, GPC packing)
+        if (G <= 2 * kThreads * 16) return launch_cluster<T, RankT, 16, 2>(keys, G, P, desc, o, st);
+        if (G <= 2 * kThreads * 20) return launch_cluster<T, RankT, 20, 2>(keys, G, P, desc, o, st);
       }
     }
     const int grid = P < num_sms() ? P : num_sms();
