@@ -4,12 +4,14 @@ one kernel stays small.  Used by the commands recorded under profiles/.
 
     python -m cudagsea_gb300.profile_case [--perms 152] [--reps 2]
         [--precision 32|64] [--form plain|chosen|chosen64] [--batch 0]
-        [--model 0]
+        [--model 0] [--genes 20000]
 
 --batch N   runs N uneven instances through gsea_batch instead (the
             persistent multi-instance enrichment kernel)
 --model N   runs N training steps of the allocator network on samples of the
             run (the model kernels)
+--genes G   the same data with G genes (the large-G sort and enrichment
+            variants: two-CTA cluster sort, ranks-only staging)
 """
 from __future__ import annotations
 
@@ -29,6 +31,7 @@ def main(argv=None) -> int:
     ap.add_argument("--form", choices=sorted(FORMS), default="plain")
     ap.add_argument("--batch", type=int, default=0)
     ap.add_argument("--model", type=int, default=0)
+    ap.add_argument("--genes", type=int, default=20000)
     a = ap.parse_args(argv)
     build.build()
     if a.batch:
@@ -40,7 +43,12 @@ def main(argv=None) -> int:
         print("batch", b.info())
         b.close()
         return 0
-    d = synthetic.full(num_perms=a.perms)
+    if a.genes == 20000:
+        d = synthetic.full(num_perms=a.perms)
+    else:
+        d = synthetic.make(a.genes, 200, 1000, a.perms, seed=4321, n_class_b=100, sd_range=(0.3, 3.0),
+                           n_shift=500, shift_range=(0.5, 2.0), set_min=15, set_max=500, enriched_frac=0.2,
+                           clamp=1e-3, name=f"full_{a.genes}x200_K1000_P{a.perms}")
     plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, a.perms, "twopass_signal2noise",
                     precision=a.precision, form=FORMS[a.form])
     plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
