@@ -22,7 +22,8 @@
 //
 // Work per (set, permutation) is O(G/32 + n) instead of O(G):
 //   * one CTA per permutation stages the rank of every gene and the weight at
-//     every position in shared memory;
+//     every position in shared memory (or, when the bitmaps of large G leave
+//     no room, the ranks only, the weights then read through L1 / L2);
 //   * a warp takes the next set from a CTA-wide counter (largest sets first),
 //     marks its members' ranks in a per-warp bitmap (duplicates collapse) and
 //     sums the weights of the marked ranks (N_R);
