@@ -224,8 +224,8 @@ int autotune_b(gsea_batch_s* b, int64_t n) {
         const int64_t items = std::min<int64_t>(b->classes[ci].nitems, std::max<int64_t>(n, 1) * 4);
         float best = 1e30f;
         gsea::EsTuning pick;
-        for (int w : {32, 16, 8}) {
-            for (int stage : {1, 2, 0}) {
+        for (int w : {32, 24, 16, 8}) {
+            for (int stage : {1, 3, 2, 0}) {
                 gsea::EsTuning t;
                 t.warps = w;
                 t.stage = stage;

@@ -279,8 +279,8 @@ __device__ __noinline__ T set_score_walk(uint32_t* bm, int w0, int w1, const T* 
 }
 
 // One permutation on the calling CTA: stage its ranks and weights (STAGE 1),
-// its ranks only (STAGE 2, the weights then gathered through L1 / L2) or
-// nothing (STAGE 0),
+// its ranks only (STAGE 2, the weights then gathered through L1 / L2), its
+// weights only (STAGE 3, the ranks gathered) or nothing (STAGE 0),
 // then warps take sets from the CTA-wide counter until the CTA's share is
 // scored.  The share is parts [part_lo, part_hi) of `parts` interleaved parts
 // of the set order (part j: slots j, j + parts, j + 2*parts, ...), so that
@@ -302,11 +302,11 @@ __device__ __forceinline__ void es_one_perm(const RankT* rk, const T* wt, int G,
     if (tid == 0) *next_set = 0;
     if (STAGE) {
         for (int i = tid; i < G; i += WARPS * 32) {
-            if (STAGE == 1) s_w[i] = wt[i];
-            s_rank[i] = rk[i];
+            if (STAGE == 1 || STAGE == 3) s_w[i] = wt[i];
+            if (STAGE == 1 || STAGE == 2) s_rank[i] = rk[i];
         }
-        rk = s_rank;
-        if (STAGE == 1) wt = s_w;
+        if (STAGE == 1 || STAGE == 2) rk = s_rank;
+        if (STAGE == 1 || STAGE == 3) wt = s_w;
     }
     __syncthreads();
     while (true) {
@@ -357,10 +357,13 @@ __device__ __forceinline__ void es_one_perm(const RankT* rk, const T* wt, int G,
     }
 }
 
-// bytes of a CTA's staging: weights + ranks (1), ranks (2), none (0)
+// bytes of a CTA's staging: weights + ranks (1), ranks (2), weights (3), none (0)
 template <class T, class RankT, int STAGE>
 __host__ __device__ __forceinline__ size_t es_stage_bytes(int G) {
-    return STAGE == 1 ? (sizeof(T) + sizeof(RankT)) * (size_t)G : STAGE == 2 ? sizeof(RankT) * (size_t)G : 0;
+    return STAGE == 1   ? (sizeof(T) + sizeof(RankT)) * (size_t)G
+           : STAGE == 2 ? sizeof(RankT) * (size_t)G
+           : STAGE == 3 ? sizeof(T) * (size_t)G
+                        : 0;
 }
 
 // shared memory of a CTA: staging for G genes (STAGE) + WARPS bitmap regions
@@ -508,16 +511,16 @@ cudaError_t launch_es_w(const RankT* ranks, const T* sorted_abs, int G, int P, c
     // words per lane for the register-resident list procedure (u16 positions);
     // 32-bit ranks (G > 65,536) always take the general procedure
     if constexpr (sizeof(RankT) == 4) {
-        if (STAGE == 2) return cudaErrorInvalidValue;
+        if (STAGE >= 2) return cudaErrorInvalidValue;
         return launch_es_v<T, RankT, WARPS, STAGE, 0>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride,
                                                       col0, grid, st);
-    } else if constexpr (STAGE == 2) {  // ranks-only staging: the large-G classes
+    } else if constexpr (STAGE >= 2) {  // ranks-only / weights-only staging: the large-G classes
         switch (es_wpl(G, true)) {
-            case 24: return launch_es_v<T, RankT, WARPS, 2, 24>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-            case 32: return launch_es_v<T, RankT, WARPS, 2, 32>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-            case 40: return launch_es_v<T, RankT, WARPS, 2, 40>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-            case 48: return launch_es_v<T, RankT, WARPS, 2, 48>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-            case 64: return launch_es_v<T, RankT, WARPS, 2, 64>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+            case 24: return launch_es_v<T, RankT, WARPS, STAGE, 24>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+            case 32: return launch_es_v<T, RankT, WARPS, STAGE, 32>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+            case 40: return launch_es_v<T, RankT, WARPS, STAGE, 40>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+            case 48: return launch_es_v<T, RankT, WARPS, STAGE, 48>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+            case 64: return launch_es_v<T, RankT, WARPS, STAGE, 64>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
             default: return cudaErrorInvalidValue;
         }
     } else {
@@ -555,22 +558,27 @@ cudaError_t launch_es_t(const RankT* ranks, const T* sorted_abs, int G, int P, c
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const size_t cap = (size_t)max_smem - 64;  // static shared counter
     const int grid = sms;  // times the resident CTAs per SM; the last round's permutations are split by sets
-    // candidates in the automatic order: full staging with the most warps,
-    // then ranks-only staging (weights through L1 / L2; the large-G classes,
-    // 24-64 bitmap words per lane), then none
+    // candidates in the automatic order: 32 warps first (staging ranks and
+    // weights, then weights only, 24 warps with weights only, 32 with ranks
+    // only, 32 with none), then fewer warps -- warps count for more than
+    // staging (measured on 24,000-40,000 genes); the partial stagings are for
+    // the large-G classes (24-64 bitmap words per lane)
     struct Cand { int warps; int stage; size_t smem; };
     const Cand cands[] = {{32, 1, es_smem_bytes<T, RankT, 32, 1>(G)},
-                          {16, 1, es_smem_bytes<T, RankT, 16, 1>(G)},
+                          {32, 3, es_smem_bytes<T, RankT, 32, 3>(G)},
+                          {24, 3, es_smem_bytes<T, RankT, 24, 3>(G)},
                           {32, 2, es_smem_bytes<T, RankT, 32, 2>(G)},
-                          {8, 1, es_smem_bytes<T, RankT, 8, 1>(G)},
-                          {16, 2, es_smem_bytes<T, RankT, 16, 2>(G)},
                           {32, 0, es_smem_bytes<T, RankT, 32, 0>(G)},
+                          {16, 1, es_smem_bytes<T, RankT, 16, 1>(G)},
+                          {24, 2, es_smem_bytes<T, RankT, 24, 2>(G)},
+                          {16, 2, es_smem_bytes<T, RankT, 16, 2>(G)},
+                          {8, 1, es_smem_bytes<T, RankT, 8, 1>(G)},
                           {16, 0, es_smem_bytes<T, RankT, 16, 0>(G)},
                           {8, 0, es_smem_bytes<T, RankT, 8, 0>(G)}};
     const int wpl = es_wpl(G, sizeof(RankT) == 2);
     for (const Cand& c : cands) {
         if (c.smem > cap) continue;
-        if (c.stage == 2 && wpl < 24) continue;
+        if (c.stage >= 2 && wpl < 24) continue;
         if (c.stage == 1 && wpl >= 40) continue;
         if (tune.warps && tune.warps != c.warps) continue;
         if (tune.stage >= 0 && tune.stage != c.stage) continue;
@@ -579,7 +587,10 @@ cudaError_t launch_es_t(const RankT* ranks, const T* sorted_abs, int G, int P, c
         if (c.warps == 32 && c.stage == 1) GSEA_ES(32, 1);
         if (c.warps == 16 && c.stage == 1) GSEA_ES(16, 1);
         if (c.warps == 8 && c.stage == 1) GSEA_ES(8, 1);
+        if (c.warps == 32 && c.stage == 3) GSEA_ES(32, 3);
+        if (c.warps == 24 && c.stage == 3) GSEA_ES(24, 3);
         if (c.warps == 32 && c.stage == 2) GSEA_ES(32, 2);
+        if (c.warps == 24 && c.stage == 2) GSEA_ES(24, 2);
         if (c.warps == 16 && c.stage == 2) GSEA_ES(16, 2);
         if (c.warps == 32) GSEA_ES(32, 0);
         if (c.warps == 16) GSEA_ES(16, 0);
@@ -614,13 +625,13 @@ cudaError_t launch_es_batch_v(const EsTask<T>* tasks, const int64_t* item_end, i
 template <class T, int WARPS, int STAGE>
 cudaError_t launch_es_batch_w(const EsTask<T>* tasks, const int64_t* item_end, int ntasks, int64_t nitems,
                               unsigned long long* counter, int Gmax, int wpl, cudaStream_t st) {
-    if constexpr (STAGE == 2) {
+    if constexpr (STAGE >= 2) {
         switch (wpl) {
-            case 24: return launch_es_batch_v<T, WARPS, 2, 24>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
-            case 32: return launch_es_batch_v<T, WARPS, 2, 32>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
-            case 40: return launch_es_batch_v<T, WARPS, 2, 40>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
-            case 48: return launch_es_batch_v<T, WARPS, 2, 48>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
-            case 64: return launch_es_batch_v<T, WARPS, 2, 64>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
+            case 24: return launch_es_batch_v<T, WARPS, STAGE, 24>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
+            case 32: return launch_es_batch_v<T, WARPS, STAGE, 32>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
+            case 40: return launch_es_batch_v<T, WARPS, STAGE, 40>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
+            case 48: return launch_es_batch_v<T, WARPS, STAGE, 48>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
+            case 64: return launch_es_batch_v<T, WARPS, STAGE, 64>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
             default: return cudaErrorInvalidValue;
         }
     } else {
@@ -660,16 +671,19 @@ cudaError_t launch_es_batch(const EsTask<T>* tasks, const int64_t* item_end, int
     const size_t cap = (size_t)max_smem - 64;
     struct Cand { int warps; int stage; size_t smem; };
     const Cand cands[] = {{32, 1, es_smem_bytes<T, uint16_t, 32, 1>(Gmax)},
-                          {16, 1, es_smem_bytes<T, uint16_t, 16, 1>(Gmax)},
+                          {32, 3, es_smem_bytes<T, uint16_t, 32, 3>(Gmax)},
+                          {24, 3, es_smem_bytes<T, uint16_t, 24, 3>(Gmax)},
                           {32, 2, es_smem_bytes<T, uint16_t, 32, 2>(Gmax)},
-                          {8, 1, es_smem_bytes<T, uint16_t, 8, 1>(Gmax)},
-                          {16, 2, es_smem_bytes<T, uint16_t, 16, 2>(Gmax)},
                           {32, 0, es_smem_bytes<T, uint16_t, 32, 0>(Gmax)},
+                          {16, 1, es_smem_bytes<T, uint16_t, 16, 1>(Gmax)},
+                          {24, 2, es_smem_bytes<T, uint16_t, 24, 2>(Gmax)},
+                          {16, 2, es_smem_bytes<T, uint16_t, 16, 2>(Gmax)},
+                          {8, 1, es_smem_bytes<T, uint16_t, 8, 1>(Gmax)},
                           {16, 0, es_smem_bytes<T, uint16_t, 16, 0>(Gmax)},
                           {8, 0, es_smem_bytes<T, uint16_t, 8, 0>(Gmax)}};
     for (const Cand& c : cands) {
         if (c.smem > cap) continue;
-        if (c.stage == 2 && wpl < 24) continue;
+        if (c.stage >= 2 && wpl < 24) continue;
         if (c.stage == 1 && wpl >= 40) continue;
         if (tune.warps && tune.warps != c.warps) continue;
         if (tune.stage >= 0 && tune.stage != c.stage) continue;
@@ -677,7 +691,10 @@ cudaError_t launch_es_batch(const EsTask<T>* tasks, const int64_t* item_end, int
         if (c.warps == 32 && c.stage == 1) GSEA_ESB(32, 1);
         if (c.warps == 16 && c.stage == 1) GSEA_ESB(16, 1);
         if (c.warps == 8 && c.stage == 1) GSEA_ESB(8, 1);
+        if (c.warps == 32 && c.stage == 3) GSEA_ESB(32, 3);
+        if (c.warps == 24 && c.stage == 3) GSEA_ESB(24, 3);
         if (c.warps == 32 && c.stage == 2) GSEA_ESB(32, 2);
+        if (c.warps == 24 && c.stage == 2) GSEA_ESB(24, 2);
         if (c.warps == 16 && c.stage == 2) GSEA_ESB(16, 2);
         if (c.warps == 32) GSEA_ESB(32, 0);
         if (c.warps == 16) GSEA_ESB(16, 0);

@@ -9,9 +9,9 @@
 //   metric      plain fp32 packed form: 4 or 8 permutations per thread;
 //               tensor-core form: 128- or 256-permutation tiles (the GEMM's N)
 //   sort        register-resident radix sort or the tiled one
-//   enrichment  8 / 16 / 32 warps per CTA; the permutation's ranks and
-//               weights staged in shared memory, its ranks only, or read
-//               from L2
+//   enrichment  8 / 16 / 24 / 32 warps per CTA; the permutation's ranks and
+//               weights staged in shared memory, its ranks only, its
+//               weights only, or read from L2
 // The autotuner runs each stage's candidates on a sample of the plan's own
 // permutations (CUDA events on the plan's stream, best of three after one
 // warm-up run) stage by stage -- metric, then sort on that stage's keys, then
@@ -120,8 +120,8 @@ int autotune_t(gsea_plan_s* p, int64_t n64, unsigned stages, gsea_tuning* best_o
     }
     // enrichment (on the last sort's output: identical for every variant)
     float ebest = 1e30f;
-    for (int w : {32, 16, 8}) {
-        for (int stage : {1, 2, 0}) {
+    for (int w : {32, 24, 16, 8}) {
+        for (int stage : {1, 3, 2, 0}) {
             if (!(stages & kEs)) break;
             gsea::EsTuning et;
             et.warps = w;
@@ -160,8 +160,9 @@ bool valid(const gsea_tuning* t) {
     return (t->metric_pb == 0 || t->metric_pb == 4 || t->metric_pb == 8) &&
            (t->chosen_tile == 0 || t->chosen_tile == 128 || t->chosen_tile == 256) &&
            (t->sort_variant >= 0 && t->sort_variant <= 2) &&
-           (t->es_warps == 0 || t->es_warps == 8 || t->es_warps == 16 || t->es_warps == 32) &&
-           (t->es_stage >= -1 && t->es_stage <= 2);
+           (t->es_warps == 0 || t->es_warps == 8 || t->es_warps == 16 || t->es_warps == 24 ||
+            t->es_warps == 32) &&
+           (t->es_stage >= -1 && t->es_stage <= 3);
 }
 
 }  // namespace
