@@ -514,7 +514,7 @@ cudaError_t launch_es_w(const RankT* ranks, const T* sorted_abs, int G, int P, c
         if (STAGE >= 2) return cudaErrorInvalidValue;
         return launch_es_v<T, RankT, WARPS, STAGE, 0>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride,
                                                       col0, grid, st);
-    } else if constexpr (STAGE >= 2) {  // ranks-only / weights-only staging: the large-G classes
+    } else if constexpr (STAGE >= 2 || WARPS == 24) {  // partial staging / 24 warps: the large-G classes
         switch (es_wpl(G, true)) {
             case 24: return launch_es_v<T, RankT, WARPS, STAGE, 24>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
             case 32: return launch_es_v<T, RankT, WARPS, STAGE, 32>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
@@ -569,6 +569,7 @@ cudaError_t launch_es_t(const RankT* ranks, const T* sorted_abs, int G, int P, c
                           {24, 3, es_smem_bytes<T, RankT, 24, 3>(G)},
                           {32, 2, es_smem_bytes<T, RankT, 32, 2>(G)},
                           {32, 0, es_smem_bytes<T, RankT, 32, 0>(G)},
+                          {24, 0, es_smem_bytes<T, RankT, 24, 0>(G)},
                           {16, 1, es_smem_bytes<T, RankT, 16, 1>(G)},
                           {24, 2, es_smem_bytes<T, RankT, 24, 2>(G)},
                           {16, 2, es_smem_bytes<T, RankT, 16, 2>(G)},
@@ -578,7 +579,7 @@ cudaError_t launch_es_t(const RankT* ranks, const T* sorted_abs, int G, int P, c
     const int wpl = es_wpl(G, sizeof(RankT) == 2);
     for (const Cand& c : cands) {
         if (c.smem > cap) continue;
-        if (c.stage >= 2 && wpl < 24) continue;
+        if ((c.stage >= 2 || c.warps == 24) && wpl < 24) continue;
         if (c.stage == 1 && wpl >= 40) continue;
         if (tune.warps && tune.warps != c.warps) continue;
         if (tune.stage >= 0 && tune.stage != c.stage) continue;
@@ -591,6 +592,7 @@ cudaError_t launch_es_t(const RankT* ranks, const T* sorted_abs, int G, int P, c
         if (c.warps == 24 && c.stage == 3) GSEA_ES(24, 3);
         if (c.warps == 32 && c.stage == 2) GSEA_ES(32, 2);
         if (c.warps == 24 && c.stage == 2) GSEA_ES(24, 2);
+        if (c.warps == 24 && c.stage == 0) GSEA_ES(24, 0);
         if (c.warps == 16 && c.stage == 2) GSEA_ES(16, 2);
         if (c.warps == 32) GSEA_ES(32, 0);
         if (c.warps == 16) GSEA_ES(16, 0);
@@ -625,7 +627,7 @@ cudaError_t launch_es_batch_v(const EsTask<T>* tasks, const int64_t* item_end, i
 template <class T, int WARPS, int STAGE>
 cudaError_t launch_es_batch_w(const EsTask<T>* tasks, const int64_t* item_end, int ntasks, int64_t nitems,
                               unsigned long long* counter, int Gmax, int wpl, cudaStream_t st) {
-    if constexpr (STAGE >= 2) {
+    if constexpr (STAGE >= 2 || WARPS == 24) {
         switch (wpl) {
             case 24: return launch_es_batch_v<T, WARPS, STAGE, 24>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
             case 32: return launch_es_batch_v<T, WARPS, STAGE, 32>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
@@ -675,6 +677,7 @@ cudaError_t launch_es_batch(const EsTask<T>* tasks, const int64_t* item_end, int
                           {24, 3, es_smem_bytes<T, uint16_t, 24, 3>(Gmax)},
                           {32, 2, es_smem_bytes<T, uint16_t, 32, 2>(Gmax)},
                           {32, 0, es_smem_bytes<T, uint16_t, 32, 0>(Gmax)},
+                          {24, 0, es_smem_bytes<T, uint16_t, 24, 0>(Gmax)},
                           {16, 1, es_smem_bytes<T, uint16_t, 16, 1>(Gmax)},
                           {24, 2, es_smem_bytes<T, uint16_t, 24, 2>(Gmax)},
                           {16, 2, es_smem_bytes<T, uint16_t, 16, 2>(Gmax)},
@@ -683,7 +686,7 @@ cudaError_t launch_es_batch(const EsTask<T>* tasks, const int64_t* item_end, int
                           {8, 0, es_smem_bytes<T, uint16_t, 8, 0>(Gmax)}};
     for (const Cand& c : cands) {
         if (c.smem > cap) continue;
-        if (c.stage >= 2 && wpl < 24) continue;
+        if ((c.stage >= 2 || c.warps == 24) && wpl < 24) continue;
         if (c.stage == 1 && wpl >= 40) continue;
         if (tune.warps && tune.warps != c.warps) continue;
         if (tune.stage >= 0 && tune.stage != c.stage) continue;
@@ -695,6 +698,7 @@ cudaError_t launch_es_batch(const EsTask<T>* tasks, const int64_t* item_end, int
         if (c.warps == 24 && c.stage == 3) GSEA_ESB(24, 3);
         if (c.warps == 32 && c.stage == 2) GSEA_ESB(32, 2);
         if (c.warps == 24 && c.stage == 2) GSEA_ESB(24, 2);
+        if (c.warps == 24 && c.stage == 0) GSEA_ESB(24, 0);
         if (c.warps == 16 && c.stage == 2) GSEA_ESB(16, 2);
         if (c.warps == 32) GSEA_ESB(32, 0);
         if (c.warps == 16) GSEA_ESB(16, 0);
