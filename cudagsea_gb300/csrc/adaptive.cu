@@ -264,8 +264,10 @@ int execute_adaptive_t(gsea_plan_s* p, gsea_model model, const gsea_adaptive_par
         if (bound_now) {  // statistics at the new counts, then the bounds: one synchronisation per round
             GSEA_CUDA(cudaMemcpyAsync(p->counts, counts.data(), sizeof(int64_t) * K, cudaMemcpyHostToDevice, st),
                       "copy counts");
+            // the stopping bound's null histogram: the pilot columns of
+            // every set (the final statistics use every score)
             GSEA_CUDA(gsea::launch_stats_ragged<T>(es, K, P, p->counts, P0, static_cast<T*>(p->stats),
-                                                   p->stats_scratch, st),
+                                                   p->stats_scratch, st, P0),
                       "round statistics");
             if ((rc = launch_bound())) return rc;
         }

@@ -228,44 +228,53 @@ __device__ __forceinline__ unsigned upper_bound_t(const T* a, unsigned n, T v) {
 
 constexpr int kHistThreads = 256;
 constexpr int kHistCols = kHistThreads * 8;  // null columns per block
-// grid (K, column chunks): block (k, c) bins the null scores of set k in the
-// chunks c, c + gridDim.y, ... of kHistCols columns of its columns 1..n_k-1
-template <class T>
-__global__ void __launch_bounds__(kHistThreads)
-stats_fdr_hist_kernel(const T* __restrict__ es, int64_t ld, const int64_t* __restrict__ counts,
-                      const T* __restrict__ fac, const T* sorted_pos, const T* sorted_neg,
+// grid (sets, column chunks): block (b, c) bins the null scores of the sets
+// b, b + gridDim.x, ... in the chunks c, c + gridDim.y, ... of kHistCols
+// columns of each set's columns 1..m_k-1, m_k = min(n_k, hist_cols) (the
+// adaptive test's intermediate rounds bin only the pilot columns: the same
+// pooled null, each set's nulls weighted to equal total weight).  With
+// stage_obs the sorted observed keys are copied to shared memory once per
+// block (one resident block per SM with THREADS = 1024 when they need more
+// than the default 48 KB).
+template <class T, int THREADS>
+__global__ void __launch_bounds__(THREADS)
+stats_fdr_hist_kernel(const T* __restrict__ es, int K, int64_t ld, const int64_t* __restrict__ counts,
+                      int64_t hist_cols, const T* __restrict__ fac, const T* sorted_pos, const T* sorted_neg,
                       double* __restrict__ hpos, double* __restrict__ hneg, unsigned long long* __restrict__ totals,
                       bool stage_obs) {
     extern __shared__ __align__(16) unsigned char hist_smem[];  // [2K] T when staged (dynamic size > 0)
-    const int64_t k = blockIdx.x;
-    const int64_t n = counts ? counts[k] : ld;
-    if (n < 2) return;
-    const double w = counts ? (double)(ld - 1) / (double)(n - 1) : 1.0;
+    constexpr int kCols = THREADS * 8;
     const unsigned npos = (unsigned)totals[2], nneg = (unsigned)totals[3];
     if (stage_obs) {  // the binary searches then run in shared memory
         T* s_pos = reinterpret_cast<T*>(hist_smem);
         T* s_neg = s_pos + npos;
-        for (unsigned i = threadIdx.x; i < npos; i += kHistThreads) s_pos[i] = sorted_pos[i];
-        for (unsigned i = threadIdx.x; i < nneg; i += kHistThreads) s_neg[i] = sorted_neg[i];
+        for (unsigned i = threadIdx.x; i < npos; i += THREADS) s_pos[i] = sorted_pos[i];
+        for (unsigned i = threadIdx.x; i < nneg; i += THREADS) s_neg[i] = sorted_neg[i];
         __syncthreads();
         sorted_pos = s_pos;
         sorted_neg = s_neg;
     }
-    const T f = fac[k];
-    const T* row = es + k * ld;
     double* wtot = reinterpret_cast<double*>(totals + 4);
     double cpos = 0.0, cneg = 0.0;
-    for (int64_t c0 = 1 + (int64_t)blockIdx.y * kHistCols; c0 < n; c0 += (int64_t)gridDim.y * kHistCols) {
-        const int64_t c1 = c0 + kHistCols < n ? c0 + kHistCols : n;
-        for (int64_t p = c0 + threadIdx.x; p < c1; p += kHistThreads) {
-            const T v = Exact<T>::mul(row[p], f);
-            if (v >= T(0)) {
-                cpos += w;
-                atomicAdd(&hpos[upper_bound_t(sorted_pos, npos, v)], w);
-            }
-            if (v <= T(0)) {
-                cneg += w;
-                atomicAdd(&hneg[upper_bound_t(sorted_neg, nneg, -v)], w);
+    for (int64_t k = blockIdx.x; k < K; k += gridDim.x) {
+        const int64_t n0 = counts ? counts[k] : ld;
+        const int64_t n = n0 < hist_cols ? n0 : hist_cols;
+        if (n < 2) continue;
+        const double w = counts ? (double)(ld - 1) / (double)(n - 1) : 1.0;
+        const T f = fac[k];
+        const T* row = es + k * ld;
+        for (int64_t c0 = 1 + (int64_t)blockIdx.y * kCols; c0 < n; c0 += (int64_t)gridDim.y * kCols) {
+            const int64_t c1 = c0 + kCols < n ? c0 + kCols : n;
+            for (int64_t p = c0 + threadIdx.x; p < c1; p += THREADS) {
+                const T v = Exact<T>::mul(row[p], f);
+                if (v >= T(0)) {
+                    cpos += w;
+                    atomicAdd(&hpos[upper_bound_t(sorted_pos, npos, v)], w);
+                }
+                if (v <= T(0)) {
+                    cneg += w;
+                    atomicAdd(&hneg[upper_bound_t(sorted_neg, nneg, -v)], w);
+                }
             }
         }
     }
@@ -548,7 +557,8 @@ template size_t stats_scratch_bytes<double>(int, int64_t);
 
 template <class T>
 cudaError_t launch_stats_ragged(const T* es, int K, int64_t ld, const int64_t* counts, int64_t p_fwer, T* stats,
-                                void* scratch, cudaStream_t st) {
+                                void* scratch, cudaStream_t st, int64_t hist_cols) {
+    if (hist_cols <= 0 || hist_cols > ld) hist_cols = ld;
     if (K <= 0 || ld <= 0 || p_fwer <= 0 || p_fwer > ld) return K <= 0 ? cudaSuccess : cudaErrorInvalidValue;
     using U = typename RadixKey<T>::U;
     const RaggedLayout<T> L(scratch, K, p_fwer);
@@ -575,7 +585,7 @@ cudaError_t launch_stats_ragged(const T* es, int K, int64_t ld, const int64_t* c
     stats_fdr_obs_kernel<T><<<(K + wpb - 1) / wpb, wpb * 32, 0, st>>>(K, stats, cnt_obs, lcount, sorted_pos,
                                                                        sorted_neg, totals);
     int rows = 0;
-    if (!counts && ld > 1) {
+    if (!counts && ld > 1 && hist_cols == ld) {
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -591,14 +601,28 @@ cudaError_t launch_stats_ragged(const T* es, int K, int64_t ld, const int64_t* c
         const int W = 2 * (K + 2) + 2;
         stats_fdr_hist_sum_kernel<<<(W + 255) / 256, 256, 0, st>>>(partial, rows, K, hpos, totals);
     } else if (ld > 1) {
-        const int64_t need = (ld - 1 + kHistCols - 1) / kHistCols;
-        const unsigned chunks = (unsigned)(need < 65535 ? need : 65535);
-        // the sorted observed keys (at most 2K values) in shared memory when
-        // they fit the default 48 KB
+        // the sorted observed keys (at most 2K values) in shared memory: per
+        // block (set x column chunk) when they fit the default 48 KB, else
+        // once per resident 1,024-thread block looping over the sets
         const size_t obs_bytes = 2 * sizeof(T) * (size_t)K;
-        const bool stage = obs_bytes <= 48 * 1024;
-        stats_fdr_hist_kernel<T><<<dim3((unsigned)K, chunks), kHistThreads, stage ? obs_bytes : 0, st>>>(
-            es, ld, counts, fac, sorted_pos, sorted_neg, hpos, hneg, totals, stage);
+        int dev = 0, max_smem = 0, sms = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (obs_bytes > 48 * 1024 && obs_bytes + 1024 <= (size_t)max_smem) {
+            auto kern = stats_fdr_hist_kernel<T, 1024>;
+            e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)obs_bytes);
+            if (e != cudaSuccess) return e;
+            kern<<<dim3((unsigned)(K < sms ? K : sms), 1), 1024, obs_bytes, st>>>(
+                es, K, ld, counts, hist_cols, fac, sorted_pos, sorted_neg, hpos, hneg, totals, true);
+        } else {
+            const int64_t need = (hist_cols - 1 + kHistCols - 1) / kHistCols;
+            const unsigned chunks = (unsigned)(need < 65535 ? need : 65535);
+            const bool stage = obs_bytes <= 48 * 1024;
+            stats_fdr_hist_kernel<T, kHistThreads><<<dim3((unsigned)K, chunks), kHistThreads, stage ? obs_bytes : 0,
+                                                      st>>>(es, K, ld, counts, hist_cols, fac, sorted_pos, sorted_neg,
+                                                            hpos, hneg, totals, stage);
+        }
     }
     stats_fdr_suffix_kernel<<<2, 1024, 0, st>>>(hpos, hneg, totals);
     stats_fdr_final_kernel<T><<<(K + 255) / 256, 256, 0, st>>>(K, cnt_obs, lcount, hpos, hneg, totals, stats);
@@ -606,9 +630,9 @@ cudaError_t launch_stats_ragged(const T* es, int K, int64_t ld, const int64_t* c
     return cudaGetLastError();
 }
 template cudaError_t launch_stats_ragged<float>(const float*, int, int64_t, const int64_t*, int64_t, float*, void*,
-                                                cudaStream_t);
+                                                cudaStream_t, int64_t);
 template cudaError_t launch_stats_ragged<double>(const double*, int, int64_t, const int64_t*, int64_t, double*, void*,
-                                                 cudaStream_t);
+                                                 cudaStream_t, int64_t);
 
 template <class T>
 cudaError_t launch_stats(const T* es, int K, int64_t P, T* stats, void* scratch, cudaStream_t st) {

@@ -99,9 +99,11 @@ cudaError_t launch_stats(const T* es, int K, int64_t P, T* stats, void* scratch,
 // Ragged form: row k of es (stride ld) holds counts[k] scores (device array;
 // null means ld for every set); FWER over the first p_fwer columns.  Scratch
 // of stats_scratch_bytes<T>(K, ld) suffices.
+// hist_cols > 0: the FDR null histogram uses each set's first
+// min(n_k, hist_cols) columns only (an estimate of the same pooled null)
 template <class T>
 cudaError_t launch_stats_ragged(const T* es, int K, int64_t ld, const int64_t* counts, int64_t p_fwer, T* stats,
-                                void* scratch, cudaStream_t st);
+                                void* scratch, cudaStream_t st, int64_t hist_cols = 0);
 
 // Chosen form (tcgen05 class statistics, fp32 inputs).  Operand buffers:
 // A1/A2 chosen_a_bytes(G, S) each, B chosen_b_bytes(P_batch, S).
