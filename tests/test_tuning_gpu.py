@@ -116,3 +116,26 @@ def test_graph_replay_matches_direct_launches(gpu, data):
     plan.close()
     for es, st in outs[1:]:
         assert same(es, outs[0][0]) and same(st, outs[0][1])
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_large_g_enrichment_stagings_identical(precision):
+    """24,000 genes (24 bitmap words per lane): every enrichment launch that
+    fits -- ranks and weights staged at 16 warps, weights only or ranks only
+    at 32 / 24 (/ 16) warps, nothing staged at 32 / 24 warps -- gives the
+    automatic choice's ES bit for bit."""
+    d = synthetic.make(24000, 24, 40, 16, seed=5, n_class_b=12, n_shift=200, set_min=15, set_max=400)
+    _, es0, st0 = run(d, precision=precision)
+    configs = [(16, 1), (32, 3), (24, 3), (32, 2), (24, 2), (16, 2), (32, 0), (24, 0)]
+    ran = 0
+    for w, stage in configs:
+        try:
+            _, es, st = run(d, precision=precision, es_warps=w, es_stage=stage)
+        except N.GseaError:
+            # fp64 staging of 24,000 weights (192 KB) does not fit beside 32 bitmaps
+            assert precision == 64 and stage in (1, 3), (w, stage)
+            continue
+        assert same(es, es0), (w, stage)
+        assert same(st, st0), (w, stage)
+        ran += 1
+    assert ran == (8 if precision == 32 else 5), ran
