@@ -4,7 +4,7 @@ one kernel stays small.  Used by the commands recorded under profiles/.
 
     python -m cudagsea_gb300.profile_case [--perms 152] [--reps 2]
         [--precision 32|64] [--form plain|chosen|chosen64] [--batch 0]
-        [--model 0] [--genes 20000]
+        [--model 0] [--genes 20000] [--adaptive 0]
 
 --batch N   runs N uneven instances through gsea_batch instead (the
             persistent multi-instance enrichment kernel)
@@ -12,6 +12,10 @@ one kernel stays small.  Used by the commands recorded under profiles/.
             run (the model kernels)
 --genes G   the same data with G genes (the large-G sort and enrichment
             variants: two-CTA cluster sort, ranks-only staging)
+--adaptive P0
+            one adaptive test (both stopping rules, no model) with a pilot of
+            P0 permutations on the allocator workload (20,000 sets, 100,000
+            permutations)
 """
 from __future__ import annotations
 
@@ -32,8 +36,19 @@ def main(argv=None) -> int:
     ap.add_argument("--batch", type=int, default=0)
     ap.add_argument("--model", type=int, default=0)
     ap.add_argument("--genes", type=int, default=20000)
+    ap.add_argument("--adaptive", type=int, default=0)
     a = ap.parse_args(argv)
     build.build()
+    if a.adaptive:
+        from . import allocator
+        d = synthetic.learned()
+        plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, d.num_perms, "twopass_signal2noise",
+                        form=N.FORM_CHOSEN)
+        plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+        r = allocator.execute_adaptive(plan, None, pilot_perms=a.adaptive)
+        print("adaptive", r.report)
+        plan.close()
+        return 0
     if a.batch:
         ds = synthetic.batch_instances(a.batch, num_perms=a.perms)
         b = api.Batch(ds, precision=a.precision, form=FORMS[a.form])
