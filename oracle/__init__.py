@@ -1,6 +1,6 @@
 """CPU oracle for the GSEA permutation pipeline -- TEST INFRASTRUCTURE ONLY.
 
-Two checkers live here:
+Two oracles live here:
 
 * ``gsea_oracle.cpp`` -- our own C++ restatement of the reference algorithm
   (each stage cites the cudaGSEA file:line it follows), built into

@@ -1,6 +1,6 @@
 #!/usr/bin/env bash
 # Builds the reference's own CPU pipeline (cudaGSEA, read-only sources) into
-# oracle/_ref/ for use as a checker and CPU baseline.  Test infrastructure only.
+# oracle/_ref/ to pin the oracle and serve as the CPU baseline.  Test infrastructure only.
 #
 # Recipe:
 #   * the reference sources are staged in a temporary directory as SYMLINKS

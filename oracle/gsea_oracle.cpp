@@ -1,6 +1,6 @@
 // gsea_oracle.cpp -- CPU restatement of cudaGSEA's permutation pipeline.
 //
-// TEST INFRASTRUCTURE ONLY.  This is the checker the CUDA path is compared
+// TEST INFRASTRUCTURE ONLY.  This is the oracle the CUDA path is compared
 // against; it is imported by tests/, by __graft_entry__.smoke() and by the
 // cpu_baseline / reference leg of bench.py, and by nothing else.  The product
 // library (cudagsea_gb300/csrc) never links or calls it.
