@@ -100,15 +100,81 @@ def dist_env():
     return world, rank, local
 
 
-class Clocks:
-    """nvidia-smi samples during the timed region."""
+class _Nvml:
+    """Read-only clock queries through the driver's NVML library (ctypes):
+    SM clock, maximum SM clock, power draw and the active clock event
+    reasons of one device.  Raises OSError where the library or the device
+    is not available."""
+
+    SM = 1  # NVML_CLOCK_SM
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown"}
 
     def __init__(self, device: int):
+        import ctypes
+        self.c = ctypes
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        rc = 1
+        try:  # the CUDA device's own UUID: NVML and CUDA may number devices differently
+            import torch
+            uuid = "GPU-" + str(torch.cuda.get_device_properties(device).uuid)
+            rc = self.lib.nvmlDeviceGetHandleByUUID(uuid.encode(), ctypes.byref(self.h))
+        except Exception:
+            pass
+        if rc != 0 and self.lib.nvmlDeviceGetHandleByIndex_v2(device, ctypes.byref(self.h)) != 0:
+            raise OSError("no NVML handle")
+        try:
+            self.reasons_fn = self.lib.nvmlDeviceGetCurrentClocksEventReasons
+        except AttributeError:
+            self.reasons_fn = self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        self.max_sm = self._uint(self.lib.nvmlDeviceGetMaxClockInfo, self.SM)
+
+    def _uint(self, fn, *args):
+        v = self.c.c_uint()
+        if fn(self.h, *args, self.c.byref(v)) != 0:
+            raise OSError(fn.__name__)
+        return v.value
+
+    def sample(self):
+        sm = self._uint(self.lib.nvmlDeviceGetClockInfo, self.SM)
+        bits = self.c.c_ulonglong()
+        self.reasons_fn(self.h, self.c.byref(bits))
+        try:
+            watts = self._uint(self.lib.nvmlDeviceGetPowerUsage) / 1e3
+        except OSError:
+            watts = None
+        return sm, self.max_sm, watts, sorted(n for b, n in self.REASONS.items() if bits.value & b)
+
+    def close(self):
+        self.lib.nvmlShutdown()
+
+
+class Clocks:
+    """Clock samples during the timed region: NVML every 10 ms (one sample
+    on entry, before the region's first launch, and one on exit), else
+    nvidia-smi every 200 ms, started before the region begins."""
+
+    def __init__(self, device: int, period_s: float = 0.01):
         self.device = device
+        self.period = period_s
         self.proc = None
-        self.lines = []
+        self.nvml = None
+        self.samples = []  # (sm_mhz, max_sm_mhz, watts, reasons)
+        self.stop = threading.Event()
 
     def __enter__(self):
+        try:
+            self.nvml = _Nvml(self.device)
+        except Exception:
+            self.nvml = None
+        if self.nvml is not None:
+            self.samples.append(self.nvml.sample())
+            self.t = threading.Thread(target=self._poll, daemon=True)
+            self.t.start()
+            return self
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -116,17 +182,47 @@ class Clocks:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.first = threading.Event()
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            self.first.wait(timeout=5.0)
         except Exception:
             self.proc = None
         return self
 
+    def _poll(self):
+        while not self.stop.wait(self.period):
+            try:
+                self.samples.append(self.nvml.sample())
+            except OSError:
+                return
+
     def _read(self):
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                try:
+                    watts = float(f[3])
+                except ValueError:
+                    watts = None
+                try:
+                    self.samples.append((float(f[1]), float(f[2]), watts,
+                                         sorted(n for n, v in zip(names, f[5:9]) if v.lower() == "active")))
+                except ValueError:
+                    pass
+            self.first.set()
+        self.first.set()  # nvidia-smi ended without a sample
 
     def __exit__(self, *exc):
+        if self.nvml is not None:
+            self.stop.set()
+            self.t.join(timeout=5)
+            try:
+                self.samples.append(self.nvml.sample())
+            except OSError:
+                pass
+            self.nvml.close()
         if self.proc:
             self.proc.terminate()
             try:
@@ -135,24 +231,15 @@ class Clocks:
                 self.proc.kill()
 
     def summary(self):
-        sm, mx, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
-            f = [x.strip() for x in line.split(",")]
-            if len(f) < 9:
-                continue
-            try:
-                sm.append(float(f[1]))
-                mx.append(float(f[2]))
-            except ValueError:
-                continue
-            for n, v in zip(names, f[5:9]):
-                if v.lower() == "active":
-                    reasons.add(n)
-        if not sm:
+        if not self.samples:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        sm = [x[0] for x in self.samples]
+        watts = [x[2] for x in self.samples if x[2] is not None]
+        return {"sm_mhz": statistics.median(sm), "sm_min_mhz": min(sm),
+                "sm_max_mhz": max(x[1] for x in self.samples),
+                "reasons": sorted({r for x in self.samples for r in x[3]}),
+                "power_w": statistics.median(watts) if watts else None,
+                "samples": len(sm), "source": "nvml" if self.nvml is not None else "nvidia-smi"}
 
 
 def peaks():
