@@ -145,14 +145,17 @@ def test_tiny_shapes_all_metrics(gpu):
             assert H.es_close(r["es"], es_o, double).all(), (m, double)
 
 
-@pytest.mark.parametrize("G", [1, 31, 4097, 20480, 20481, 30000, 40000, 49152, 65536])
+@pytest.mark.parametrize("G", [1, 31, 4097, 20480, 20481, 30000, 40000, 49152, 65536, 70000, 150001])
 @pytest.mark.parametrize("double", [False, True], ids=["f32", "f64"])
 def test_sort_sizes(gpu, G, double):
     """Register-resident sort up to 20,480 genes (fp32), two-CTA clusters up to
     40,960, tiled sort beyond and for fp64; the ES register procedure up to
-    65,536 genes (ranks-only staging above ~20,000)."""
+    65,536 genes (partial staging above ~20,000); beyond, 32-bit ranks and the
+    general two-walk procedure (16 warps at 70,000 genes, 8 at 150,001, whose
+    last bitmap word is partly used)."""
     d = synthetic.make(G, 12, 3, 5, seed=G, n_class_b=6, n_shift=min(10, G), set_min=1, set_max=min(40, G))
     r = run_plan(d, "twopass_signal2noise", double=double)
+    assert r["ranks"].dtype == (np.uint16 if G <= 65536 else np.uint32)
     sk, order = check_sort(r["keys"], r["order"], r["ranks"], r["sorted"])
     es_o = oracle.es(sk, order, d.set_offsets, d.set_genes)
     assert H.es_close(r["es"], es_o, double).all()
