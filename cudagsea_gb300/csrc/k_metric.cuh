@@ -276,8 +276,11 @@ metric_fast_kernel(const float* __restrict__ X, int G, int S, const uint32_t* __
     unsigned long long mA[PAIRS], mB[PAIRS], vA[PAIRS], vB[PAIRS];
 #pragma unroll
     for (int q = 0; q < PAIRS; q++) mA[q] = mB[q] = vA[q] = vB[q] = 0ull;
+    // samples per unrolled step: four loads of the table in flight (two
+    // for onepass, whose extra accumulators leave no registers for more)
+    constexpr int kUnroll = ACC == ACC_ONEPASS ? 2 : 4;
     // pass 1: class sums (and sums of squares for onepass)
-#pragma unroll 2
+#pragma unroll kUnroll
     for (int sidx = 0; sidx < S; sidx++) {
         const float x = __ldg(xg + (int64_t)sidx * G);
         const unsigned long long xx = f2_pack(x, x);
@@ -331,7 +334,7 @@ metric_fast_kernel(const float* __restrict__ X, int G, int S, const uint32_t* __
             mA[q] = f2_pack(fmA[2 * q], fmA[2 * q + 1]);
             mB[q] = f2_pack(fmB[2 * q], fmB[2 * q + 1]);
         }
-#pragma unroll 2
+#pragma unroll kUnroll
         for (int sidx = 0; sidx < S; sidx++) {
             const float x = __ldg(xg + (int64_t)sidx * G);
             const unsigned long long xx = f2_pack(x, x);
