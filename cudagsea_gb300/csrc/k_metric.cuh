@@ -276,9 +276,9 @@ metric_fast_kernel(const float* __restrict__ X, int G, int S, const uint32_t* __
     unsigned long long mA[PAIRS], mB[PAIRS], vA[PAIRS], vB[PAIRS];
 #pragma unroll
     for (int q = 0; q < PAIRS; q++) mA[q] = mB[q] = vA[q] = vB[q] = 0ull;
-    // samples per unrolled step: four loads of the table in flight (two
+    // samples per unrolled step: eight loads of the table in flight (two
     // for onepass, whose extra accumulators leave no registers for more)
-    constexpr int kUnroll = ACC == ACC_ONEPASS ? 2 : 4;
+    constexpr int kUnroll = ACC == ACC_ONEPASS ? 2 : 8;
     // pass 1: class sums (and sums of squares for onepass)
 #pragma unroll kUnroll
     for (int sidx = 0; sidx < S; sidx++) {
