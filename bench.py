@@ -302,22 +302,35 @@ def stage_bytes(d, P, esize, ranks16):
     }
 
 
-def cpu_sample(d, metric_id, double, target_s, use_ref):
-    """Time the CPU path on a sample of the permutations; returns (ES/s, sample P, seconds, kind)."""
-    import numpy as np
+def cpu_sample(d, metric_id, double, target_s, use_ref, max_s=10.0):
+    """Time the CPU path on a sample of the permutations; returns (ES/s, sample P, seconds, kind).
+
+    Two pilot calls (2n and 4n permutations on n threads: the stages run in
+    parallel over permutations, so fewer than n permutations hide the cost
+    of one) split a call's time into a fixed part and a part per permutation.  The reference's own build has a large
+    fixed part: its CPU pipeline matches gene symbols to every 32-set batch
+    (create_bitmaps) once per call, ~0.85 s at 20,000 genes x 1,000 sets on
+    8 x86 cores, which a full run pays once.  The sample is sized to at least
+    `target_s` of work and to keep the fixed part at most a tenth of it,
+    within `max_s` and the workload's permutation count."""
     import oracle
     kind = "reference" if use_ref else "port"
-    P = 4
-    while True:
+    fn = oracle.ref_gsea if use_ref else oracle.gsea
+
+    def run(P):
         t0 = time.perf_counter()
-        if use_ref:
-            oracle.ref_gsea(metric_id, d.exprs, d.labels, d.set_offsets, d.set_genes, P, double=double)
-        else:
-            oracle.gsea(metric_id, d.exprs, d.labels, d.set_offsets, d.set_genes, P, double=double)
-        dt = time.perf_counter() - t0
-        if dt >= 0.3 * target_s or P >= 512:
-            return d.num_sets * P / dt, P, dt, kind
-        P = min(512, max(P * 2, int(P * target_s / max(dt, 1e-3))))
+        fn(metric_id, d.exprs, d.labels, d.set_offsets, d.set_genes, P, double=double)
+        return time.perf_counter() - t0
+
+    n = int(os.environ.get("OMP_NUM_THREADS") or os.cpu_count() or 1)
+    p1 = max(1, min(2 * n, d.num_perms // 4))
+    t1, t2 = run(p1), run(2 * p1)
+    per = max((t2 - t1) / p1, 1e-6)
+    fixed = max(2 * t1 - t2, 0.0)
+    want = max(target_s - fixed, 9 * fixed) / per
+    P = int(min(d.num_perms, max(2 * p1, want), max((max_s - fixed) / per, 2 * p1)))
+    dt = run(P)
+    return d.num_sets * P / dt, P, dt, kind
 
 
 def run_reference(args):
