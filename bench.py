@@ -584,7 +584,11 @@ def run_ours(args):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     from cudagsea_gb300 import api, build
     from cudagsea_gb300 import _native as N
+    if world > 1 and rank != 0:
+        torch.distributed.barrier()  # rank 0 brings the in-tree build up to date first
     build.build()
+    if world > 1 and rank == 0:
+        torch.distributed.barrier()
     torch.cuda.set_device(local)
     d = workload(args.workload)
     P, K = d.num_perms, d.num_sets

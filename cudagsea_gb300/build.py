@@ -68,15 +68,21 @@ def _stale(obj: str, src: str, newest_header: float) -> bool:
 
 
 def _compile(src: str, obj: str, verbose: bool) -> None:
+    # written under a temporary name and renamed: a build running beside
+    # this one (one process per GPU) never links a half-written object
+    tmp = obj + f".tmp{os.getpid()}"
     if src.endswith(".cu"):
-        cmd = [_nvcc()] + ARCH + NVCC_FLAGS + ["-c", src, "-o", obj]
+        cmd = [_nvcc()] + ARCH + NVCC_FLAGS + ["-c", src, "-o", tmp]
     else:
-        cmd = ["g++"] + CXX_FLAGS + ["-I" + os.path.join(_cuda_home(), "include"), "-c", src, "-o", obj]
+        cmd = ["g++"] + CXX_FLAGS + ["-I" + os.path.join(_cuda_home(), "include"), "-c", src, "-o", tmp]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if r.returncode != 0:
+        if os.path.exists(tmp):
+            os.remove(tmp)
         raise RuntimeError(f"compilation of {os.path.basename(src)} failed:\n{r.stdout}")
+    os.replace(tmp, obj)
 
 
 def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -> str:
