@@ -78,6 +78,9 @@ def parse():
                          "instances in one CUDA graph (each its own JSON line)")
     ap.add_argument("--instances", type=int, default=256, help="instances of the batched workload")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-precision-check", action="store_true",
+                    help="skip the NES check of the tensor-core forms against the plain form in FP64 (outside the "
+                         "timed region)")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the adaptive forms (sequential rule with and without the learned prior)")
     ap.add_argument("--pilot", type=int, default=250, help="pilot permutations of the adaptive forms")
@@ -85,6 +88,8 @@ def parse():
                     help="keep the automatic launch configuration (by default each form's plan is autotuned on a "
                          "sample of its permutations before the warm-up, outside the timed region)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU-baseline sample time")
+    ap.add_argument("--ref-seconds", type=float, default=150.0,
+                    help="reference arm: target time of all warm-up and timed steps together")
     return ap.parse_args()
 
 
@@ -333,38 +338,51 @@ def cpu_sample(d, metric_id, double, target_s, use_ref, max_s=10.0):
     return d.num_sets * P / dt, P, dt, kind
 
 
+def headline_config(d, args, world):
+    """The `config` of both arms' lines (identical, so that the two are
+    compared on the same workload)."""
+    return {"workload": d.name, "metric_string": args.metric, "precision": args.precision,
+            "l2": "256 MB write between timed GPU steps", "parallelism": f"perm-shard x{world}"}
+
+
 def run_reference(args):
+    """The reference's own CPU pipeline (its build from the cudaGSEA sources,
+    oracle/_ref, where it exists on this machine; else the oracle's port of
+    it) on all host cores.  A step is a bounded sample of the workload's
+    permutations -- all sets -- sized so that the warm-up and timed steps
+    together take about `--ref-seconds`."""
     world, rank, _ = dist_env()
     if rank != 0:
         return 0
     import oracle
     from cudagsea_gb300.api import METRICS
     oracle.build()
+    oracle.build_ref()
     d = workload(args.workload)
     mid = METRICS.index(args.metric)
     double = args.precision == 64
     use_ref = oracle.ref_available()
     ncores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(ncores))
-    # size one step's sample to about 2 s of CPU work
-    _, P, dt, kind = cpu_sample(d, mid, double, 2.0, use_ref)
+    fn = oracle.ref_gsea if use_ref else oracle.gsea
+    per_step = min(10.0, max(1.0, args.ref_seconds / max(1, args.steps + args.warmup)))
+    _, P, dt, kind = cpu_sample(d, mid, double, per_step, use_ref, max_s=1.5 * per_step)
     for _ in range(args.warmup):
-        (oracle.ref_gsea if use_ref else oracle.gsea)(mid, d.exprs, d.labels, d.set_offsets, d.set_genes, P,
-                                                       double=double)
+        fn(mid, d.exprs, d.labels, d.set_offsets, d.set_genes, P, double=double)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        (oracle.ref_gsea if use_ref else oracle.gsea)(mid, d.exprs, d.labels, d.set_offsets, d.set_genes, P,
-                                                       double=double)
+        fn(mid, d.exprs, d.labels, d.set_offsets, d.set_genes, P, double=double)
         times.append(time.perf_counter() - t0)
     mean = sum(times) / len(times)
     value = d.num_sets * P / mean
-    sample = f"{P} of {d.num_perms} permutations per step, all {d.num_sets} sets, {d.name}"
+    sample = (f"{P} of {d.num_perms} permutations per step (one call: metric, sort, scores and statistics), "
+              f"all {d.num_sets} sets, {d.name}; {'the reference build' if use_ref else 'the oracle port'}")
     out = {
         "impl": "reference", "metric": METRIC_NAME, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64" if double else "f32", "data": "synthetic",
-        "config": {"workload": d.name, "metric_string": args.metric, "precision": args.precision},
+        "config": headline_config(d, args, world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]),
                          "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -594,14 +612,15 @@ def run_ours(args):
     P, K = d.num_perms, d.num_sets
     double = args.precision == 64
     esize = 8 if double else 4
-    forms = ["plain"] if (double or args.form == "plain-only") else ["plain", "chosen"]
+    forms = ["plain"] if (double or args.form == "plain-only") else ["plain", "chosen", "chosen_fp64"]
+    form_ids = {"plain": N.FORM_PLAIN, "chosen": N.FORM_CHOSEN, "chosen_fp64": N.FORM_CHOSEN_FP64}
     stream = torch.cuda.Stream(device=local)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
     measured = {}
     plans = {}
     clk = None
     for form_name in forms:
-        form = N.FORM_CHOSEN if form_name == "chosen" else N.FORM_PLAIN
+        form = form_ids[form_name]
         plan = api.Plan(d.num_genes, d.num_samples, K, P, args.metric, precision=args.precision, form=form,
                         perm_offset=rank * P, device=local)
         plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
@@ -644,13 +663,14 @@ def run_ours(args):
             mean_ms = float(t.item())
         measured[form_name] = {"mean_ms": mean_ms, "value": world * K * P / (mean_ms / 1e3),
                                "stages": dict(stage_sum), "launches": launches,
-                               "tuning": tuning[0]}
+                               "tuning": tuning[0], "clocks": c.summary()}
         plans[form_name] = plan
-        if form_name == forms[-1]:
-            clk = c
     if "chosen" in measured and world == 1 and not args.no_learned:
         measured.update(run_adaptive(args, d, plans["chosen"], stream, flush, local))
-    head = forms[-1]  # the fastest form computing every score: chosen when available
+    # the headline: the tensor-core form with the error-free FP32 variance when
+    # measured (the fastest form computing every score), else the plain form
+    head = "chosen" if "chosen" in measured else "plain"
+    clk = measured[head]["clocks"]
     plan = plans[head]
     mean_ms = measured[head]["mean_ms"]
     value = measured[head]["value"]
@@ -721,6 +741,33 @@ def run_ours(args):
     pipeline_roof = {"bound": "hbm", "algorithmic_bytes": pipe_bytes, "achieved": pipe_gbs, "peak": peak,
                      "unit": "GB/s", "frac": pipe_gbs / peak}
 
+    # ---- issue-slot roofline of the dominant stage: its warp instructions
+    # per launch (ncu count per (set, permutation) or per permutation, from
+    # the committed profile record) over its event time, against the issue
+    # slots of the SMs at the sampled median SM clock
+    issue_roof = None
+    cnt = traffic_record().get("warp_instructions", {}).get(dominant)
+    if cnt and clk.get("sm_mhz"):
+        units = K * P if cnt.get("per") == "set_perm" else P
+        inst = cnt["value"] * units
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        slots = sms * 4 * clk["sm_mhz"] * 1e6
+        ach = inst / (stage_avg[dominant] / 1e3)
+        issue_roof = {"bound": "issue", "kernel": dominant, "warp_instructions": inst,
+                      "achieved": ach, "peak": slots, "unit": "warp-inst/s", "frac": ach / slots,
+                      "source": cnt.get("source")}
+
+    # ---- the headline's accuracy condition, outside every timed region:
+    # both tensor-core forms against the plain form in FP64 on this workload
+    nes_check = None
+    if rank == 0 and "chosen" in measured and not args.no_precision_check:
+        from cudagsea_gb300 import precision_check as PC
+        t0 = time.perf_counter()
+        reps = PC.check_forms(d, args.metric)
+        nes_check = {name: PC.summary(r) for name, r in reps.items()}
+        nes_check["reference"] = "plain form in FP64, same inputs and permutations"
+        nes_check["seconds"] = time.perf_counter() - t0
+
     out = None
     if rank == 0:
         cpu = None
@@ -736,9 +783,8 @@ def run_ours(args):
             "metric": METRIC_NAME, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if double else "f32", "data": "synthetic",
-            "config": {"workload": d.name, "metric_string": args.metric, "form": head,
-                       "precision": args.precision, "l2": "256 MB write between timed steps",
-                       "parallelism": f"perm-shard x{world}"},
+            "config": headline_config(d, args, world),
+            "form": head,
             "forms": {k: ({"value": v["value"], "ms_per_step": v["mean_ms"], "stages_ms": v["stages"],
                            "tuning": v["tuning"]} if "stages" in v else v) for k, v in measured.items()},
             "chosen_over_plain": (measured["chosen"]["value"] / measured["plain"]["value"]
@@ -746,9 +792,11 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": roof,
             "pipeline_roofline": pipeline_roof,
+            "issue_roofline": issue_roof,
+            "nes_vs_fp64": nes_check,
             "stages_ms": stage_avg,
             "cpu_baseline": cpu,
-            "clocks": clk.summary(),
+            "clocks": clk,
             "gpu_launches": launches,
         }
         print(json.dumps(out), flush=True)

@@ -133,6 +133,8 @@ SIGNATURES = [
     ("gsea_plan_last_launches", ctypes.c_int, [_p, ctypes.POINTER(_i64)]),
     ("gsea_plan_set_profiling", ctypes.c_int, [_p, ctypes.c_int]),
     ("gsea_plan_stage_times", ctypes.c_int, [_p, ctypes.POINTER(ctypes.c_double)]),
+    ("gsea_stats_scratch_bytes", ctypes.c_int, [_i64, _i64, ctypes.c_int, ctypes.POINTER(_sz)]),
+    ("gsea_stats_device", ctypes.c_int, [_p, _i64, _i64, ctypes.c_int, _p, _p, _sz, _p]),
     ("gsea_stats_device_noalloc", ctypes.c_int, [_p, _i64, _i64, ctypes.c_int, _p, _p]),
     ("gsea_tuning_init", None, [ctypes.POINTER(Tuning)]),
     ("gsea_plan_set_tuning", ctypes.c_int, [_p, ctypes.POINTER(Tuning)]),

@@ -12,9 +12,13 @@
 // file-scope __device__ array of kNoAllocScratchBytes (4 MiB) that every GPU
 // loading this library holds until the process exits.  Host code cannot use
 // the array's name as a device address, so the address is looked up with
-// cudaGetSymbolAddress once per device, with that device current, the first
-// time the entry point runs on it; make that first call before any stream
-// capture.  All calls share the array and it keeps the previous call's
+// cudaGetSymbolAddress, with the device current, the first time the entry
+// point runs on a device's context: the look-up is cached per device under
+// the context's process-unique id (cuCtxGetId), so that a context that was
+// reset (cudaDeviceReset) and re-created -- whose module, and with it the
+// array, is loaded anew -- gets a fresh look-up instead of a stale address.
+// Make the first call on a context before any stream capture.  All calls
+// share the array and it keeps the previous call's
 // contents: the counters that must start at zero are cleared on the stream
 // by every call, and calls whose work overlaps on the GPU race on the array.
 #include <cstdint>
@@ -37,6 +41,43 @@ static __device__ __align__(256) unsigned char g_stats_scratch[kNoAllocScratchBy
 
 std::mutex g_lock;
 void* g_scratch_addr[kMaxDevices] = {};
+unsigned long long g_scratch_ctx[kMaxDevices] = {};  // context id of each cached address (0: none)
+
+// the driver's cuCtxGetCurrent / cuCtxGetId, fetched through the runtime (no
+// link against the driver library); null where the driver lacks them
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
+struct CtxFns {
+    CtxGetCurrentFn current = nullptr;
+    CtxGetIdFn id = nullptr;
+};
+const CtxFns& ctx_fns() {
+    static const CtxFns fns = [] {
+        CtxFns f;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            f.current = reinterpret_cast<CtxGetCurrentFn>(p);
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            f.id = reinterpret_cast<CtxGetIdFn>(p);
+        return f;
+    }();
+    return fns;
+}
+
+// process-unique id of the current context, 0 if unknown (no context yet, or
+// a driver without cuCtxGetId: every call then looks the address up again)
+unsigned long long current_context_id() {
+    const CtxFns& f = ctx_fns();
+    if (!f.current || !f.id) return 0;
+    void* ctx = nullptr;
+    if (f.current(&ctx) != 0 || !ctx) return 0;
+    unsigned long long id = 0;
+    return f.id(ctx, &id) == 0 ? id : 0;
+}
 
 int scratch_for_current_device(void** out) {
     int dev = 0;
@@ -50,14 +91,16 @@ int scratch_for_current_device(void** out) {
         return GSEA_ERR_UNSUPPORTED;
     }
     std::lock_guard<std::mutex> guard(g_lock);
-    if (!g_scratch_addr[dev]) {
+    const unsigned long long ctx = current_context_id();
+    if (!g_scratch_addr[dev] || ctx == 0 || ctx != g_scratch_ctx[dev]) {
         void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_stats_scratch);
+        e = cudaGetSymbolAddress(&p, g_stats_scratch);  // creates the context if there is none yet
         if (e != cudaSuccess || !p) {
             gsea::set_last_error((std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e)).c_str());
             return GSEA_ERR_CUDA;
         }
         g_scratch_addr[dev] = p;
+        g_scratch_ctx[dev] = ctx != 0 ? ctx : current_context_id();
     }
     *out = g_scratch_addr[dev];
     return GSEA_OK;

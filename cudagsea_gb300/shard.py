@@ -72,13 +72,18 @@ def run_sharded(d, num_perms: int, metric="twopass_signal2noise", precision: int
     es_local, _ = plan.read(stats=False)
     plan.close()
     es = gather_es(es_local[:, :count], num_perms, group)
-    # statistics of the merged matrix, on this rank's GPU, without allocating in the library
+    # statistics of the merged matrix on this rank's GPU; the working memory
+    # comes from torch's allocator (no size limit but the device's memory)
     dt = torch.float64 if precision == 64 else torch.float32
     es_dev = torch.from_numpy(np.ascontiguousarray(es)).to(device="cuda", dtype=dt)
     st_dev = torch.empty(5 * d.num_sets, dtype=dt, device="cuda")
-    N.check(N.lib().gsea_stats_device_noalloc(ctypes.c_void_p(es_dev.data_ptr()), d.num_sets, num_perms,
-                                              precision, ctypes.c_void_p(st_dev.data_ptr()),
-                                              ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    L = N.lib()
+    need = ctypes.c_size_t(0)
+    N.check(L.gsea_stats_scratch_bytes(d.num_sets, num_perms, precision, ctypes.byref(need)))
+    scratch = torch.empty(need.value, dtype=torch.uint8, device="cuda")
+    N.check(L.gsea_stats_device(ctypes.c_void_p(es_dev.data_ptr()), d.num_sets, num_perms, precision,
+                                ctypes.c_void_p(st_dev.data_ptr()), ctypes.c_void_p(scratch.data_ptr()),
+                                need.value, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
     return es, st_dev.cpu().numpy()
 
 

@@ -239,16 +239,33 @@ typedef enum {
 int gsea_plan_set_profiling(gsea_plan plan, int on);
 int gsea_plan_stage_times(gsea_plan plan, double* ms /* [GSEA_NUM_STAGES] */);
 
+/* Final statistics of a device ES matrix [K][P] (row-major, permutation 0 =
+ * observed) into a device buffer of 5*K values with the caller's own working
+ * memory: the statistics stage of a plan, on any device matrix (e.g. the
+ * columns of a sharded run gathered on one rank).  Replaces the host-side
+ * final_statistics (src/include/statistics.cuh:46-117).
+ * gsea_stats_scratch_bytes gives the bytes of `scratch` (256-byte aligned,
+ * contents need not be cleared) that gsea_stats_device needs; the library
+ * allocates nothing.  `stream` a cudaStream_t (NULL = default); asynchronous. */
+int gsea_stats_scratch_bytes(int64_t num_sets, int64_t num_perms, int precision, size_t* bytes);
+int gsea_stats_device(const void* es, int64_t num_sets, int64_t num_perms, int precision, void* stats,
+                      void* scratch, size_t scratch_bytes, void* stream);
+
 /* Final statistics of a device ES matrix [K][P] into a device buffer of 5*K
  * values, allocating no device memory at all.  No counterpart in the
  * reference.  For hosts that cannot let a library allocate (an application
  * that gives all device memory to its own pool, or a loop that must not call
  * cudaMalloc/cudaFree because they can synchronise the device).  The working
  * memory is a fixed 4 MiB array inside the library, held by every GPU that
- * loads it; sizes whose scratch (sizeof(T)*(3K+2P) + 8*(4K+12) + 320 bytes)
- * exceeds it are rejected with GSEA_ERR_INVALID_ARGUMENT.  The first call on
- * a device looks the array up for that device (make it before any stream
- * capture); calls share the array, so calls that overlap on the GPU race.
+ * loads it; sizes whose scratch exceeds it are rejected with
+ * GSEA_ERR_INVALID_ARGUMENT.  The scratch is sizeof(T)*(3K+2P) + 8*(4K+12)
+ * + 320 bytes, plus the FDR histogram's per-block rows (up to 1 MiB:
+ * floor(2^20 / (4W)) * 4W + 16 bytes, W = 2K + 6) when K <= 6,142 (fp32) /
+ * 4,095 (fp64); gsea_stats_scratch_bytes gives the exact figure.  The first
+ * call on a device -- and the first after that device's context was reset
+ * and re-created -- looks the array up for the current context (make it
+ * before any stream capture); calls share the array, so calls that overlap
+ * on the GPU race.
  * `stream` is a cudaStream_t (NULL = default stream); asynchronous.        */
 int gsea_stats_device_noalloc(const void* es, int64_t num_sets, int64_t num_perms, int precision,
                               void* stats, void* stream);

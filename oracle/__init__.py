@@ -62,15 +62,40 @@ def build(force: bool = False) -> str:
     return ORACLE_SO
 
 
-def build_ref(reference_root: str = "/root/reference") -> Optional[str]:
-    """Build the reference's CPU stages when its sources are present."""
-    if not os.path.isdir(os.path.join(reference_root, "cudaGSEA", "src")):
+STAGED_REF = os.path.join(os.path.dirname(HERE), "baseline", "_ref")
+
+
+def stage_ref() -> None:
+    """Stage the reference's CPU-path sources into baseline/_ref/ (git-ignored)
+    where they exist on this machine, so that they travel to the GPU host and
+    build_ref() can compile them there (oracle/stage_ref.sh)."""
+    subprocess.check_call(["bash", os.path.join(HERE, "stage_ref.sh")])
+
+
+def _ref_root(reference_root: Optional[str]) -> Optional[str]:
+    for root in (reference_root, os.environ.get("GSEA_REFERENCE_ROOT"), STAGED_REF):
+        if root and os.path.isdir(os.path.join(root, "cudaGSEA", "src", "include")):
+            return root
+    return None
+
+
+def build_ref(reference_root: Optional[str] = None, wait: bool = True):
+    """Build the reference's CPU stages (oracle/build_ref.sh) from
+    `reference_root`, $GSEA_REFERENCE_ROOT or the staged copy, whichever
+    exists first; None when there are no sources.  wait=False starts the
+    build and returns its process (or REF_SO when it is up to date)."""
+    root = _ref_root(reference_root)
+    if root is None:
         return None
     script = os.path.join(HERE, "build_ref.sh")
-    if os.path.exists(REF_SO) and os.path.getmtime(REF_SO) >= max(
+    if ref_available() and os.path.getmtime(REF_SO) >= max(
             os.path.getmtime(script), os.path.getmtime(os.path.join(HERE, "ref_harness.cu"))):
         return REF_SO
-    subprocess.check_call(["bash", script, reference_root])
+    proc = subprocess.Popen(["bash", script, root])
+    if not wait:
+        return proc
+    if proc.wait() != 0:
+        raise subprocess.CalledProcessError(proc.returncode, script)
     return REF_SO
 
 

@@ -15,11 +15,14 @@
 #   * -ffp-contract=off keeps the host compiler from fusing multiply-adds,
 #     which is what the reference's x86-64 CPU build computes.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#   REFERENCE_ROOT defaults to $GSEA_REFERENCE_ROOT, else to the copy that
+#   oracle/stage_ref.sh staged in baseline/_ref/ (git-ignored; it travels to
+#   the GPU host, where this script then builds the reference natively).
 set -euo pipefail
-REF_ROOT="${1:-/root/reference}"
-SRC="$REF_ROOT/cudaGSEA/src"
 HERE="$(cd "$(dirname "$0")" && pwd)"
+REF_ROOT="${1:-${GSEA_REFERENCE_ROOT:-$(dirname "$HERE")/baseline/_ref}}"
+SRC="$REF_ROOT/cudaGSEA/src"
 OUT="$HERE/_ref"
 if [ ! -d "$SRC/include" ]; then
   echo "reference sources not found under $SRC" >&2
@@ -42,9 +45,10 @@ ARCH="-gencode arch=compute_103a,code=sm_103a"
 HOSTFLAGS="-fopenmp -ffp-contract=off -fPIC -w"
 QUIET="-diag-suppress 174,177,550,20012"
 
-# 1) harness library (stage functions)
+# 1) harness library (stage functions), built beside the CLI below
 nvcc -O3 -std=c++17 $QUIET $ARCH -I"$STAGE" -Xcompiler "$HOSTFLAGS" -shared \
-     -o "$OUT/libgsea_ref.so" "$HERE/ref_harness.cu" -lgomp
+     -o "$OUT/libgsea_ref.so.tmp$$" "$HERE/ref_harness.cu" -lgomp &
+HARNESS=$!
 
 # 2) the reference CLI, CPU mode usable without a GPU
 cat > "$STAGE/shim.cu" <<'EOF'
@@ -58,5 +62,8 @@ cat > "$STAGE/shim.cu" <<'EOF'
 #include "cudaGSEA.cu"
 EOF
 nvcc -O3 -std=c++17 $QUIET $ARCH -I"$STAGE" -Xcompiler "-fopenmp -ffp-contract=off -w -DCUDA_GSEA_OPENMP_ENABLED" \
-     -o "$OUT/cudaGSEA_cpu" "$STAGE/shim.cu" -lgomp
+     -o "$OUT/cudaGSEA_cpu.tmp$$" "$STAGE/shim.cu" -lgomp
+wait "$HARNESS"
+mv "$OUT/libgsea_ref.so.tmp$$" "$OUT/libgsea_ref.so"
+mv "$OUT/cudaGSEA_cpu.tmp$$" "$OUT/cudaGSEA_cpu"
 echo "built $OUT/libgsea_ref.so $OUT/cudaGSEA_cpu"

@@ -249,32 +249,51 @@ def test_injected_launch_failure_keeps_context(gpu, monkeypatch):
     np.testing.assert_array_equal(es, es2)
 
 
-def test_full_size_properties(gpu):
-    """20,000 x 200, 1,000 sets, 1,000 permutations (fp32): size-independent checks."""
+@pytest.mark.parametrize("double", [False, True], ids=["f32", "f64"])
+@pytest.mark.parametrize("metric", range(14), ids=api.METRICS)
+def test_full_size_properties(gpu, metric, double):
+    """20,000 x 200, 1,000 sets, 1,000 permutations, every metric in fp32 and
+    fp64: size-independent checks (finite |ES| <= 1, statistics bit-identical
+    to the oracle's for the GPU's ES) and spot permutations against the
+    oracle (keys bit-exact -- log2 metrics <= 2 ulp --, order equal to the
+    oracle's stable order of the GPU's keys, ES within tolerance).  The
+    packed metric unroll at 200 samples, the register sort at 20,000 genes
+    (fp32) / the tiled sort (fp64) and the 32-warp enrichment staging all run
+    at this size."""
+    from cudagsea_gb300.precision_check import _DeviceRows
     d = synthetic.full()
-    plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, d.num_perms, "twopass_signal2noise")
+    dt = np.float64 if double else np.float32
+    plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, d.num_perms, metric, precision=64 if double else 32,
+                    perm_batch=d.num_perms)
     plan.set_debug(True)
     plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
     plan.execute()
     es, st = plan.read()
     assert np.isfinite(es).all() and (np.abs(es) <= 1.0 + 1e-6).all()
-    keys = plan.read_buffer(N.BUF_KEYS, np.float32, (plan.perm_batch, d.num_genes))
-    order = plan.read_buffer(N.BUF_ORDER, np.uint32, (plan.perm_batch, d.num_genes))
-    # spot-check permutations against the oracle: keys, order, ES
+    keys = _DeviceRows(plan, N.BUF_KEYS, dt, d.num_genes)
+    order = _DeviceRows(plan, N.BUF_ORDER, np.uint32, d.num_genes)
     perms = [0, 1, 499, d.num_perms - 1]
-    for p in perms:
-        k1 = oracle.metric(8, d.exprs, d.labels, 1, shift=p)
-        np.testing.assert_array_equal(keys[p], k1[0])
-        sk, o = oracle.sort(k1)
-        np.testing.assert_array_equal(order[p], o[0])
+    kg, og = keys.rows(perms), order.rows(perms)
+    x = d.exprs.astype(np.float64) if double else d.exprs
+    for i, p in enumerate(perms):
+        k1 = oracle.metric(metric, x, d.labels, 1, shift=p, double=double)
+        if metric in H.LOG_METRICS:
+            assert H.ulp_diff(kg[i], k1[0]).max() <= 2, p
+        else:
+            np.testing.assert_array_equal(kg[i].view(np.uint8), k1[0].view(np.uint8), err_msg=str(p))
+        sk, o = oracle.sort(kg[i:i + 1])
+        np.testing.assert_array_equal(og[i], o[0])
         e1 = oracle.es(sk, o, d.set_offsets, d.set_genes)
-        assert H.es_close(es[:, p], e1[:, 0], False).all()
+        assert H.es_close(es[:, p], e1[:, 0], double).all(), p
     np.testing.assert_array_equal(oracle.stats(es).view(np.uint8), st.view(np.uint8))
-    # a sharded plan reproduces the columns
-    tail = api.Plan(d.num_genes, d.num_samples, d.num_sets, 100, "twopass_signal2noise", perm_offset=900)
-    tail.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
-    tail.execute()
-    np.testing.assert_array_equal(tail.read()[0], es[:, 900:])
+    plan.close()
+    if metric == 8 and not double:
+        # a sharded plan reproduces the columns
+        tail = api.Plan(d.num_genes, d.num_samples, d.num_sets, 100, metric, perm_offset=900)
+        tail.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+        tail.execute()
+        np.testing.assert_array_equal(tail.read()[0], es[:, 900:])
+        tail.close()
 
 
 @pytest.mark.parametrize("value", [np.inf, -np.inf, np.nan, 3e18], ids=["inf", "-inf", "nan", "huge"])
@@ -403,3 +422,61 @@ def test_shard_partial_statistics_on_device(gpu, precision, shards):
     st = ops.finish(head, P, counts, hist).cpu().numpy()
     u = np.uint64 if precision == 64 else np.uint32
     assert np.array_equal(st.view(u), st_ref.view(u))
+
+
+def test_run_sharded_statistics_beyond_fixed_scratch(gpu):
+    """The gather driver computes the merged statistics with torch-allocated
+    scratch (gsea_stats_device): a size whose statistics need more than the
+    allocation-free entry point's fixed 4 MiB (20 sets x 600,000
+    permutations in fp32: ~4.8 MB) goes through and equals a single plan's
+    statistics bit for bit."""
+    import ctypes
+    import socket
+    import torch.distributed as dist
+    from cudagsea_gb300.shard import run_sharded
+    d = synthetic.make(300, 12, 20, 600_000, seed=31, n_class_b=6, set_min=5, set_max=60)
+    need = ctypes.c_size_t(0)
+    N.check(N.lib().gsea_stats_scratch_bytes(d.num_sets, d.num_perms, 32, ctypes.byref(need)))
+    assert need.value > 4 << 20
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=0, world_size=1)
+    try:
+        es, st = run_sharded(d, d.num_perms)
+    finally:
+        dist.destroy_process_group()
+    plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, d.num_perms, "twopass_signal2noise")
+    plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+    plan.execute()
+    es2, st2 = plan.read()
+    plan.close()
+    np.testing.assert_array_equal(es, es2)
+    np.testing.assert_array_equal(st.view(np.uint32), st2.view(np.uint32))
+
+
+def test_null_distribution_compliance_at_reference_scale(gpu):
+    """The reference's compliance scale: 2^20 permutations of the 2,000 x 40
+    workload, 50 sets.  fp32 against fp64 nulls: every set's KS distance far
+    below the 1% critical distance; the GPU's fp32 scores against the oracle
+    (the reference's arithmetic) on 2,048 columns at each end of the range."""
+    from cudagsea_gb300 import compliance
+    P = 1 << 20
+    d = synthetic.small(num_perms=P)
+    runs = {}
+    for prec in (32, 64):
+        plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, P, "twopass_signal2noise", precision=prec)
+        plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+        plan.execute()
+        runs[prec] = plan.read(stats=False)[0]
+        plan.close()
+    crit = compliance.critical_value(P - 1, P - 1)
+    dist = compliance.null_distances(runs[32], runs[64])
+    assert dist.max() < 0.1 * crit, (dist.max(), crit)
+    n = 2048
+    for s in (0, P - n):
+        k1 = oracle.metric(8, d.exprs, d.labels, n, shift=s)
+        sk, o = oracle.sort(k1)
+        e1 = oracle.es(sk, o, d.set_offsets, d.set_genes)
+        assert H.es_close(runs[32][:, s:s + n], e1, False).all(), s
