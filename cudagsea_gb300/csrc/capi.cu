@@ -493,6 +493,10 @@ int gsea_plan_create(const gsea_config* cfg, gsea_plan* out) {
     const size_t per_perm = (size_t)G * (2 * p->tsize + (p->ranks16 ? 2 : 4)) + 4 * (size_t)p->words;
     int64_t pb = cfg->perm_batch > 0 ? cfg->perm_batch : (int64_t)(kBatchBudget / per_perm);
     if (pb < 1) pb = 1;
+    // the metric kernels' second grid dimension is one block per 4 or 8
+    // permutations of a batch and may not exceed 65,535
+    constexpr int64_t kMaxBatch = (int64_t)4 * 65535;
+    if (pb > kMaxBatch) pb = kMaxBatch;
     if (pb > P) pb = P;
     p->pb = pb;
     e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);

@@ -85,7 +85,7 @@ typedef struct {
     int32_t ascending;     /* 0 = descending ranking (reference default), 1 = ascending */
     int32_t form;          /* gsea_form */
     int64_t perm_offset;   /* global index of this plan's first permutation (sharding) */
-    int64_t perm_batch;    /* permutations per device batch, 0 = automatic */
+    int64_t perm_batch;    /* permutations per device batch (at most 262,140), 0 = automatic */
     uint32_t seed;         /* permutation seed, 42 in the reference (configuration.cuh:29) */
     int32_t device;        /* CUDA device ordinal, -1 = current device */
 } gsea_config;
@@ -280,11 +280,11 @@ typedef struct gsea_tuning {
                              automatic choice) or 256 (one CTA per SM) */
     int32_t sort_variant; /* 1 register radix sort (fp32, G <= 40,960: one CTA up to 20,480, a two-CTA
                              cluster exchanging through distributed shared memory beyond), 2 tiled */
-    int32_t es_warps;     /* warps per CTA of the enrichment kernel: 8, 16, 24 or 32 (24: with
-                             es_stage 2 or 3 only) */
+    int32_t es_warps;     /* warps per CTA of the enrichment kernel: 8, 16, 24 or 32 (24: from 8,193
+                             genes) */
     int32_t es_stage;     /* 1 stage the permutation's ranks and weights in shared memory, 2 its ranks
-                             only, 3 its weights only (2 and 3: 24-64 bitmap words per lane,
-                             20,481-65,536 genes), 0 read it from L2, -1 automatic */
+                             only, 3 its weights only (2 and 3: 12-64 bitmap words per lane,
+                             8,193-65,536 genes), 0 read it from L2, -1 automatic */
 } gsea_tuning;
 /* all automatic */
 void gsea_tuning_init(gsea_tuning* t);
