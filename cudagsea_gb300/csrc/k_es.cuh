@@ -119,94 +119,9 @@ __device__ __forceinline__ void consider(T val, int pos, T& best, int& bpos) {
     }
 }
 
-// Sets of at most kListMax distinct members (bitmap classes of up to 32 words
-// per lane, G <= 32,768) take the list procedure; each warp then owns
-// kListMax 16-bit list slots behind its bitmap.
-constexpr int kListMax = 512;
-__host__ __device__ constexpr int es_list_words(int wpl) { return (wpl > 0 && wpl <= 32) ? kListMax / 2 : 0; }
-
 // ---------------------------------------------------------------------------
 // Per-set procedures.  Both run on one warp with the set's member ranks marked
 // in the warp's bitmap `bm` (G bits) and leave the bitmap all zero.
-
-// the warp's largest-magnitude candidate, earliest position on ties (the
-// lanes' shifted extrema and the end of the list on lane 31)
-template <class T>
-__device__ __forceinline__ T warp_winner(T mx, int pmx, T mn, int pmn, const Acc<T>& Wl, bool shifted, int n,
-                                         T inv, T d, const Acc<T>& Wt, int G, int lane) {
-    Acc<T> W_incl = Wl;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const Acc<T> y = W_incl.shfl_up(o);
-        if (lane >= o) W_incl.merge(y);
-    }
-    const Acc<T> W_pre = W_incl.shfl_up(1);  // weight of the hits before this lane's
-    const T shift = shifted ? W_pre.scaled_plus(inv, T(0)) : T(0);
-    mx += shift;
-    mn += shift;
-    if (lane == 31) {  // end of the list, after the trailing misses
-        const T tail = -(T)(G - n) * d;
-        const T end = n > 0 ? Wt.scaled_plus(inv, tail) : tail;
-        if (end < mn) { mn = end; pmn = G - 1; }
-    }
-    // the largest value is always just after a hit and the smallest just
-    // before one (or at the end): only a positive maximum and a negative
-    // minimum are candidates
-    T best = T(0);
-    int bpos = -1;
-    if (pmx >= 0 && mx > T(0)) consider<T>(mx, pmx, best, bpos);
-    if (pmn >= 0 && mn < T(0)) consider<T>(mn, pmn, best, bpos);
-#pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) {
-        const T ob = __shfl_xor_sync(kFullMask, best, o);
-        const int op = __shfl_xor_sync(kFullMask, bpos, o);
-        consider<T>(ob, op, best, bpos);
-    }
-    return best;
-}
-
-// List procedure (n <= kListMax hits, after the direct procedure's scan):
-// every lane copies its hits' ranks, in rank order, into the warp's list
-// (list[excl + t], clearing the bitmap words as it reads them), then the
-// list is cut into 32 equal contiguous chunks -- one per lane, whatever the
-// lanes' word ranges held -- and each lane walks its chunk with a
-// lane-local compensated prefix, as the direct procedure walks its words.
-// The walk is balanced (ceil(n/32) steps) and holds no bit search.
-template <class T, int WPL, class Mask>
-__device__ __forceinline__ T set_score_list(uint32_t* bm, int w0, int cnt, Mask nzm, int excl, int n, T inv, T d,
-                                            const T* wt, int G, int lane, const Acc<T>& Wt) {
-    uint16_t* list = reinterpret_cast<uint16_t*>(bm + WPL * 32);
-    uint32_t cur = 0u;
-    int wi = 0;
-    for (int t = 0; t < cnt; t++) {
-        if (cur == 0u) {  // next nonzero word of the lane
-            wi = (WPL > 32 ? __ffsll((long long)nzm) : __ffs((int)nzm)) - 1;
-            nzm &= nzm - 1;
-            cur = bm[w0 + wi];
-            bm[w0 + wi] = 0u;
-        }
-        const int bit = __ffs(cur) - 1;
-        cur &= cur - 1;
-        list[excl + t] = (uint16_t)(((w0 + wi) << 5) + bit);
-    }
-    __syncwarp();
-    const int c = (n + 31) >> 5;
-    const int lo = min(lane * c, n), hi = min(lo + c, n);
-    Acc<T> Wl;
-    T mx = -CUDART_INF, mn = CUDART_INF;
-    int pmx = -1, pmn = -1;
-    for (int t = lo; t < hi; t++) {
-        const int r = list[t];
-        const T md = -(T)(r - t) * d;  // misses before this hit, times the decay
-        const T before = t > lo ? Wl.scaled_plus(inv, md) : md;
-        Wl.add(wt[r]);
-        const T after = Wl.scaled_plus(inv, md);
-        if (before < mn) { mn = before; pmn = r - 1; }
-        if (after > mx) { mx = after; pmx = r; }
-    }
-    __syncwarp();  // the list is read before the next set writes it
-    return warp_winner<T>(mx, pmx, mn, pmn, Wl, lo > 0, n, inv, d, Wt, G, lane);
-}
 
 // Direct procedure (G <= 1024*WPL): the lane's bitmap words (WPL, a multiple
 // of 4, loaded as 16-byte vectors) give its hit count and a mask of its
@@ -242,10 +157,6 @@ __device__ __forceinline__ T set_score_direct(uint32_t* bm, int w0, const T* wt,
     const int excl = incl - cnt;  // hits in the lanes before
     const T inv = n > 0 ? T(1) / Wt.value() : T(0);
     const T d = decay[n];
-    if constexpr (es_list_words(WPL) > 0) {
-        if (n <= kListMax)  // warp-uniform
-            return set_score_list<T, WPL, Mask>(bm, w0, cnt, nzm, excl, n, inv, d, wt, G, lane, Wt);
-    }
     Acc<T> Wl;  // weight of this lane's hits so far
     T mx = -CUDART_INF, mn = CUDART_INF;
     int pmx = -1, pmn = -1;
@@ -268,7 +179,35 @@ __device__ __forceinline__ T set_score_direct(uint32_t* bm, int w0, const T* wt,
         if (before < mn) { mn = before; pmn = r - 1; }
         if (after > mx) { mx = after; pmx = r; }
     }
-    return warp_winner<T>(mx, pmx, mn, pmn, Wl, excl > 0, n, inv, d, Wt, G, lane);
+    Acc<T> W_incl = Wl;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const Acc<T> y = W_incl.shfl_up(o);
+        if (lane >= o) W_incl.merge(y);
+    }
+    const Acc<T> W_pre = W_incl.shfl_up(1);  // weight of the hits before this lane's
+    const T shift = excl > 0 ? W_pre.scaled_plus(inv, T(0)) : T(0);
+    mx += shift;
+    mn += shift;
+    if (lane == 31) {  // end of the list, after the trailing misses
+        const T tail = -(T)(G - n) * d;
+        const T end = n > 0 ? Wt.scaled_plus(inv, tail) : tail;
+        if (end < mn) { mn = end; pmn = G - 1; }
+    }
+    // the largest value is always just after a hit and the smallest just
+    // before one (or at the end): only a positive maximum and a negative
+    // minimum are candidates
+    T best = T(0);
+    int bpos = -1;
+    if (pmx >= 0 && mx > T(0)) consider<T>(mx, pmx, best, bpos);
+    if (pmn >= 0 && mn < T(0)) consider<T>(mn, pmn, best, bpos);
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        const T ob = __shfl_xor_sync(kFullMask, best, o);
+        const int op = __shfl_xor_sync(kFullMask, bpos, o);
+        consider<T>(ob, op, best, bpos);
+    }
+    return best;
 }
 
 // General procedure (any G, any set size): each lane walks its own word range
@@ -452,7 +391,7 @@ es_kernel(const RankT* __restrict__ ranks, const T* __restrict__ sorted_abs, int
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int next_set;
     const int words = (G + 31) >> 5;
-    const int region = WPL > 0 ? WPL * 32 + es_list_words(WPL) : words;  // per-warp bitmap (+ list) words
+    const int region = WPL > 0 ? WPL * 32 : words;  // per-warp bitmap words
     T* s_w;
     RankT* s_rank;
     uint32_t* bm;
@@ -505,7 +444,7 @@ es_batch_kernel(const EsTask<T>* __restrict__ tasks, const int64_t* __restrict__
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int next_set;
     __shared__ long long s_item;
-    const int region = WPL > 0 ? WPL * 32 + es_list_words(WPL) : (Gmax + 31) >> 5;
+    const int region = WPL > 0 ? WPL * 32 : (Gmax + 31) >> 5;
     T* s_w;
     RankT* s_rank;
     uint32_t* bm;
@@ -531,9 +470,8 @@ es_batch_kernel(const EsTask<T>* __restrict__ tasks, const int64_t* __restrict__
     }
 }
 
-// words of a warp's region: WPL*32 bitmap words (+ the list slots) for the
-// register procedures, one bit per gene for the general one
-inline int es_region_words(int G, int wpl) { return wpl > 0 ? wpl * 32 + es_list_words(wpl) : (G + 31) >> 5; }
+// words of a warp's bitmap region: WPL*32 for the register procedure
+inline int es_region_words(int G, int wpl) { return wpl > 0 ? wpl * 32 : (G + 31) >> 5; }
 
 inline int es_wpl(int G, bool ranks16) {
     const int need = (((G + 31) >> 5) + 31) >> 5;
@@ -578,11 +516,8 @@ cudaError_t launch_es_w(const RankT* ranks, const T* sorted_abs, int G, int P, c
         if (STAGE >= 2) return cudaErrorInvalidValue;
         return launch_es_v<T, RankT, WARPS, STAGE, 0>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride,
                                                       col0, grid, st);
-    } else if constexpr (STAGE >= 2 || WARPS == 24) {  // partial staging / 24 warps: the classes from 8,193 genes
+    } else if constexpr (STAGE >= 2 || WARPS == 24) {  // partial staging / 24 warps: the large-G classes
         switch (es_wpl(G, true)) {
-            case 12: return launch_es_v<T, RankT, WARPS, STAGE, 12>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-            case 16: return launch_es_v<T, RankT, WARPS, STAGE, 16>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-            case 20: return launch_es_v<T, RankT, WARPS, STAGE, 20>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
             case 24: return launch_es_v<T, RankT, WARPS, STAGE, 24>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
             case 32: return launch_es_v<T, RankT, WARPS, STAGE, 32>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
             case 40: return launch_es_v<T, RankT, WARPS, STAGE, 40>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
@@ -628,14 +563,11 @@ cudaError_t launch_es_t(const RankT* ranks, const T* sorted_abs, int G, int P, c
     // candidates in the automatic order: 32 warps first (staging ranks and
     // weights, then weights only, 24 warps with weights only, 32 with ranks
     // only, 32 with none), then fewer warps -- warps count for more than
-    // staging (measured on 24,000-40,000 genes); the partial stagings and 24
-    // warps are for the classes of 12-64 bitmap words per lane (8,193-65,536
-    // genes), where the bitmaps and list slots of 32 warps leave no room to
-    // stage both
+    // staging (measured on 24,000-40,000 genes); the partial stagings are for
+    // the large-G classes (24-64 bitmap words per lane)
     struct Cand { int warps; int stage; size_t smem; };
     const Cand cands[] = {{32, 1, es_smem_bytes<T, RankT, 32, 1>(G)},
                           {32, 3, es_smem_bytes<T, RankT, 32, 3>(G)},
-                          {24, 1, es_smem_bytes<T, RankT, 24, 1>(G)},
                           {24, 3, es_smem_bytes<T, RankT, 24, 3>(G)},
                           {32, 2, es_smem_bytes<T, RankT, 32, 2>(G)},
                           {32, 0, es_smem_bytes<T, RankT, 32, 0>(G)},
@@ -649,14 +581,13 @@ cudaError_t launch_es_t(const RankT* ranks, const T* sorted_abs, int G, int P, c
     const int wpl = es_wpl(G, sizeof(RankT) == 2);
     for (const Cand& c : cands) {
         if (c.smem > cap) continue;
-        if ((c.stage >= 2 || c.warps == 24) && wpl < 12) continue;
+        if ((c.stage >= 2 || c.warps == 24) && wpl < 24) continue;
         if (c.stage == 1 && wpl >= 40) continue;
         if (tune.warps && tune.warps != c.warps) continue;
         if (tune.stage >= 0 && tune.stage != c.stage) continue;
 #define GSEA_ES(W, S) \
     return launch_es_w<T, RankT, W, S>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st)
         if (c.warps == 32 && c.stage == 1) GSEA_ES(32, 1);
-        if (c.warps == 24 && c.stage == 1) GSEA_ES(24, 1);
         if (c.warps == 16 && c.stage == 1) GSEA_ES(16, 1);
         if (c.warps == 8 && c.stage == 1) GSEA_ES(8, 1);
         if (c.warps == 32 && c.stage == 3) GSEA_ES(32, 3);
@@ -700,9 +631,6 @@ cudaError_t launch_es_batch_w(const EsTask<T>* tasks, const int64_t* item_end, i
                               unsigned long long* counter, int Gmax, int wpl, cudaStream_t st) {
     if constexpr (STAGE >= 2 || WARPS == 24) {
         switch (wpl) {
-            case 12: return launch_es_batch_v<T, WARPS, STAGE, 12>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
-            case 16: return launch_es_batch_v<T, WARPS, STAGE, 16>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
-            case 20: return launch_es_batch_v<T, WARPS, STAGE, 20>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
             case 24: return launch_es_batch_v<T, WARPS, STAGE, 24>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
             case 32: return launch_es_batch_v<T, WARPS, STAGE, 32>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
             case 40: return launch_es_batch_v<T, WARPS, STAGE, 40>(tasks, item_end, ntasks, nitems, counter, Gmax, st);
@@ -748,7 +676,6 @@ cudaError_t launch_es_batch(const EsTask<T>* tasks, const int64_t* item_end, int
     struct Cand { int warps; int stage; size_t smem; };
     const Cand cands[] = {{32, 1, es_smem_bytes<T, uint16_t, 32, 1>(Gmax)},
                           {32, 3, es_smem_bytes<T, uint16_t, 32, 3>(Gmax)},
-                          {24, 1, es_smem_bytes<T, uint16_t, 24, 1>(Gmax)},
                           {24, 3, es_smem_bytes<T, uint16_t, 24, 3>(Gmax)},
                           {32, 2, es_smem_bytes<T, uint16_t, 32, 2>(Gmax)},
                           {32, 0, es_smem_bytes<T, uint16_t, 32, 0>(Gmax)},
@@ -761,13 +688,12 @@ cudaError_t launch_es_batch(const EsTask<T>* tasks, const int64_t* item_end, int
                           {8, 0, es_smem_bytes<T, uint16_t, 8, 0>(Gmax)}};
     for (const Cand& c : cands) {
         if (c.smem > cap) continue;
-        if ((c.stage >= 2 || c.warps == 24) && wpl < 12) continue;
+        if ((c.stage >= 2 || c.warps == 24) && wpl < 24) continue;
         if (c.stage == 1 && wpl >= 40) continue;
         if (tune.warps && tune.warps != c.warps) continue;
         if (tune.stage >= 0 && tune.stage != c.stage) continue;
 #define GSEA_ESB(W, S) return launch_es_batch_w<T, W, S>(tasks, item_end, ntasks, nitems, counter, Gmax, wpl, st)
         if (c.warps == 32 && c.stage == 1) GSEA_ESB(32, 1);
-        if (c.warps == 24 && c.stage == 1) GSEA_ESB(24, 1);
         if (c.warps == 16 && c.stage == 1) GSEA_ESB(16, 1);
         if (c.warps == 8 && c.stage == 1) GSEA_ESB(8, 1);
         if (c.warps == 32 && c.stage == 3) GSEA_ESB(32, 3);

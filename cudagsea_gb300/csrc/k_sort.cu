@@ -17,8 +17,10 @@
 //                      ITEMS keys); each pass exchanges keys and gene ids
 //                      through one shared-memory buffer.  fp32, G <= 20,480.
 //   sort_cluster_kernel the same over a cluster of two CTAs (SMs), the
-//                      exchange through distributed shared memory.  fp32,
-//                      20,480 < G <= 40,960.
+//                      exchange through distributed shared memory: fp32,
+//                      20,480 < G <= 40,960; fp64 (keys and gene ids
+//                      exchanged separately), one CTA up to 10,240 genes,
+//                      two up to 20,480.
 //   sort_tiled_kernel  any key width and any G: the segment ping-pongs
 //                      between two per-CTA global (L2-resident) buffers and
 //                      each pass streams it in tiles of 4,096 items.
@@ -266,8 +268,8 @@ size_t regs_smem_bytes() {
 }
 
 // ---------------------------------------------------------------------------
-// Cluster form (fp32, 20,480 < G <= CL x 1024 x ITEMS): one cluster of CL
-// CTAs (2 or 4) per permutation, CTA r holding the items of positions
+// Cluster form (G <= CL x 1024 x ITEMS; fp32 beyond 20,480 genes, fp64 from
+// the smallest G): one cluster of CL CTAs (1 or 2) per permutation, CTA r holding the items of positions
 // [r*TILE, (r+1)*TILE) in registers as sort_regs_kernel does.  A pass ranks
 // items inside each warp as there, then the CTAs' digit totals are read
 // through distributed shared memory: an item's destination is
@@ -599,7 +601,13 @@ cudaError_t launch_cluster(const T* keys, int G, int P, bool desc, const SortBuf
     auto kern = sort_cluster_kernel<T, RankT, ITEMS, CL>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    const int groups = num_sms() / CL > 0 ? num_sms() / CL : 1;
+    int per_sm = 1;  // a one-CTA "cluster" may share its SM with another CTA
+    if (CL == 1) {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) return cudaErrorInvalidValue;
+    }
+    const int groups = num_sms() * per_sm / CL > 0 ? num_sms() * per_sm / CL : 1;
     const int clusters = P < groups ? P : groups;
     kern<<<CL * clusters, kThreads, smem, st>>>(keys, G, P, desc, static_cast<RankT*>(o.ranks),
                                                 static_cast<T*>(o.sorted_abs), o.order);
@@ -607,9 +615,25 @@ cudaError_t launch_cluster(const T* keys, int G, int P, bool desc, const SortBuf
     return cudaGetLastError();
 }
 
+// largest G of the register-resident forms (variant 1): fp32 keys and gene
+// ids as 8-byte slots, 20 per thread over two CTAs; fp64 keys 10 per thread
+// (16 spill registers at 1,024 threads)
+template <class T>
+constexpr int regs_max_genes() { return sizeof(T) == 4 ? 2 * kThreads * 20 : 2 * kThreads * 10; }
+
 template <class T, class RankT>
 cudaError_t launch_sort_t(const T* keys, int G, int P, bool desc, const SortBuffers& o, cudaStream_t st) {
-    if (o.variant == 1 && !(sizeof(T) == 4 && G <= 2 * kThreads * 20)) return cudaErrorInvalidValue;
+    if (o.variant == 1 && G > regs_max_genes<T>()) return cudaErrorInvalidValue;
+    if constexpr (sizeof(T) == 8) {
+        // fp64: the cluster form holds the segment in registers (keys and
+        // gene ids exchanged separately); one CTA up to 10,240 genes, a
+        // two-CTA cluster beyond
+        if (o.variant != 2) {
+            if (G <= kThreads * 4) return launch_cluster<T, RankT, 4, 1>(keys, G, P, desc, o, st);
+            if (G <= kThreads * 10) return launch_cluster<T, RankT, 10, 1>(keys, G, P, desc, o, st);
+            if (G <= 2 * kThreads * 10) return launch_cluster<T, RankT, 10, 2>(keys, G, P, desc, o, st);
+        }
+    }
     if constexpr (sizeof(T) == 4) {
       if (o.variant != 2) {
         if (G <= kThreads * 4) return launch_regs<T, RankT, 4>(keys, G, P, desc, o, st);

@@ -279,12 +279,13 @@ typedef struct gsea_tuning {
     int32_t chosen_tile;  /* tensor-core form: permutations per tile, 128 (two CTAs per SM, the
                              automatic choice) or 256 (one CTA per SM) */
     int32_t sort_variant; /* 1 register radix sort (fp32, G <= 40,960: one CTA up to 20,480, a two-CTA
-                             cluster exchanging through distributed shared memory beyond), 2 tiled */
-    int32_t es_warps;     /* warps per CTA of the enrichment kernel: 8, 16, 24 or 32 (24: from 8,193
-                             genes) */
+                             cluster exchanging through distributed shared memory beyond; fp64,
+                             G <= 20,480: one CTA up to 10,240, a two-CTA cluster beyond), 2 tiled */
+    int32_t es_warps;     /* warps per CTA of the enrichment kernel: 8, 16, 24 or 32 (24: with
+                             es_stage 2 or 3 only) */
     int32_t es_stage;     /* 1 stage the permutation's ranks and weights in shared memory, 2 its ranks
-                             only, 3 its weights only (2 and 3: 12-64 bitmap words per lane,
-                             8,193-65,536 genes), 0 read it from L2, -1 automatic */
+                             only, 3 its weights only (2 and 3: 24-64 bitmap words per lane,
+                             20,481-65,536 genes), 0 read it from L2, -1 automatic */
 } gsea_tuning;
 /* all automatic */
 void gsea_tuning_init(gsea_tuning* t);
