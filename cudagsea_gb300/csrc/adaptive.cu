@@ -24,6 +24,7 @@
 // from the permutations a set received.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "kernels.h"
@@ -129,6 +130,69 @@ bool prior_agrees(double pm, double w, double n, double c, double z) {
 
 namespace {
 
+// Records the whole adaptive test on `st`: the pilot over every set, the
+// decisions (kernels: stop_p, model fallback test, stopping rule, active
+// list), then every round of the fixed schedule over the sets a kernel left
+// active -- the set count is read on the device, so nothing waits for the
+// host -- and the final ragged statistics.
+template <class T>
+int record_adaptive(gsea_plan_s* p, gsea_model model, bool use_model, const gsea::AdaptiveRule& rule, bool q_on,
+                    const std::vector<std::pair<int64_t, int64_t>>& schedule, cudaStream_t st) {
+    const int K = (int)p->cfg.num_sets;
+    const int64_t P = p->cfg.num_perms, P0 = rule.P0;
+    const T* es = static_cast<const T*>(p->es);
+    T* stats = static_cast<T*>(p->stats);
+    auto* ctl = static_cast<gsea::AdaptiveCtl*>(p->ad_ctl);
+    const float* pred = use_model ? p->pred : nullptr;
+    int rc;
+    GSEA_CUDA(cudaMemsetAsync(p->exceed, 0, sizeof(unsigned long long) * K, st), "clear exceedances");
+    GSEA_CUDA(cudaMemsetAsync(p->sumabs, 0, sizeof(double) * 2 * K, st), "clear sums");
+    GSEA_CUDA(gsea::launch_adaptive_reset(K, P0, p->counts, ctl, st), "adaptive reset");
+    // pilot: every set, permutations [0, P0)
+    if ((rc = gsea::plan_run_range(p, st, 0, P0, p->set_order, K))) return rc;
+    GSEA_CUDA(gsea::launch_exceed<T>(es, P, K, nullptr, K, 0, P0, p->exceed, p->sumabs, st), "exceedance kernel");
+    GSEA_CUDA(gsea::launch_stats_ragged<T>(es, K, P, p->counts, P0, stats, p->stats_scratch, st), "pilot statistics");
+    const bool bound0 = q_on && P0 < P;
+    if (bound0)
+        GSEA_CUDA(gsea::launch_fdr_bound<T>(K, P0, stats, p->counts, p->sumabs, rule.z, p->stats_scratch, p->qlow, st),
+                  "FDR bound kernel");
+    if (use_model) {
+        GSEA_CUDA(gsea::launch_model_features<T>(es, P, p->set_off, K, p->moments, p->sumabs, P0, p->feat, st),
+                  "features");
+        if ((rc = gsea_model_predict(model, p->feat, K, p->pred, st))) return rc;
+    }
+    GSEA_CUDA(gsea::launch_adaptive_prepare<T>(K, stats, pred, p->sumabs, rule, p->ad_err, ctl, st),
+              "adaptive pilot decisions");
+    GSEA_CUDA(gsea::launch_adaptive_decide(K, nullptr, nullptr, p->counts, p->exceed, pred, p->qlow, bound0, true, rule,
+                                           p->stop, ctl, st),
+              "stopping rule");
+    GSEA_CUDA(gsea::launch_adaptive_compact(K, p->set_order, p->stop, p->active, ctl, st), "active sets");
+    for (const auto& r : schedule) {
+        const int64_t cur = r.first, next = r.second;
+        if ((rc = gsea::plan_run_range(p, st, cur, next, p->active, K, &ctl->n_active))) return rc;
+        GSEA_CUDA(gsea::launch_exceed<T>(es, P, K, p->active, K, cur, next, p->exceed, p->sumabs, st, &ctl->n_active),
+                  "exceedances");
+        GSEA_CUDA(gsea::launch_adaptive_counts(K, p->active, ctl, next, p->counts, st), "set counts");
+        const bool bound_now = q_on && next < P;
+        if (bound_now) {  // statistics at the new counts, then the bounds
+            // the stopping bound's null histogram: the pilot columns of
+            // every set (the final statistics use every score)
+            GSEA_CUDA(gsea::launch_stats_ragged<T>(es, K, P, p->counts, P0, stats, p->stats_scratch, st, P0),
+                      "round statistics");
+            GSEA_CUDA(gsea::launch_fdr_bound<T>(K, P0, stats, p->counts, p->sumabs, rule.z, p->stats_scratch, p->qlow,
+                                                st),
+                      "FDR bound kernel");
+        }
+        GSEA_CUDA(gsea::launch_adaptive_decide(K, p->active, &ctl->n_active, p->counts, p->exceed, pred, p->qlow,
+                                               bound_now, false, rule, p->stop, ctl, st),
+                  "stopping rule");
+        GSEA_CUDA(gsea::launch_adaptive_compact(K, p->set_order, p->stop, p->active, ctl, st), "active sets");
+    }
+    GSEA_CUDA(gsea::launch_stats_ragged<T>(es, K, P, p->counts, P0, stats, p->stats_scratch, st),
+              "statistics kernels");
+    return GSEA_OK;
+}
+
 template <class T>
 int execute_adaptive_t(gsea_plan_s* p, gsea_model model, const gsea_adaptive_params& ap, int64_t* counts_out,
                        gsea_adaptive_report* report) {
@@ -136,173 +200,109 @@ int execute_adaptive_t(gsea_plan_s* p, gsea_model model, const gsea_adaptive_par
     const int64_t P = p->cfg.num_perms;
     const int64_t P0 = std::min<int64_t>(std::max<int64_t>(ap.pilot_perms, 2), P);
     cudaStream_t st = p->stream;
-    const T* es = static_cast<const T*>(p->es);
     int rc = ensure_buffers(p);
     if (rc) return rc;
-    gsea::launches_take();
-    p->events_used = 0;
-    GSEA_CUDA(cudaMemsetAsync(p->exceed, 0, sizeof(unsigned long long) * K, st), "clear exceedances");
-    GSEA_CUDA(cudaMemsetAsync(p->sumabs, 0, sizeof(double) * 2 * K, st), "clear sums");
-    // pilot: every set, permutations [0, P0)
-    if ((rc = gsea::plan_run_range(p, st, 0, P0, p->set_order, K))) return rc;
-    GSEA_CUDA(gsea::launch_exceed<T>(es, P, K, nullptr, K, 0, P0, p->exceed, p->sumabs, st), "exceedance kernel");
-    std::vector<int64_t> counts((size_t)K, P0);
-    GSEA_CUDA(cudaMemcpyAsync(p->counts, counts.data(), sizeof(int64_t) * K, cudaMemcpyHostToDevice, st),
-              "copy counts");
-    GSEA_CUDA(gsea::launch_stats_ragged<T>(es, K, P, p->counts, P0, static_cast<T*>(p->stats), p->stats_scratch, st),
-              "pilot statistics");
-    // FDR rule: lower bounds of the sets' q from the statistics just computed
-    // (launched before the host synchronises, copied back with the rest)
-    const bool q_on = ap.q_margin > 0.0;
-    std::vector<float> qlow((size_t)K);
-    auto launch_bound = [&]() -> int {
-        GSEA_CUDA(gsea::launch_fdr_bound<T>(K, P0, static_cast<const T*>(p->stats), p->counts, p->sumabs, ap.z,
-                                            p->stats_scratch, p->qlow, st),
-                  "FDR bound kernel");
-        GSEA_CUDA(cudaMemcpyAsync(qlow.data(), p->qlow, sizeof(float) * K, cudaMemcpyDeviceToHost, st), "copy bounds");
-        return GSEA_OK;
-    };
-    if (q_on && P0 < P && (rc = launch_bound())) return rc;
-    std::vector<T> stats((size_t)5 * K);
-    std::vector<unsigned long long> exceed((size_t)K);
-    std::vector<double> sumabs((size_t)K);
-    GSEA_CUDA(cudaMemcpyAsync(stats.data(), p->stats, sizeof(T) * 5 * K, cudaMemcpyDeviceToHost, st), "copy stats");
-    GSEA_CUDA(cudaMemcpyAsync(exceed.data(), p->exceed, sizeof(unsigned long long) * K, cudaMemcpyDeviceToHost, st),
-              "copy exceedances");
-    GSEA_CUDA(cudaMemcpyAsync(sumabs.data(), p->sumabs, sizeof(double) * K, cudaMemcpyDeviceToHost, st), "copy sums");
-    GSEA_CUDA(cudaStreamSynchronize(st), "stream sync");
-    double pstar = 0.0;
-    for (int k = 0; k < K; k++) {
-        const double q = (double)stats[4 * (size_t)K + k], np = (double)stats[2 * (size_t)K + k];
-        if (q < ap.q_call && np > pstar) pstar = np;
-    }
-    const double stop_p = std::min(1.0, std::max(ap.p_floor, ap.margin * pstar));
-    // learned prior
-    std::vector<float> pm, prior;
-    int32_t model_used = 0;
-    double mean_err = NAN;
+    if (!p->stop && (rc = gsea::plan_dev_alloc((void**)&p->stop, (size_t)K, "stop flags"))) return rc;
+    if (!p->ad_err && (rc = gsea::plan_dev_alloc((void**)&p->ad_err, sizeof(double) * K, "model errors"))) return rc;
+    if (!p->ad_ctl && (rc = gsea::plan_dev_alloc(&p->ad_ctl, sizeof(gsea::AdaptiveCtl), "adaptive record")))
+        return rc;
+    // the learned prior: only a trained model (norms[14] set by calibration)
+    float norms[GSEA_MODEL_NORMS] = {};
+    bool use_model = false;
     if (model) {
-        float norms[GSEA_MODEL_NORMS];
         if ((rc = gsea_model_get(model, nullptr, norms))) return rc;
-        if (norms[14] != 0.f) {
-            if (!p->moments_ready) {  // a property of the inputs: computed once per upload
-                if ((rc = compute_moments<T>(p, st))) return rc;
-                p->moments_ready = true;
-            }
-            GSEA_CUDA(gsea::launch_model_features<T>(es, P, p->set_off, K, p->moments, p->sumabs, P0, p->feat, st),
-                      "features");
-            if ((rc = gsea_model_predict(model, p->feat, K, p->pred, st))) return rc;
-            std::vector<float> pred((size_t)2 * K);
-            GSEA_CUDA(cudaMemcpyAsync(pred.data(), p->pred, sizeof(float) * 2 * K, cudaMemcpyDeviceToHost, st),
-                      "copy predictions");
-            GSEA_CUDA(cudaStreamSynchronize(st), "stream sync");
-            std::vector<double> errs;
-            for (int k = 0; k < K; k++) {
-                const double mt = pred[2 * (size_t)k + 1], mh = sumabs[k] / (double)P0;
-                if (std::isfinite(mt) && mt > 0 && std::isfinite(mh) && mh > 0) errs.push_back(std::fabs(std::log(mt / mh)));
-            }
-            mean_err = median(errs);
-            if (mean_err <= ap.fallback_tol) {
-                model_used = 1;
-                const double s2 = (double)norms[12] * (double)norms[12];
-                const double cap = ap.prior_cap * (double)P0;
-                pm.resize((size_t)K);
-                prior.resize((size_t)K);
-                for (int k = 0; k < K; k++) {
-                    const double v = std::min(std::max((double)pred[2 * (size_t)k], 1e-6), 1.0 - 1e-6);
-                    pm[k] = (float)v;
-                    prior[k] = (float)std::min(1.0 / (s2 * v * (1.0 - v)), cap);
-                }
-            }
-        }
+        use_model = norms[14] != 0.f;
     }
-    std::vector<int64_t> ex64((size_t)K);
-    std::vector<uint8_t> stop((size_t)K), now((size_t)K);
-    auto decide = [&](std::vector<uint8_t>& out) {
-        for (int k = 0; k < K; k++) ex64[k] = (int64_t)exceed[k];
-        return gsea_adaptive_decide(K, counts.data(), ex64.data(), model_used ? pm.data() : nullptr,
-                                    model_used ? prior.data() : nullptr, stop_p, ap.z, out.data());
-    };
-    if ((rc = decide(stop))) return rc;
-    int64_t stopped_q = 0;
-    const double q_stop = ap.q_margin * ap.q_call;
-    auto apply_bound = [&](std::vector<uint8_t>& st_out) {  // after the synchronisation that brought qlow
-        for (int k = 0; k < K; k++)
-            if (!st_out[k] && counts[k] < P && (double)qlow[k] >= q_stop) {
-                st_out[k] = 1;
-                stopped_q++;
-            }
-    };
-    if (q_on && P0 < P) apply_bound(stop);
-    int64_t prior_sets = 0, prior_agreed = 0;
-    if (model_used) {
-        for (int k = 0; k < K; k++) {
-            if (!(std::isfinite(pm[k]) && std::isfinite(prior[k]) && prior[k] > 0)) continue;
-            prior_sets++;
-            const double v = std::min(std::max((double)pm[k], 1e-6), 1.0 - 1e-6);
-            prior_agreed += gsea::prior_agrees(v, prior[k], (double)P0, (double)exceed[k], ap.z) ? 1 : 0;
-        }
+    if (use_model && !p->moments_ready) {  // a property of the inputs: computed once per upload
+        if ((rc = compute_moments<T>(p, st))) return rc;
+        p->moments_ready = true;
     }
-    int64_t stopped_pilot = 0;
-    for (int k = 0; k < K; k++) stopped_pilot += stop[k];
-    int64_t cur = P0, rounds = 1;
-    std::vector<int32_t> active;
-    active.reserve((size_t)K);
-    while (cur < P) {
+    gsea::AdaptiveRule rule;
+    rule.q_call = ap.q_call;
+    rule.margin = ap.margin;
+    rule.p_floor = ap.p_floor;
+    rule.z = ap.z;
+    rule.q_stop = ap.q_margin * ap.q_call;
+    rule.tol = ap.fallback_tol;
+    rule.cap = ap.prior_cap * (double)P0;
+    rule.s2 = (double)norms[12] * (double)norms[12];
+    rule.P = P;
+    rule.P0 = P0;
+    const bool q_on = ap.q_margin > 0.0;
+    std::vector<std::pair<int64_t, int64_t>> schedule;
+    for (int64_t cur = P0; cur < P;) {
         const int64_t next = std::min<int64_t>(P, std::max<int64_t>(cur + 1, (int64_t)std::ceil((double)cur * ap.growth)));
-        active.clear();
-        for (int32_t k : p->h_set_order)
-            if (!stop[k]) active.push_back(k);
-        if (active.empty()) break;
-        const int n = (int)active.size();
-        GSEA_CUDA(cudaMemcpyAsync(p->active, active.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st),
-                  "copy active sets");
-        if ((rc = gsea::plan_run_range(p, st, cur, next, p->active, n))) return rc;
-        GSEA_CUDA(gsea::launch_exceed<T>(es, P, K, p->active, n, cur, next, p->exceed, p->sumabs, st), "exceedances");
-        for (int32_t k : active) counts[k] = next;
-        const bool bound_now = q_on && next < P;
-        if (bound_now) {  // statistics at the new counts, then the bounds: one synchronisation per round
-            GSEA_CUDA(cudaMemcpyAsync(p->counts, counts.data(), sizeof(int64_t) * K, cudaMemcpyHostToDevice, st),
-                      "copy counts");
-            // the stopping bound's null histogram: the pilot columns of
-            // every set (the final statistics use every score)
-            GSEA_CUDA(gsea::launch_stats_ragged<T>(es, K, P, p->counts, P0, static_cast<T*>(p->stats),
-                                                   p->stats_scratch, st, P0),
-                      "round statistics");
-            if ((rc = launch_bound())) return rc;
-        }
-        GSEA_CUDA(cudaMemcpyAsync(exceed.data(), p->exceed, sizeof(unsigned long long) * K, cudaMemcpyDeviceToHost, st),
-                  "copy exceedances");
-        GSEA_CUDA(cudaStreamSynchronize(st), "stream sync");
-        if ((rc = decide(now))) return rc;
-        for (int32_t k : active) stop[k] = now[k];
-        if (bound_now) apply_bound(stop);
+        schedule.emplace_back(cur, next);
         cur = next;
-        rounds++;
     }
-    GSEA_CUDA(cudaMemcpyAsync(p->counts, counts.data(), sizeof(int64_t) * K, cudaMemcpyHostToDevice, st),
+    // what a captured graph was recorded for: the parameters and the model
+    std::vector<unsigned char> key(sizeof(ap) + sizeof(model) + sizeof(norms) + 1);
+    std::memcpy(key.data(), &ap, sizeof(ap));
+    std::memcpy(key.data() + sizeof(ap), &model, sizeof(model));
+    std::memcpy(key.data() + sizeof(ap) + sizeof(model), norms, sizeof(norms));
+    key.back() = use_model ? 1 : 0;
+    gsea::launches_take();
+    int64_t launches = 0;
+    if (p->profile) {  // stage events between the launches: issued one by one
+        p->events_used = 0;
+        if ((rc = record_adaptive<T>(p, model, use_model, rule, q_on, schedule, st))) return rc;
+        launches = gsea::launches_take();
+    } else {
+        if (!p->ad_exec || p->ad_key != key) {
+            if (p->ad_exec) cudaGraphExecDestroy(p->ad_exec);
+            if (p->ad_graph) cudaGraphDestroy(p->ad_graph);
+            p->ad_exec = nullptr;
+            p->ad_graph = nullptr;
+            GSEA_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+            rc = record_adaptive<T>(p, model, use_model, rule, q_on, schedule, st);
+            cudaGraph_t g = nullptr;
+            const cudaError_t e = cudaStreamEndCapture(st, &g);
+            if (rc) {
+                if (g) cudaGraphDestroy(g);
+                cudaGetLastError();
+                return rc;
+            }
+            GSEA_CUDA(e, "end capture");
+            p->ad_graph = g;
+            p->ad_launches = gsea::launches_take();
+            GSEA_CUDA(cudaGraphInstantiate(&p->ad_exec, g, 0), "graph instantiate");
+            p->ad_key = key;
+        }
+        GSEA_CUDA(cudaGraphLaunch(p->ad_exec, st), "graph launch");
+        launches = p->ad_launches;
+    }
+    std::vector<int64_t> counts((size_t)K);
+    gsea::AdaptiveCtl ctl{};
+    std::vector<double> err(use_model ? (size_t)K : 0);
+    GSEA_CUDA(cudaMemcpyAsync(counts.data(), p->counts, sizeof(int64_t) * K, cudaMemcpyDeviceToHost, st),
               "copy counts");
-    GSEA_CUDA(gsea::launch_stats_ragged<T>(es, K, P, p->counts, P0, static_cast<T*>(p->stats), p->stats_scratch, st),
-              "statistics kernels");
+    GSEA_CUDA(cudaMemcpyAsync(&ctl, p->ad_ctl, sizeof(ctl), cudaMemcpyDeviceToHost, st), "copy decisions");
+    if (use_model)
+        GSEA_CUDA(cudaMemcpyAsync(err.data(), p->ad_err, sizeof(double) * K, cudaMemcpyDeviceToHost, st),
+                  "copy model errors");
     GSEA_CUDA(cudaStreamSynchronize(st), "stream sync");
-    p->last_launches = gsea::launches_take();
+    if ((rc = gsea::plan_check_error(p))) return rc;
+    p->last_launches = launches;
     if (counts_out) std::copy(counts.begin(), counts.end(), counts_out);
     if (report) {
-        report->rounds = rounds;
         int64_t total = 0, full = 0;
         for (int64_t c : counts) {
             total += c;
             full += c == P;
         }
+        std::vector<double> valid;
+        for (double e : err)
+            if (std::isfinite(e)) valid.push_back(e);
+        report->rounds = (int64_t)ctl.rounds;
         report->scores = total;
-        report->stopped_pilot = stopped_pilot;
+        report->stopped_pilot = (int64_t)ctl.stopped_pilot;
         report->full_sets = full;
-        report->stop_p = stop_p;
-        report->model_used = model_used;
-        report->model_mean_err = mean_err;
-        report->prior_sets = prior_sets;
-        report->prior_agreed = prior_agreed;
-        report->stopped_q = stopped_q;
+        report->stop_p = ctl.stop_p;
+        report->model_used = ctl.model_used;
+        report->model_mean_err = use_model ? median(valid) : NAN;
+        report->prior_sets = (int64_t)ctl.prior_sets;
+        report->prior_agreed = (int64_t)ctl.prior_agreed;
+        report->stopped_q = (int64_t)ctl.stopped_q;
     }
     return GSEA_OK;
 }

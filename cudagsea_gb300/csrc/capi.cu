@@ -100,7 +100,8 @@ void free_plan_buffers(gsea_plan_s* p) {
     void* bufs[] = {p->exprs, p->labels, p->set_off, p->set_genes, p->set_order, p->masks, p->fast_ok, p->decay, p->gene_mu,
                     p->gene_t1, p->gene_t2, p->opA1, p->opA2, p->opB, p->dev_error, p->keys,
                     p->ranks, p->sorted, p->order, p->sort_scratch, p->es, p->stats, p->stats_scratch,
-                    p->moments, p->active, p->counts, p->exceed, p->sumabs, p->qlow, p->feat, p->pred};
+                    p->moments, p->active, p->counts, p->exceed, p->sumabs, p->qlow, p->feat, p->pred,
+                    p->stop, p->ad_err, p->ad_ctl};
     for (void* b : bufs)
         if (b) cudaFree(b);
     p->exprs = p->labels = nullptr;
@@ -124,6 +125,9 @@ void free_plan_buffers(gsea_plan_s* p) {
     p->sumabs = nullptr;
     p->qlow = nullptr;
     p->feat = p->pred = nullptr;
+    p->stop = nullptr;
+    p->ad_err = nullptr;
+    p->ad_ctl = nullptr;
 }
 
 void drop_graph(gsea_plan_s* p) {
@@ -131,6 +135,11 @@ void drop_graph(gsea_plan_s* p) {
     if (p->graph) cudaGraphDestroy(p->graph);
     p->graph_exec = nullptr;
     p->graph = nullptr;
+    if (p->ad_exec) cudaGraphExecDestroy(p->ad_exec);  // the adaptive test's graph holds the same launches
+    if (p->ad_graph) cudaGraphDestroy(p->ad_graph);
+    p->ad_exec = nullptr;
+    p->ad_graph = nullptr;
+    p->ad_key.clear();
 }
 
 template <class Ptr>
@@ -239,7 +248,7 @@ int check_device_error(gsea_plan_s* p) {
 
 template <class T>
 int run_range_t(gsea_plan_s* p, cudaStream_t st, int64_t lo, int64_t hi, const int32_t* set_list, int n_sets,
-                bool with_es = true) {
+                bool with_es = true, const int* n_dev = nullptr) {
     const gsea_config& c = p->cfg;
     const int G = (int)c.num_genes, S = (int)c.num_samples;
     const int64_t P = c.num_perms;
@@ -280,7 +289,7 @@ int run_range_t(gsea_plan_s* p, cudaStream_t st, int64_t lo, int64_t hi, const i
         if (!with_es) continue;
         GSEA_CUDA(gsea::launch_es<T>(p->ranks, p->ranks16, static_cast<const T*>(p->sorted), G, nb, p->set_off,
                                      p->set_genes, set_list, static_cast<const T*>(p->decay), n_sets,
-                                     static_cast<T*>(p->es), P, b0, st, et),
+                                     static_cast<T*>(p->es), P, b0, st, et, n_dev),
                   "enrichment kernel");
         if ((rc = mark(p, 3, st))) return rc;
     }
@@ -355,13 +364,15 @@ int write_dump(const char* prefix, const void* es, int64_t K, int64_t P, int pre
 }  // namespace
 
 namespace gsea {
-int plan_run_range(gsea_plan_s* p, cudaStream_t st, int64_t lo, int64_t hi, const int32_t* set_list, int n_sets) {
+int plan_run_range(gsea_plan_s* p, cudaStream_t st, int64_t lo, int64_t hi, const int32_t* set_list, int n_sets,
+                   const int* n_dev) {
     if (injected("launch")) return fail(GSEA_ERR_INJECTED, "injected launch failure");
-    return p->cfg.precision == 64 ? run_range_t<double>(p, st, lo, hi, set_list, n_sets)
-                                  : run_range_t<float>(p, st, lo, hi, set_list, n_sets);
+    return p->cfg.precision == 64 ? run_range_t<double>(p, st, lo, hi, set_list, n_sets, true, n_dev)
+                                  : run_range_t<float>(p, st, lo, hi, set_list, n_sets, true, n_dev);
 }
 int plan_dev_alloc(void** ptr, size_t bytes, const char* what) { return dev_alloc(ptr, bytes, what); }
 void plan_drop_graph(gsea_plan_s* p) { drop_graph(p); }
+int plan_check_error(gsea_plan_s* p) { return p->cfg.form != GSEA_FORM_PLAIN ? check_device_error(p) : GSEA_OK; }
 int plan_run_stage1(gsea_plan_s* p, cudaStream_t st) {
     return p->cfg.precision == 64 ? run_range_t<double>(p, st, 0, p->cfg.num_perms, nullptr, 0, false)
                                   : run_range_t<float>(p, st, 0, p->cfg.num_perms, nullptr, 0, false);

@@ -2,6 +2,8 @@
 // moments, per-set null statistics, training samples, features and the
 // exceedance counts of the sequential stopping rule.  No counterpart in the
 // reference.
+#include <math_constants.h>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -163,8 +165,9 @@ __global__ void model_features_kernel(const T* __restrict__ es, int64_t ld, cons
 template <class T>
 __global__ void exceed_kernel(const T* __restrict__ es, int64_t ld, const int32_t* __restrict__ list, int n_list,
                               int K, int64_t lo, int64_t hi, unsigned long long* __restrict__ exceed,
-                              double* __restrict__ sumabs) {
+                              double* __restrict__ sumabs, const int* __restrict__ n_dev) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (n_dev) n_list = min(n_list, *n_dev);
     if (warp >= n_list) return;
     const int64_t k = list ? list[warp] : warp;
     const T* row = es + k * ld;
@@ -190,7 +193,200 @@ __global__ void exceed_kernel(const T* __restrict__ es, int64_t ld, const int32_
     }
 }
 
+// ---- the adaptive test's decisions on the device -------------------------
+
+__device__ __forceinline__ double block_max(double v, double* sh) {
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) v = fmax(v, __shfl_xor_sync(kFullMask, v, o));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    double r = sh[0];
+    for (int w = 1; w < nw; w++) r = fmax(r, sh[w]);
+    return r;
+}
+
+// one block of 1,024 threads
+template <class T>
+__global__ void __launch_bounds__(1024)
+adaptive_prepare_kernel(int K, const T* __restrict__ stats, const float* __restrict__ pred,
+                        const double* __restrict__ sumabs, AdaptiveRule rule, double* __restrict__ err,
+                        AdaptiveCtl* __restrict__ ctl) {
+    __shared__ double sh[32];
+    double pstar = 0.0, valid = 0.0, ok = 0.0;
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+        const double q = (double)stats[4 * (size_t)K + k], np = (double)stats[2 * (size_t)K + k];
+        if (q < rule.q_call && np > pstar) pstar = np;
+        if (pred) {
+            const double mt = (double)pred[2 * (size_t)k + 1], mh = sumabs[k] / (double)rule.P0;
+            double e = CUDART_NAN;
+            if (isfinite(mt) && mt > 0.0 && isfinite(mh) && mh > 0.0) {
+                e = fabs(log(mt / mh));
+                valid += 1.0;
+                ok += e <= rule.tol ? 1.0 : 0.0;
+            }
+            err[k] = e;
+        }
+    }
+    pstar = block_max(pstar, sh);
+    valid = block_sum(valid, sh);
+    ok = block_sum(ok, sh);
+    if (threadIdx.x == 0) {
+        ctl->stop_p = fmin(1.0, fmax(rule.p_floor, rule.margin * pstar));
+        // the median error is within tolerance iff at least n/2 + 1 of the n errors are
+        const unsigned long long nv = (unsigned long long)valid, nk = (unsigned long long)ok;
+        ctl->model_used = (pred && nv > 0 && nk >= nv / 2 + 1) ? 1 : 0;
+        ctl->valid = nv;
+        ctl->within_tol = nk;
+    }
+}
+
+// the model's prior of set k: probability pm and pseudo-count w (w = 0: none),
+// rounded through float as the host rule receives them
+__device__ __forceinline__ void model_prior(const float* pred, int64_t k, const AdaptiveRule& rule, double& pm,
+                                            double& w) {
+    const double v = fmin(fmax((double)pred[2 * k], 1e-6), 1.0 - 1e-6);
+    const float pf = (float)v;
+    const float wf = (float)fmin(1.0 / (rule.s2 * v * (1.0 - v)), rule.cap);
+    pm = fmin(fmax((double)pf, 1e-6), 1.0 - 1e-6);
+    w = (isfinite(pf) && isfinite(wf) && wf > 0.f) ? (double)wf : 0.0;
+}
+
+__device__ __forceinline__ bool prior_agrees_dev(double pm, double w, double n, double c, double z) {
+    const double sd_pp = sqrt(pm * (1.0 - pm) * (w + n) / (n * (w + 1.0)));
+    return fabs(c / n - pm) <= z * sd_pp;
+}
+
+__global__ void adaptive_decide_kernel(int K, const int32_t* __restrict__ list, const int* __restrict__ n_dev,
+                                       const int64_t* __restrict__ counts, const unsigned long long* __restrict__ exceed,
+                                       const float* __restrict__ pred, const float* __restrict__ qlow, int bound_on,
+                                       int pilot, AdaptiveRule rule, uint8_t* __restrict__ stop,
+                                       AdaptiveCtl* __restrict__ ctl) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n_list = list ? min(K, *n_dev) : K;
+    if (i >= n_list) return;
+    const int64_t k = list ? list[i] : i;
+    const double n = (double)counts[k], c = (double)exceed[k];
+    uint8_t s = 0;
+    if (n > 0 && c >= 0 && c <= n) {
+        double a = 0.5 + c, b = 0.5 + (n - c);
+        if (pred && ctl->model_used) {
+            double pm, w;
+            model_prior(pred, k, rule, pm, w);
+            if (w > 0.0) {
+                const bool agree = prior_agrees_dev(pm, w, n, c, rule.z);
+                if (agree) {
+                    a += pm * w;
+                    b += (1.0 - pm) * w;
+                }
+                if (pilot) {
+                    atomicAdd(&ctl->prior_sets, 1ull);
+                    if (agree) atomicAdd(&ctl->prior_agreed, 1ull);
+                }
+            }
+        }
+        const double t = a + b, mean = a / t, sd = sqrt(a * b / (t * t * (t + 1.0)));
+        s = mean - rule.z * sd >= ctl->stop_p ? 1 : 0;
+    }
+    if (bound_on && !s && counts[k] < rule.P && (double)qlow[k] >= rule.q_stop) {
+        s = 1;
+        atomicAdd(&ctl->stopped_q, 1ull);
+    }
+    if (pilot && s) atomicAdd(&ctl->stopped_pilot, 1ull);
+    stop[k] = s;
+}
+
+// one block of 1,024 threads: a block-wide scan per chunk of the set order
+__global__ void __launch_bounds__(1024)
+adaptive_compact_kernel(int K, const int32_t* __restrict__ order, const uint8_t* __restrict__ stop,
+                        int32_t* __restrict__ active, AdaptiveCtl* __restrict__ ctl) {
+    __shared__ int warp_tot[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int carry = 0;
+    for (int base = 0; base < K; base += 1024) {
+        const int i = base + threadIdx.x;
+        const int k = i < K ? order[i] : 0;
+        const int f = (i < K && !stop[k]) ? 1 : 0;
+        const unsigned bal = __ballot_sync(kFullMask, f);
+        const int in_warp = __popc(bal & ((1u << lane) - 1u));
+        if (lane == 0) warp_tot[warp] = __popc(bal);
+        __syncthreads();
+        int before = carry;
+        for (int w = 0; w < warp; w++) before += warp_tot[w];
+        if (f) active[before + in_warp] = k;
+        int total = 0;
+        for (int w = 0; w < 32; w++) total += warp_tot[w];
+        __syncthreads();  // warp_tot is rewritten by the next chunk
+        carry += total;
+    }
+    if (threadIdx.x == 0) ctl->n_active = carry;
+}
+
+__global__ void adaptive_counts_kernel(int K, const int32_t* __restrict__ active, AdaptiveCtl* __restrict__ ctl,
+                                       int64_t next, int64_t* __restrict__ counts) {
+    const int n = min(K, ctl->n_active);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) counts[active[i]] = next;
+    if (i == 0 && n > 0) ctl->rounds += 1;
+}
+
+__global__ void adaptive_reset_kernel(int K, int64_t v, int64_t* __restrict__ counts, AdaptiveCtl* __restrict__ ctl) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < K) counts[i] = v;
+    if (i == 0) {
+        AdaptiveCtl z{};
+        z.rounds = 1;
+        z.n_active = K;
+        *ctl = z;
+    }
+}
+
 }  // namespace
+
+template <class T>
+cudaError_t launch_adaptive_prepare(int K, const T* stats, const float* pred, const double* sumabs,
+                                    const AdaptiveRule& rule, double* err, AdaptiveCtl* ctl, cudaStream_t st) {
+    adaptive_prepare_kernel<T><<<1, 1024, 0, st>>>(K, stats, pred, sumabs, rule, err, ctl);
+    launches_add(1);
+    return cudaGetLastError();
+}
+template cudaError_t launch_adaptive_prepare<float>(int, const float*, const float*, const double*,
+                                                    const AdaptiveRule&, double*, AdaptiveCtl*, cudaStream_t);
+template cudaError_t launch_adaptive_prepare<double>(int, const double*, const float*, const double*,
+                                                     const AdaptiveRule&, double*, AdaptiveCtl*, cudaStream_t);
+
+cudaError_t launch_adaptive_decide(int K, const int32_t* list, const int* n_dev, const int64_t* counts,
+                                   const unsigned long long* exceed, const float* pred, const float* qlow,
+                                   bool bound_on, bool pilot, const AdaptiveRule& rule, uint8_t* stop,
+                                   AdaptiveCtl* ctl, cudaStream_t st) {
+    if (K <= 0) return cudaSuccess;
+    adaptive_decide_kernel<<<(K + 255) / 256, 256, 0, st>>>(K, list, n_dev, counts, exceed, pred, qlow,
+                                                            bound_on ? 1 : 0, pilot ? 1 : 0, rule, stop, ctl);
+    launches_add(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adaptive_compact(int K, const int32_t* order, const uint8_t* stop, int32_t* active,
+                                    AdaptiveCtl* ctl, cudaStream_t st) {
+    adaptive_compact_kernel<<<1, 1024, 0, st>>>(K, order, stop, active, ctl);
+    launches_add(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adaptive_counts(int K, const int32_t* active, AdaptiveCtl* ctl, int64_t next,
+                                   int64_t* counts, cudaStream_t st) {
+    if (K <= 0) return cudaSuccess;
+    adaptive_counts_kernel<<<(K + 255) / 256, 256, 0, st>>>(K, active, ctl, next, counts);
+    launches_add(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adaptive_reset(int K, int64_t v, int64_t* counts, AdaptiveCtl* ctl, cudaStream_t st) {
+    adaptive_reset_kernel<<<(K + 255) / 256, 256, 0, st>>>(K, v, counts, ctl);
+    launches_add(1);
+    return cudaGetLastError();
+}
 
 template <class T>
 cudaError_t launch_moments(const T* keys, int G, double* moments, cudaStream_t st) {
@@ -245,15 +441,15 @@ template cudaError_t launch_model_features<double>(const double*, int64_t, const
 
 template <class T>
 cudaError_t launch_exceed(const T* es, int64_t ld, int K, const int32_t* list, int n_list, int64_t lo, int64_t hi,
-                          unsigned long long* exceed, double* sumabs, cudaStream_t st) {
+                          unsigned long long* exceed, double* sumabs, cudaStream_t st, const int* n_dev) {
     if (n_list <= 0 || hi <= lo) return cudaSuccess;
-    exceed_kernel<T><<<(n_list + 7) / 8, 256, 0, st>>>(es, ld, list, n_list, K, lo, hi, exceed, sumabs);
+    exceed_kernel<T><<<(n_list + 7) / 8, 256, 0, st>>>(es, ld, list, n_list, K, lo, hi, exceed, sumabs, n_dev);
     launches_add(1);
     return cudaGetLastError();
 }
 template cudaError_t launch_exceed<float>(const float*, int64_t, int, const int32_t*, int, int64_t, int64_t,
-                                          unsigned long long*, double*, cudaStream_t);
+                                          unsigned long long*, double*, cudaStream_t, const int*);
 template cudaError_t launch_exceed<double>(const double*, int64_t, int, const int32_t*, int, int64_t, int64_t,
-                                           unsigned long long*, double*, cudaStream_t);
+                                           unsigned long long*, double*, cudaStream_t, const int*);
 
 }  // namespace gsea

@@ -387,9 +387,11 @@ __global__ void __launch_bounds__(WARPS * 32)
 es_kernel(const RankT* __restrict__ ranks, const T* __restrict__ sorted_abs, int G, int num_perms,
           const int64_t* __restrict__ set_off, const int32_t* __restrict__ set_genes,
           const int32_t* __restrict__ set_order, const T* __restrict__ decay, int K, T* __restrict__ es,
-          int64_t es_stride, int64_t col0) {
+          int64_t es_stride, int64_t col0, const int* __restrict__ K_dev) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int next_set;
+    if (K_dev) K = min(K, *K_dev);  // a set list whose length a kernel decided
+    if (K <= 0) return;
     const int words = (G + 31) >> 5;
     const int region = WPL > 0 ? WPL * 32 : words;  // per-warp bitmap words
     T* s_w;
@@ -491,7 +493,7 @@ size_t es_smem_bytes(int G) {
 template <class T, class RankT, int WARPS, int STAGE, int WPL>
 cudaError_t launch_es_v(const RankT* ranks, const T* sorted_abs, int G, int P, const int64_t* off,
                         const int32_t* genes, const int32_t* order, const T* decay, int K, T* es, int64_t stride,
-                        int64_t col0, int grid, cudaStream_t st) {
+                        int64_t col0, int grid, cudaStream_t st, const int* K_dev) {
     const size_t smem = es_smem_bytes<T, RankT, WARPS, STAGE>(G);
     auto kern = es_kernel<T, RankT, WARPS, STAGE, WPL>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -501,7 +503,8 @@ cudaError_t launch_es_v(const RankT* ranks, const T* sorted_abs, int G, int P, c
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidValue;
     grid *= per_sm;
-    kern<<<grid, WARPS * 32, smem, st>>>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0);
+    kern<<<grid, WARPS * 32, smem, st>>>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0,
+                                         K_dev);
     launches_add(1);
     return cudaGetLastError();
 }
@@ -509,51 +512,51 @@ cudaError_t launch_es_v(const RankT* ranks, const T* sorted_abs, int G, int P, c
 template <class T, class RankT, int WARPS, int STAGE>
 cudaError_t launch_es_w(const RankT* ranks, const T* sorted_abs, int G, int P, const int64_t* off,
                         const int32_t* genes, const int32_t* order, const T* decay, int K, T* es, int64_t stride,
-                        int64_t col0, int grid, cudaStream_t st) {
+                        int64_t col0, int grid, cudaStream_t st, const int* K_dev) {
     // words per lane for the register-resident list procedure (u16 positions);
     // 32-bit ranks (G > 65,536) always take the general procedure
     if constexpr (sizeof(RankT) == 4) {
         if (STAGE >= 2) return cudaErrorInvalidValue;
         return launch_es_v<T, RankT, WARPS, STAGE, 0>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride,
-                                                      col0, grid, st);
+                                                      col0, grid, st, K_dev);
     } else if constexpr (STAGE >= 2 || WARPS == 24) {  // partial staging / 24 warps: the large-G classes
         switch (es_wpl(G, true)) {
-            case 24: return launch_es_v<T, RankT, WARPS, STAGE, 24>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-            case 32: return launch_es_v<T, RankT, WARPS, STAGE, 32>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-            case 40: return launch_es_v<T, RankT, WARPS, STAGE, 40>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-            case 48: return launch_es_v<T, RankT, WARPS, STAGE, 48>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-            case 64: return launch_es_v<T, RankT, WARPS, STAGE, 64>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+            case 24: return launch_es_v<T, RankT, WARPS, STAGE, 24>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st, K_dev);
+            case 32: return launch_es_v<T, RankT, WARPS, STAGE, 32>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st, K_dev);
+            case 40: return launch_es_v<T, RankT, WARPS, STAGE, 40>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st, K_dev);
+            case 48: return launch_es_v<T, RankT, WARPS, STAGE, 48>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st, K_dev);
+            case 64: return launch_es_v<T, RankT, WARPS, STAGE, 64>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st, K_dev);
             default: return cudaErrorInvalidValue;
         }
     } else {
         switch (es_wpl(G, true)) {
-            case 4: return launch_es_v<T, RankT, WARPS, STAGE, 4>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-            case 8: return launch_es_v<T, RankT, WARPS, STAGE, 8>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-            case 12: return launch_es_v<T, RankT, WARPS, STAGE, 12>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-            case 16: return launch_es_v<T, RankT, WARPS, STAGE, 16>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-            case 20: return launch_es_v<T, RankT, WARPS, STAGE, 20>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-            case 24: return launch_es_v<T, RankT, WARPS, STAGE, 24>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
-            case 32: return launch_es_v<T, RankT, WARPS, STAGE, 32>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+            case 4: return launch_es_v<T, RankT, WARPS, STAGE, 4>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st, K_dev);
+            case 8: return launch_es_v<T, RankT, WARPS, STAGE, 8>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st, K_dev);
+            case 12: return launch_es_v<T, RankT, WARPS, STAGE, 12>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st, K_dev);
+            case 16: return launch_es_v<T, RankT, WARPS, STAGE, 16>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st, K_dev);
+            case 20: return launch_es_v<T, RankT, WARPS, STAGE, 20>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st, K_dev);
+            case 24: return launch_es_v<T, RankT, WARPS, STAGE, 24>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st, K_dev);
+            case 32: return launch_es_v<T, RankT, WARPS, STAGE, 32>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st, K_dev);
             case 40:  // the staging of ranks and weights never fits beside these regions
-                if constexpr (STAGE == 0) return launch_es_v<T, RankT, WARPS, 0, 40>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+                if constexpr (STAGE == 0) return launch_es_v<T, RankT, WARPS, 0, 40>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st, K_dev);
                 return cudaErrorInvalidValue;
             case 48:
-                if constexpr (STAGE == 0) return launch_es_v<T, RankT, WARPS, 0, 48>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+                if constexpr (STAGE == 0) return launch_es_v<T, RankT, WARPS, 0, 48>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st, K_dev);
                 return cudaErrorInvalidValue;
             case 64:
-                if constexpr (STAGE == 0) return launch_es_v<T, RankT, WARPS, 0, 64>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st);
+                if constexpr (STAGE == 0) return launch_es_v<T, RankT, WARPS, 0, 64>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st, K_dev);
                 return cudaErrorInvalidValue;
             default: break;
         }
         return launch_es_v<T, RankT, WARPS, STAGE, 0>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride,
-                                                      col0, grid, st);
+                                                      col0, grid, st, K_dev);
     }
 }
 
 template <class T, class RankT>
 cudaError_t launch_es_t(const RankT* ranks, const T* sorted_abs, int G, int P, const int64_t* off,
                         const int32_t* genes, const int32_t* order, const T* decay, int K, T* es, int64_t stride,
-                        int64_t col0, EsTuning tune, cudaStream_t st) {
+                        int64_t col0, EsTuning tune, cudaStream_t st, const int* K_dev) {
     int dev = 0, max_smem = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
@@ -586,7 +589,8 @@ cudaError_t launch_es_t(const RankT* ranks, const T* sorted_abs, int G, int P, c
         if (tune.warps && tune.warps != c.warps) continue;
         if (tune.stage >= 0 && tune.stage != c.stage) continue;
 #define GSEA_ES(W, S) \
-    return launch_es_w<T, RankT, W, S>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st)
+    return launch_es_w<T, RankT, W, S>(ranks, sorted_abs, G, P, off, genes, order, decay, K, es, stride, col0, grid, st, \
+                                       K_dev)
         if (c.warps == 32 && c.stage == 1) GSEA_ES(32, 1);
         if (c.warps == 16 && c.stage == 1) GSEA_ES(16, 1);
         if (c.warps == 8 && c.stage == 1) GSEA_ES(8, 1);
@@ -714,13 +718,13 @@ template <class T>
 cudaError_t launch_es(const void* ranks, bool ranks16, const T* sorted_abs, int G, int num_perms,
                       const int64_t* set_offsets, const int32_t* set_genes, const int32_t* set_order,
                       const T* decay, int K, T* es, int64_t es_stride, int64_t perm_col0, cudaStream_t st,
-                      EsTuning tune) {
+                      EsTuning tune, const int* K_dev) {
     if (num_perms <= 0 || K <= 0) return cudaSuccess;
     if (ranks16)
         return launch_es_t<T, uint16_t>(static_cast<const uint16_t*>(ranks), sorted_abs, G, num_perms, set_offsets,
-                                        set_genes, set_order, decay, K, es, es_stride, perm_col0, tune, st);
+                                        set_genes, set_order, decay, K, es, es_stride, perm_col0, tune, st, K_dev);
     return launch_es_t<T, uint32_t>(static_cast<const uint32_t*>(ranks), sorted_abs, G, num_perms, set_offsets,
-                                    set_genes, set_order, decay, K, es, es_stride, perm_col0, tune, st);
+                                    set_genes, set_order, decay, K, es, es_stride, perm_col0, tune, st, K_dev);
 }
 
 // decay[n] = (T)(1.0 / (G - n)) for n < G, 0 for n = G: the miss step of a

@@ -60,7 +60,9 @@ template <class T>
 cudaError_t launch_es(const void* ranks, bool ranks16, const T* sorted_abs, int G, int num_perms,
                       const int64_t* set_offsets, const int32_t* set_genes, const int32_t* set_order,
                       const T* decay, int K, T* es, int64_t es_stride, int64_t perm_col0, cudaStream_t st,
-                      EsTuning tune = EsTuning());
+                      EsTuning tune = EsTuning(), const int* K_dev = nullptr);
+// (K_dev: when not null, the number of sets is min(K, *K_dev), read on the
+// device -- a set list whose length a kernel decided)
 template <class T>
 cudaError_t launch_decay_table(int G, T* decay, cudaStream_t st);
 
@@ -140,14 +142,55 @@ template <class T>
 cudaError_t launch_model_features(const T* es, int64_t ld, const int64_t* off, int K, const double* mom,
                                   const double* sumabs, int64_t n, float* x, cudaStream_t st);
 // sumabs: [2K], sum of |S| then sum of S^2 per set
+// (n_dev: when not null, the list holds min(n_list, *n_dev) sets, read on the device)
 template <class T>
 cudaError_t launch_exceed(const T* es, int64_t ld, int K, const int32_t* list, int n_list, int64_t lo, int64_t hi,
-                          unsigned long long* exceed, double* sumabs, cudaStream_t st);
+                          unsigned long long* exceed, double* sumabs, cudaStream_t st, const int* n_dev = nullptr);
 // after launch_stats_ragged with the same (K, p_fwer, scratch): a lower bound
 // of every set's FDR q with its NES pushed z standard errors outward
 template <class T>
 cudaError_t launch_fdr_bound(int K, int64_t p_fwer, const T* stats, const int64_t* counts, const double* sums,
                              double z, const void* scratch, float* qlow, cudaStream_t st);
+
+// The adaptive test's decisions on the device (k_adaptive.cu): the pilot's
+// p threshold and model fallback test, the stopping rule per round, the list
+// of sets still running.  Counters for the report.
+struct AdaptiveCtl {
+    double stop_p;                    // p threshold of the stopping rule
+    int n_active;                     // sets still running (length of the active list)
+    int model_used;                   // 1: the model's prior enters the rule
+    unsigned long long stopped_pilot;  // sets stopped after the pilot
+    unsigned long long stopped_q;      // sets stopped by the FDR bound, any round
+    unsigned long long prior_sets;     // sets with a usable model prior
+    unsigned long long prior_agreed;   // of those, pilots within z sd of the prior predictive
+    unsigned long long rounds;         // rounds run, the pilot included
+    unsigned long long valid;          // sets whose model error is defined
+    unsigned long long within_tol;     // of those, error <= the fallback tolerance
+};
+struct AdaptiveRule {  // the rule's constants
+    double q_call, margin, p_floor, z, q_stop, tol, cap, s2;  // s2: sigma_tail^2 of the model
+    int64_t P, P0;
+};
+// pilot: stop_p = min(1, max(p_floor, margin * max{NP_k : FDR_k < q_call}))
+// and the model fallback test (pred may be null: no model)
+template <class T>
+cudaError_t launch_adaptive_prepare(int K, const T* stats, const float* pred, const double* sumabs,
+                                    const AdaptiveRule& rule, double* err, AdaptiveCtl* ctl, cudaStream_t st);
+// the stopping rule over the sets of `list` (n_dev entries; list null: all K
+// sets), optionally the FDR bound (qlow); pilot != 0 also counts the prior's
+// agreement and the sets stopped after the pilot
+cudaError_t launch_adaptive_decide(int K, const int32_t* list, const int* n_dev, const int64_t* counts,
+                                   const unsigned long long* exceed, const float* pred, const float* qlow,
+                                   bool bound_on, bool pilot, const AdaptiveRule& rule, uint8_t* stop,
+                                   AdaptiveCtl* ctl, cudaStream_t st);
+// active list (ctl->n_active) = sets of `order` not stopped, in that order
+cudaError_t launch_adaptive_compact(int K, const int32_t* order, const uint8_t* stop, int32_t* active,
+                                    AdaptiveCtl* ctl, cudaStream_t st);
+// counts[active[i]] = next for the active sets; counts the round if any ran
+cudaError_t launch_adaptive_counts(int K, const int32_t* active, AdaptiveCtl* ctl, int64_t next,
+                                   int64_t* counts, cudaStream_t st);
+// counts[k] = v for every set, and the decision record cleared (rounds = 1)
+cudaError_t launch_adaptive_reset(int K, int64_t v, int64_t* counts, AdaptiveCtl* ctl, cudaStream_t st);
 
 // number of kernel launches issued by the launchers above since the last reset
 int64_t launches_take();

@@ -91,6 +91,16 @@ struct gsea_plan_s {
     float* qlow = nullptr;             // [K] lower bound of each set's FDR q (adaptive stopping)
     float* feat = nullptr;             // [K][5] model features
     float* pred = nullptr;             // [K][2] model predictions
+    // the adaptive test on the device: per-set stop flags, the model's error
+    // per set, the decision record (gsea::AdaptiveCtl) and the captured graph
+    // of the whole test with what it was captured for (parameters, model)
+    uint8_t* stop = nullptr;           // [K]
+    double* ad_err = nullptr;          // [K] |log m~ - log m^| of the model, NaN where undefined
+    void* ad_ctl = nullptr;
+    cudaGraph_t ad_graph = nullptr;
+    cudaGraphExec_t ad_exec = nullptr;
+    std::vector<unsigned char> ad_key;
+    int64_t ad_launches = 0;
     // stage timing (gsea_plan_set_profiling): events recorded at every stage
     // boundary of the last execute, tagged with the stage they close
     bool profile = false;
@@ -103,10 +113,14 @@ namespace gsea {
 // Scores permutations [lo, hi) (global indices perm_offset + lo ...) of the
 // sets set_list[0..n_sets) into columns lo..hi-1 of the plan's ES matrix
 // (row stride num_perms).  No statistics.
-int plan_run_range(gsea_plan_s* p, cudaStream_t st, int64_t lo, int64_t hi, const int32_t* set_list, int n_sets);
+// n_dev (may be null): the list holds min(n_sets, *n_dev) sets, read on the device.
+int plan_run_range(gsea_plan_s* p, cudaStream_t st, int64_t lo, int64_t hi, const int32_t* set_list, int n_sets,
+                   const int* n_dev = nullptr);
 int plan_dev_alloc(void** ptr, size_t bytes, const char* what);
 // forget the captured execute graph (buffers, tuning or debug changed)
 void plan_drop_graph(gsea_plan_s* p);
+// after a synchronisation: GSEA_ERR_CUDA if a tensor-core kernel's bounded wait expired
+int plan_check_error(gsea_plan_s* p);
 // permutation, metric and sort of every permutation (one device batch) without
 // the enrichment kernel; and the statistics of the plan's ES matrix
 int plan_run_stage1(gsea_plan_s* p, cudaStream_t st);

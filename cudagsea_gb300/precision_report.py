@@ -1,4 +1,4 @@
-"""Error of the tensor-core form against FP64, per metric, at the precision
+"""Error of the tensor-core forms against FP64, per metric, at the precision
 workload (20,000 genes x 600 samples, 300/300, 2,000 sets).
 
 The FP64 reference is the plain form in double precision (every stage in
@@ -10,7 +10,12 @@ permutations -- positions where the tensor-core order differs from the FP64
 order -- split into near-ties (FP64 keys within 1e-4 of the permutation's key
 scale) and the rest.  The same comparison for the plain form in fp32 (the
 reference's own single-precision arithmetic) shows what any FP32 evaluation
-of the path loses against FP64.
+of the path loses against FP64.  Both tensor-core forms are reported: the
+error-free FP32 variance (GSEA_FORM_CHOSEN) and the FP64 variance
+finalisation (GSEA_FORM_CHOSEN_FP64); for each, every set above
+|dNES| = 1e-4 is traced to its moved scores (precision_check.compare: a
+moved score is order-explained when the FP64 keys walked in the form's own
+rank order reproduce it).
 
     python -m cudagsea_gb300.precision_report [--perms 10000] [--sample 64] [--json out.json]
 """
@@ -91,11 +96,31 @@ def main(argv=None) -> int:
                 "calls_fp64": len(calls_r), "calls": len(calls_c), "call_diff": len(calls_c ^ calls_r),
                 "rank_flips_near_tie": near, "rank_flips_other": other}
 
+    from . import precision_check as PC
+
+    def traced(form, ref_run):
+        cur = PC.run_form(d, m, 32, form)
+        try:
+            rep = PC.compare(d, cur, ref_run)
+        finally:
+            cur.close()
+        return {"sets_dNES_over_1e-4": rep["sets_over_tol"], "all_tie_explained": rep["all_tie_explained"],
+                "traced_not_explained": sum(1 for e in rep["exceedances"] if not e["tie_explained"]),
+                "fdr_call_diffs": rep["fdr_call_diffs"]}
+
     for m, name in enumerate(api.METRICS):
         ref = run(d, m, 64, N.FORM_PLAIN, a.sample)
         tensor = compare(*run(d, m, 32, N.FORM_CHOSEN, a.sample), *ref)
+        tensor64 = compare(*run(d, m, 32, N.FORM_CHOSEN_FP64, a.sample), *ref)
         plain32 = compare(*run(d, m, 32, N.FORM_PLAIN, a.sample), *ref)
-        row = {"metric": name, "tensor_core_fp32": tensor, "plain_fp32": plain32}
+        ref_run = PC.run_form(d, m, 64, N.FORM_PLAIN)
+        try:
+            tensor["trace"] = traced(N.FORM_CHOSEN, ref_run)
+            tensor64["trace"] = traced(N.FORM_CHOSEN_FP64, ref_run)
+        finally:
+            ref_run.close()
+        row = {"metric": name, "tensor_core_fp32": tensor, "tensor_core_fp64_variance": tensor64,
+               "plain_fp32": plain32}
         rows.append(row)
         print(json.dumps(row), flush=True)
     if a.json:

@@ -323,3 +323,32 @@ def test_adaptive_double_precision_matches_full_test(gpu):
     for k in sorted(calls ^ calls_f):
         assert abs(st_f[4][k] - Q_CALL) <= Q_BAND, (k, st_f[4][k], st_a[4][k])
     assert np.all(counts[sorted(calls)] == P_MAX)
+
+
+def test_adaptive_graph_replays_and_matches_the_host_rule(gpu):
+    """The adaptive test runs as one captured CUDA graph: the decisions are
+    kernels, the set counts read on the device.  A replay gives the same
+    counts and statistics bit for bit, a parameter change records a new graph,
+    and the final decisions equal the host-side rule (gsea_adaptive_decide)
+    applied to the final counts and exceedances."""
+    d = case(seed=91)
+    plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, P_MAX, "twopass_signal2noise")
+    plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+    a = allocator.execute_adaptive(plan, None, pilot_perms=250, q_margin=0.0)
+    st_a = plan.read(es=False)[1]
+    b = allocator.execute_adaptive(plan, None, pilot_perms=250, q_margin=0.0)
+    st_b = plan.read(es=False)[1]
+    assert np.array_equal(a.counts, b.counts) and a.report == b.report
+    assert np.array_equal(st_a.view(np.uint32), st_b.view(np.uint32))
+    c = allocator.execute_adaptive(plan, None, pilot_perms=500, q_margin=0.0)
+    assert c.counts.min() >= 500 and not np.array_equal(c.counts, a.counts)
+    a2 = allocator.execute_adaptive(plan, None, pilot_perms=250, q_margin=0.0)
+    assert np.array_equal(a2.counts, a.counts)
+    # the host rule on the final state: every set that stopped short of P_MAX
+    # is one the rule stops, given the run's own stop_p
+    es, _ = plan.read(stats=False)
+    exceed = np.array([int(np.sum(np.abs(es[k, :a.counts[k]]) >= np.abs(es[k, 0]))) for k in range(d.num_sets)])
+    stop = allocator.decide(a.counts, exceed, a.report["stop_p"])
+    short = a.counts < P_MAX
+    assert np.all(stop[short] == 1)
+    plan.close()

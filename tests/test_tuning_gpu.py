@@ -63,15 +63,32 @@ def test_invalid_tuning_is_rejected(gpu, data):
         plan.set_tuning(es_warps=12)
     with pytest.raises(N.GseaError):
         plan.set_tuning(chosen_tile=64)
-    # fp64 keys cannot take the register sort
-    p64 = api.Plan(data.num_genes, data.num_samples, data.num_sets, 64, 8, precision=64)
+    # fp64 keys take the register sort up to 20,480 genes (one CTA, then a
+    # two-CTA cluster), not beyond
+    big = synthetic.make(20481, 8, 3, 4, seed=3, n_class_b=4)
+    p64 = api.Plan(big.num_genes, big.num_samples, big.num_sets, 4, 8, precision=64)
     p64.set_tuning(sort_variant=1)
-    p64.set_inputs(data.exprs, data.labels, data.set_offsets, data.set_genes)
+    p64.set_inputs(big.exprs, big.labels, big.set_offsets, big.set_genes)
     with pytest.raises(N.GseaError):
         p64.execute()
         p64.synchronize()
     plan.close()
     p64.close()
+
+
+def test_fp64_register_sort_equals_tiled(gpu, data):
+    """fp64 at this size: the register / cluster sort (variant 1) and the
+    tiled sort (variant 2) give the same ranks, hence the same ES bit for bit."""
+    out = []
+    for v in (1, 2):
+        plan = api.Plan(data.num_genes, data.num_samples, data.num_sets, data.num_perms, 8, precision=64)
+        plan.set_tuning(sort_variant=v)
+        plan.set_inputs(data.exprs, data.labels, data.set_offsets, data.set_genes)
+        plan.execute()
+        out.append(plan.read())
+        plan.close()
+    assert np.array_equal(out[0][0].view(np.uint64), out[1][0].view(np.uint64))
+    assert np.array_equal(out[0][1].view(np.uint64), out[1][1].view(np.uint64))
 
 
 @pytest.mark.parametrize("form", [N.FORM_PLAIN, N.FORM_CHOSEN])
