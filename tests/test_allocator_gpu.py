@@ -338,7 +338,9 @@ def test_adaptive_graph_replays_and_matches_the_host_rule(gpu):
     st_a = plan.read(es=False)[1]
     b = allocator.execute_adaptive(plan, None, pilot_perms=250, q_margin=0.0)
     st_b = plan.read(es=False)[1]
-    assert np.array_equal(a.counts, b.counts) and a.report == b.report
+    assert np.array_equal(a.counts, b.counts)
+    assert all(a.report[k] == b.report[k] or (a.report[k] != a.report[k] and b.report[k] != b.report[k])
+               for k in a.report)  # NaN (no model error) on both sides counts as equal
     assert np.array_equal(st_a.view(np.uint32), st_b.view(np.uint32))
     c = allocator.execute_adaptive(plan, None, pilot_perms=500, q_margin=0.0)
     assert c.counts.min() >= 500 and not np.array_equal(c.counts, a.counts)
