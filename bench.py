@@ -84,6 +84,10 @@ def parse():
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the adaptive forms (sequential rule with and without the learned prior)")
     ap.add_argument("--pilot", type=int, default=250, help="pilot permutations of the adaptive forms")
+    ap.add_argument("--growth", type=float, default=4.0,
+                    help="growth of the permutation count between rounds of the headline's adaptive forms (4: the "
+                         "pilot, then one round to all 1,000 permutations); the learned workload keeps the "
+                         "library's doubling")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the automatic launch configuration (by default each form's plan is autotuned on a "
                          "sample of its permutations before the warm-up, outside the timed region)")
@@ -417,14 +421,14 @@ def run_adaptive(args, d, full_plan, stream, flush, local):
         plan = api.Plan(d.num_genes, d.num_samples, K, P, args.metric, form=N.FORM_CHOSEN, device=local)
         plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
         for _ in range(args.warmup):
-            allocator.execute_adaptive(plan, m, pilot_perms=args.pilot)
+            allocator.execute_adaptive(plan, m, pilot_perms=args.pilot, growth=args.growth)
         times = []
         for _ in range(args.steps):
             with torch.cuda.stream(stream):
                 flush.zero_()
             torch.cuda.synchronize()
             t1 = time.perf_counter()
-            res = allocator.execute_adaptive(plan, m, pilot_perms=args.pilot)  # returns after its last copy
+            res = allocator.execute_adaptive(plan, m, pilot_perms=args.pilot, growth=args.growth)  # after its last copy
             times.append(time.perf_counter() - t1)
         _, st = plan.read(es=False)
         calls = set(np.where(st.reshape(5, -1)[4] < 0.25)[0])
@@ -432,6 +436,7 @@ def run_adaptive(args, d, full_plan, stream, flush, local):
         out[name] = {"ms_per_step": mean_s * 1e3, "value_equivalent": K * P / mean_s,
                      "scores_per_s": res.report["scores"] / mean_s,
                      "scores_fraction": res.report["scores"] / (K * P), "pilot_perms": args.pilot,
+                     "growth": args.growth,
                      "rounds": res.report["rounds"], "stop_p": res.report["stop_p"],
                      "stopped_after_pilot": res.report["stopped_pilot"], "stopped_by_fdr_bound": res.report["stopped_q"],
                      "full_sets": res.report["full_sets"],
