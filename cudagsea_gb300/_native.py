@@ -71,6 +71,7 @@ class AdaptiveParams(ctypes.Structure):
         ("prior_cap", ctypes.c_double),
         ("fallback_tol", ctypes.c_double),
         ("q_margin", ctypes.c_double),
+        ("sig_margin", ctypes.c_double),
     ]
 
 
@@ -86,6 +87,8 @@ class AdaptiveReport(ctypes.Structure):
         ("prior_sets", ctypes.c_int64),
         ("prior_agreed", ctypes.c_int64),
         ("stopped_q", ctypes.c_int64),
+        ("stopped_sig", ctypes.c_int64),
+        ("p_sig", ctypes.c_double),
     ]
 
 

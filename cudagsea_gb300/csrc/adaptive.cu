@@ -19,9 +19,21 @@
 // p~ (1 - p~) (w + n) / (n (w + 1))) ignores the prior: the permutations
 // overrule the model.  The model is dropped for the run if the
 // median |log m~_k - log m^_k| between its predicted and the pilot's
-// measured null mean exceeds fallback_tol.  Sets that never stop run all
-// num_perms permutations, the full test; every reported statistic is counted
-// from the permutations a set received.
+// measured null mean exceeds fallback_tol.  Two rules on the set's FDR q,
+// from bounds over its NES uncertainty (z standard errors of its normalising
+// mean): a set whose q lower bound is >= q_margin * q_call stops as clearly
+// non-significant; a set whose q upper bound is <= q_call / sig_margin and
+// whose p upper bound (posterior mean + z sd, the same posterior, model prior
+// included) is <= p_sig = min{NP_k^pilot : FDR_k^pilot >= q_call} / sig_margin
+// stops as clearly significant -- the permutations go to the sets near the
+// call level.  Sets that never stop run all num_perms permutations, the full
+// test; every reported statistic is counted from the permutations a set
+// received.
+//
+// The whole test -- pilot, decisions, rounds, statistics -- is recorded once
+// into a CUDA graph and replayed: the decisions are kernels and the rounds
+// read the number of sets still running on the device, so the host waits
+// only for the final report.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -136,7 +148,7 @@ namespace {
 // active -- the set count is read on the device, so nothing waits for the
 // host -- and the final ragged statistics.
 template <class T>
-int record_adaptive(gsea_plan_s* p, gsea_model model, bool use_model, const gsea::AdaptiveRule& rule, bool q_on,
+int record_adaptive(gsea_plan_s* p, gsea_model model, bool use_model, const gsea::AdaptiveRule& rule, bool bounds_on,
                     const std::vector<std::pair<int64_t, int64_t>>& schedule, cudaStream_t st) {
     const int K = (int)p->cfg.num_sets;
     const int64_t P = p->cfg.num_perms, P0 = rule.P0;
@@ -152,9 +164,10 @@ int record_adaptive(gsea_plan_s* p, gsea_model model, bool use_model, const gsea
     if ((rc = gsea::plan_run_range(p, st, 0, P0, p->set_order, K))) return rc;
     GSEA_CUDA(gsea::launch_exceed<T>(es, P, K, nullptr, K, 0, P0, p->exceed, p->sumabs, st), "exceedance kernel");
     GSEA_CUDA(gsea::launch_stats_ragged<T>(es, K, P, p->counts, P0, stats, p->stats_scratch, st), "pilot statistics");
-    const bool bound0 = q_on && P0 < P;
+    const bool bound0 = bounds_on && P0 < P;
     if (bound0)
-        GSEA_CUDA(gsea::launch_fdr_bound<T>(K, P0, stats, p->counts, p->sumabs, rule.z, p->stats_scratch, p->qlow, st),
+        GSEA_CUDA(gsea::launch_fdr_bound<T>(K, P0, stats, p->counts, p->sumabs, rule.z, p->stats_scratch, p->qlow, st,
+                                            p->qhigh),
                   "FDR bound kernel");
     if (use_model) {
         GSEA_CUDA(gsea::launch_model_features<T>(es, P, p->set_off, K, p->moments, p->sumabs, P0, p->feat, st),
@@ -163,8 +176,8 @@ int record_adaptive(gsea_plan_s* p, gsea_model model, bool use_model, const gsea
     }
     GSEA_CUDA(gsea::launch_adaptive_prepare<T>(K, stats, pred, p->sumabs, rule, p->ad_err, ctl, st),
               "adaptive pilot decisions");
-    GSEA_CUDA(gsea::launch_adaptive_decide(K, nullptr, nullptr, p->counts, p->exceed, pred, p->qlow, bound0, true, rule,
-                                           p->stop, ctl, st),
+    GSEA_CUDA(gsea::launch_adaptive_decide(K, nullptr, nullptr, p->counts, p->exceed, pred, p->qlow, p->qhigh, bound0,
+                                           true, rule, p->stop, ctl, st),
               "stopping rule");
     GSEA_CUDA(gsea::launch_adaptive_compact(K, p->set_order, p->stop, p->active, ctl, st), "active sets");
     for (const auto& r : schedule) {
@@ -173,18 +186,18 @@ int record_adaptive(gsea_plan_s* p, gsea_model model, bool use_model, const gsea
         GSEA_CUDA(gsea::launch_exceed<T>(es, P, K, p->active, K, cur, next, p->exceed, p->sumabs, st, &ctl->n_active),
                   "exceedances");
         GSEA_CUDA(gsea::launch_adaptive_counts(K, p->active, ctl, next, p->counts, st), "set counts");
-        const bool bound_now = q_on && next < P;
+        const bool bound_now = bounds_on && next < P;
         if (bound_now) {  // statistics at the new counts, then the bounds
             // the stopping bound's null histogram: the pilot columns of
             // every set (the final statistics use every score)
             GSEA_CUDA(gsea::launch_stats_ragged<T>(es, K, P, p->counts, P0, stats, p->stats_scratch, st, P0),
                       "round statistics");
             GSEA_CUDA(gsea::launch_fdr_bound<T>(K, P0, stats, p->counts, p->sumabs, rule.z, p->stats_scratch, p->qlow,
-                                                st),
+                                                st, p->qhigh),
                       "FDR bound kernel");
         }
         GSEA_CUDA(gsea::launch_adaptive_decide(K, p->active, &ctl->n_active, p->counts, p->exceed, pred, p->qlow,
-                                               bound_now, false, rule, p->stop, ctl, st),
+                                               p->qhigh, bound_now, false, rule, p->stop, ctl, st),
                   "stopping rule");
         GSEA_CUDA(gsea::launch_adaptive_compact(K, p->set_order, p->stop, p->active, ctl, st), "active sets");
     }
@@ -204,6 +217,7 @@ int execute_adaptive_t(gsea_plan_s* p, gsea_model model, const gsea_adaptive_par
     if (rc) return rc;
     if (!p->stop && (rc = gsea::plan_dev_alloc((void**)&p->stop, (size_t)K, "stop flags"))) return rc;
     if (!p->ad_err && (rc = gsea::plan_dev_alloc((void**)&p->ad_err, sizeof(double) * K, "model errors"))) return rc;
+    if (!p->qhigh && (rc = gsea::plan_dev_alloc((void**)&p->qhigh, sizeof(float) * K, "q upper bounds"))) return rc;
     if (!p->ad_ctl && (rc = gsea::plan_dev_alloc(&p->ad_ctl, sizeof(gsea::AdaptiveCtl), "adaptive record")))
         return rc;
     // the learned prior: only a trained model (norms[14] set by calibration)
@@ -226,9 +240,10 @@ int execute_adaptive_t(gsea_plan_s* p, gsea_model model, const gsea_adaptive_par
     rule.tol = ap.fallback_tol;
     rule.cap = ap.prior_cap * (double)P0;
     rule.s2 = (double)norms[12] * (double)norms[12];
+    rule.sig_margin = ap.sig_margin;
     rule.P = P;
     rule.P0 = P0;
-    const bool q_on = ap.q_margin > 0.0;
+    const bool bounds_on = ap.q_margin > 0.0 || ap.sig_margin > 0.0;  // either rule needs the q bounds
     std::vector<std::pair<int64_t, int64_t>> schedule;
     for (int64_t cur = P0; cur < P;) {
         const int64_t next = std::min<int64_t>(P, std::max<int64_t>(cur + 1, (int64_t)std::ceil((double)cur * ap.growth)));
@@ -245,7 +260,7 @@ int execute_adaptive_t(gsea_plan_s* p, gsea_model model, const gsea_adaptive_par
     int64_t launches = 0;
     if (p->profile) {  // stage events between the launches: issued one by one
         p->events_used = 0;
-        if ((rc = record_adaptive<T>(p, model, use_model, rule, q_on, schedule, st))) return rc;
+        if ((rc = record_adaptive<T>(p, model, use_model, rule, bounds_on, schedule, st))) return rc;
         launches = gsea::launches_take();
     } else {
         if (!p->ad_exec || p->ad_key != key) {
@@ -254,7 +269,7 @@ int execute_adaptive_t(gsea_plan_s* p, gsea_model model, const gsea_adaptive_par
             p->ad_exec = nullptr;
             p->ad_graph = nullptr;
             GSEA_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
-            rc = record_adaptive<T>(p, model, use_model, rule, q_on, schedule, st);
+            rc = record_adaptive<T>(p, model, use_model, rule, bounds_on, schedule, st);
             cudaGraph_t g = nullptr;
             const cudaError_t e = cudaStreamEndCapture(st, &g);
             if (rc) {
@@ -303,6 +318,8 @@ int execute_adaptive_t(gsea_plan_s* p, gsea_model model, const gsea_adaptive_par
         report->prior_sets = (int64_t)ctl.prior_sets;
         report->prior_agreed = (int64_t)ctl.prior_agreed;
         report->stopped_q = (int64_t)ctl.stopped_q;
+        report->stopped_sig = (int64_t)ctl.stopped_sig;
+        report->p_sig = ctl.p_sig;
     }
     return GSEA_OK;
 }
@@ -322,6 +339,7 @@ void gsea_adaptive_params_init(gsea_adaptive_params* ap) {
     ap->prior_cap = 4.0;
     ap->fallback_tol = 0.25;
     ap->q_margin = 1.5;
+    ap->sig_margin = 2.0;
 }
 
 int gsea_adaptive_decide(int64_t num_sets, const int64_t* counts, const int64_t* exceed, const float* p_model,
@@ -370,7 +388,7 @@ int gsea_plan_execute_adaptive(gsea_plan p, gsea_model model, const gsea_adaptiv
     gsea_adaptive_params_init(&def);
     const gsea_adaptive_params& a = ap ? *ap : def;
     if (a.pilot_perms < 2 || !(a.growth > 1.0) || !(a.z >= 0.0) || !(a.margin > 0.0) || !(a.p_floor >= 0.0) ||
-        !(a.prior_cap >= 0.0) || !(a.q_call > 0.0) || !(a.q_margin >= 0.0))
+        !(a.prior_cap >= 0.0) || !(a.q_call > 0.0) || !(a.q_margin >= 0.0) || !(a.sig_margin >= 0.0))
         return fail(GSEA_ERR_INVALID_ARGUMENT, "invalid adaptive parameters");
     GSEA_CUDA(cudaSetDevice(p->device), "cudaSetDevice");
     return p->cfg.precision == 64 ? execute_adaptive_t<double>(p, model, a, counts, report)

@@ -101,7 +101,7 @@ void free_plan_buffers(gsea_plan_s* p) {
                     p->gene_t1, p->gene_t2, p->opA1, p->opA2, p->opB, p->dev_error, p->keys,
                     p->ranks, p->sorted, p->order, p->sort_scratch, p->es, p->stats, p->stats_scratch,
                     p->moments, p->active, p->counts, p->exceed, p->sumabs, p->qlow, p->feat, p->pred,
-                    p->stop, p->ad_err, p->ad_ctl};
+                    p->stop, p->ad_err, p->ad_ctl, p->qhigh};
     for (void* b : bufs)
         if (b) cudaFree(b);
     p->exprs = p->labels = nullptr;
@@ -128,6 +128,7 @@ void free_plan_buffers(gsea_plan_s* p) {
     p->stop = nullptr;
     p->ad_err = nullptr;
     p->ad_ctl = nullptr;
+    p->qhigh = nullptr;
 }
 
 void drop_graph(gsea_plan_s* p) {

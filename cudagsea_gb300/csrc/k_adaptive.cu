@@ -214,10 +214,11 @@ adaptive_prepare_kernel(int K, const T* __restrict__ stats, const float* __restr
                         const double* __restrict__ sumabs, AdaptiveRule rule, double* __restrict__ err,
                         AdaptiveCtl* __restrict__ ctl) {
     __shared__ double sh[32];
-    double pstar = 0.0, valid = 0.0, ok = 0.0;
+    double pstar = 0.0, plo = CUDART_INF, valid = 0.0, ok = 0.0;
     for (int k = threadIdx.x; k < K; k += blockDim.x) {
         const double q = (double)stats[4 * (size_t)K + k], np = (double)stats[2 * (size_t)K + k];
         if (q < rule.q_call && np > pstar) pstar = np;
+        if (!(q < rule.q_call) && np < plo) plo = np;  // the pilot's non-calls
         if (pred) {
             const double mt = (double)pred[2 * (size_t)k + 1], mh = sumabs[k] / (double)rule.P0;
             double e = CUDART_NAN;
@@ -230,10 +231,12 @@ adaptive_prepare_kernel(int K, const T* __restrict__ stats, const float* __restr
         }
     }
     pstar = block_max(pstar, sh);
+    plo = -block_max(-plo, sh);
     valid = block_sum(valid, sh);
     ok = block_sum(ok, sh);
     if (threadIdx.x == 0) {
         ctl->stop_p = fmin(1.0, fmax(rule.p_floor, rule.margin * pstar));
+        ctl->p_sig = rule.sig_margin > 0.0 ? plo / rule.sig_margin : 0.0;
         // the median error is within tolerance iff at least n/2 + 1 of the n errors are
         const unsigned long long nv = (unsigned long long)valid, nk = (unsigned long long)ok;
         ctl->model_used = (pred && nv > 0 && nk >= nv / 2 + 1) ? 1 : 0;
@@ -260,9 +263,9 @@ __device__ __forceinline__ bool prior_agrees_dev(double pm, double w, double n, 
 
 __global__ void adaptive_decide_kernel(int K, const int32_t* __restrict__ list, const int* __restrict__ n_dev,
                                        const int64_t* __restrict__ counts, const unsigned long long* __restrict__ exceed,
-                                       const float* __restrict__ pred, const float* __restrict__ qlow, int bound_on,
-                                       int pilot, AdaptiveRule rule, uint8_t* __restrict__ stop,
-                                       AdaptiveCtl* __restrict__ ctl) {
+                                       const float* __restrict__ pred, const float* __restrict__ qlow,
+                                       const float* __restrict__ qhigh, int bound_on, int pilot, AdaptiveRule rule,
+                                       uint8_t* __restrict__ stop, AdaptiveCtl* __restrict__ ctl) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n_list = list ? min(K, *n_dev) : K;
     if (i >= n_list) return;
@@ -288,8 +291,16 @@ __global__ void adaptive_decide_kernel(int K, const int32_t* __restrict__ list, 
         }
         const double t = a + b, mean = a / t, sd = sqrt(a * b / (t * t * (t + 1.0)));
         s = mean - rule.z * sd >= ctl->stop_p ? 1 : 0;
+        // clearly significant: p confidently below every pilot non-call's
+        // p (by sig_margin) and the q upper bound below the call level (by
+        // sig_margin)
+        if (!s && bound_on && qhigh && rule.sig_margin > 0.0 && counts[k] < rule.P &&
+            mean + rule.z * sd <= ctl->p_sig && (double)qhigh[k] <= rule.q_call / rule.sig_margin) {
+            s = 1;
+            atomicAdd(&ctl->stopped_sig, 1ull);
+        }
     }
-    if (bound_on && !s && counts[k] < rule.P && (double)qlow[k] >= rule.q_stop) {
+    if (bound_on && !s && rule.q_stop > 0.0 && counts[k] < rule.P && (double)qlow[k] >= rule.q_stop) {
         s = 1;
         atomicAdd(&ctl->stopped_q, 1ull);
     }
@@ -358,10 +369,10 @@ template cudaError_t launch_adaptive_prepare<double>(int, const double*, const f
 
 cudaError_t launch_adaptive_decide(int K, const int32_t* list, const int* n_dev, const int64_t* counts,
                                    const unsigned long long* exceed, const float* pred, const float* qlow,
-                                   bool bound_on, bool pilot, const AdaptiveRule& rule, uint8_t* stop,
-                                   AdaptiveCtl* ctl, cudaStream_t st) {
+                                   const float* qhigh, bool bound_on, bool pilot, const AdaptiveRule& rule,
+                                   uint8_t* stop, AdaptiveCtl* ctl, cudaStream_t st) {
     if (K <= 0) return cudaSuccess;
-    adaptive_decide_kernel<<<(K + 255) / 256, 256, 0, st>>>(K, list, n_dev, counts, exceed, pred, qlow,
+    adaptive_decide_kernel<<<(K + 255) / 256, 256, 0, st>>>(K, list, n_dev, counts, exceed, pred, qlow, qhigh,
                                                             bound_on ? 1 : 0, pilot ? 1 : 0, rule, stop, ctl);
     launches_add(1);
     return cudaGetLastError();

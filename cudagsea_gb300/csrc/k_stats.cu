@@ -492,11 +492,11 @@ __global__ void stats_fdr_bound_kernel(int K, const T* __restrict__ stats, const
                                        const double* __restrict__ sums, double z, const T* __restrict__ sorted_pos,
                                        const T* __restrict__ sorted_neg, const double* __restrict__ spos,
                                        const double* __restrict__ sneg, const unsigned long long* __restrict__ totals,
-                                       float* __restrict__ qlow) {
+                                       float* __restrict__ qlow, float* __restrict__ qhigh) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= K) return;
     const double s = (double)stats[K + k];
-    float out = 0.f;
+    float out = 0.f, out_hi = 1.f;
     const double n = (double)counts[k];
     if (s == s && s != 0.0 && n > 0) {
         const bool up = s > 0.0;
@@ -522,27 +522,40 @@ __global__ void stats_fdr_bound_kernel(int K, const T* __restrict__ stats, const
             const double obs = (double)(mcount - i_lo > 0 ? mcount - i_lo : 1u);
             const double r = fn / (obs / (double)mcount);
             out = (float)(r < 1.0 ? r : 1.0);
+            if (qhigh) {
+                // upper bound: the most null weight (at the interval's bottom,
+                // |NES| pulled inward) over the fewest observed keys (at or
+                // above its top; the set's own key is one of them)
+                const double key_in = fabs(s) * fmax(1.0 - z * cv / sqrt(n), 0.0);
+                const unsigned j_in = below(key_in);
+                const double c_in = j_in <= mcount ? (up ? spos : sneg)[j_in] : 0.0;
+                const double fn_hi = wtot > 0.0 ? c_in / wtot : 1.0;
+                const double obs_hi = (double)(mcount - i_up > 0 ? mcount - i_up : 1u);
+                const double rh = fn_hi / (obs_hi / (double)mcount);
+                out_hi = (float)(rh < 1.0 ? rh : 1.0);
+            }
         }
     }
     qlow[k] = out;
+    if (qhigh) qhigh[k] = out_hi;
 }
 
 }  // namespace
 
 template <class T>
 cudaError_t launch_fdr_bound(int K, int64_t p_fwer, const T* stats, const int64_t* counts, const double* sums,
-                             double z, const void* scratch, float* qlow, cudaStream_t st) {
+                             double z, const void* scratch, float* qlow, cudaStream_t st, float* qhigh) {
     if (K <= 0) return cudaSuccess;
     const RaggedLayout<T> L(const_cast<void*>(scratch), K, p_fwer);
     stats_fdr_bound_kernel<T><<<(K + 255) / 256, 256, 0, st>>>(K, stats, counts, sums, z, L.sorted_pos, L.sorted_neg,
-                                                               L.hpos, L.hneg, L.totals, qlow);
+                                                               L.hpos, L.hneg, L.totals, qlow, qhigh);
     launches_add(1);
     return cudaGetLastError();
 }
 template cudaError_t launch_fdr_bound<float>(int, int64_t, const float*, const int64_t*, const double*, double,
-                                             const void*, float*, cudaStream_t);
+                                             const void*, float*, cudaStream_t, float*);
 template cudaError_t launch_fdr_bound<double>(int, int64_t, const double*, const int64_t*, const double*, double,
-                                              const void*, float*, cudaStream_t);
+                                              const void*, float*, cudaStream_t, float*);
 
 template <class T>
 size_t stats_scratch_bytes(int K, int64_t P) {

@@ -150,7 +150,9 @@ cudaError_t launch_exceed(const T* es, int64_t ld, int K, const int32_t* list, i
 // of every set's FDR q with its NES pushed z standard errors outward
 template <class T>
 cudaError_t launch_fdr_bound(int K, int64_t p_fwer, const T* stats, const int64_t* counts, const double* sums,
-                             double z, const void* scratch, float* qlow, cudaStream_t st);
+                             double z, const void* scratch, float* qlow, cudaStream_t st, float* qhigh = nullptr);
+// (qhigh, may be null: an upper bound of every set's q with its NES pulled z
+// standard errors inward)
 
 // The adaptive test's decisions on the device (k_adaptive.cu): the pilot's
 // p threshold and model fallback test, the stopping rule per round, the list
@@ -161,6 +163,8 @@ struct AdaptiveCtl {
     int model_used;                   // 1: the model's prior enters the rule
     unsigned long long stopped_pilot;  // sets stopped after the pilot
     unsigned long long stopped_q;      // sets stopped by the FDR bound, any round
+    unsigned long long stopped_sig;    // sets stopped as clearly significant, any round
+    double p_sig;                      // p threshold of the significance rule (0: off)
     unsigned long long prior_sets;     // sets with a usable model prior
     unsigned long long prior_agreed;   // of those, pilots within z sd of the prior predictive
     unsigned long long rounds;         // rounds run, the pilot included
@@ -169,6 +173,7 @@ struct AdaptiveCtl {
 };
 struct AdaptiveRule {  // the rule's constants
     double q_call, margin, p_floor, z, q_stop, tol, cap, s2;  // s2: sigma_tail^2 of the model
+    double sig_margin;  // significance rule: q_high <= q_call / sig_margin, p_high <= p_sig (0: off)
     int64_t P, P0;
 };
 // pilot: stop_p = min(1, max(p_floor, margin * max{NP_k : FDR_k < q_call}))
@@ -181,8 +186,8 @@ cudaError_t launch_adaptive_prepare(int K, const T* stats, const float* pred, co
 // agreement and the sets stopped after the pilot
 cudaError_t launch_adaptive_decide(int K, const int32_t* list, const int* n_dev, const int64_t* counts,
                                    const unsigned long long* exceed, const float* pred, const float* qlow,
-                                   bool bound_on, bool pilot, const AdaptiveRule& rule, uint8_t* stop,
-                                   AdaptiveCtl* ctl, cudaStream_t st);
+                                   const float* qhigh, bool bound_on, bool pilot, const AdaptiveRule& rule,
+                                   uint8_t* stop, AdaptiveCtl* ctl, cudaStream_t st);
 // active list (ctl->n_active) = sets of `order` not stopped, in that order
 cudaError_t launch_adaptive_compact(int K, const int32_t* order, const uint8_t* stop, int32_t* active,
                                     AdaptiveCtl* ctl, cudaStream_t st);

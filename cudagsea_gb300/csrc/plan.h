@@ -89,6 +89,7 @@ struct gsea_plan_s {
     unsigned long long* exceed = nullptr;  // [K] #{|S| >= |ES|} per set
     double* sumabs = nullptr;          // [2K] sum of |S| per set, then sum of S^2 per set
     float* qlow = nullptr;             // [K] lower bound of each set's FDR q (adaptive stopping)
+    float* qhigh = nullptr;            // [K] upper bound of each set's FDR q (significance stopping)
     float* feat = nullptr;             // [K][5] model features
     float* pred = nullptr;             // [K][2] model predictions
     // the adaptive test on the device: per-set stop flags, the model's error

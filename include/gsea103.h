@@ -406,6 +406,12 @@ typedef struct gsea_adaptive_params {
     double fallback_tol; /* model dropped if its median |log m~ - log m^| on the pilot exceeds (0.25) */
     double q_margin;     /* also stop a set once a lower bound of its FDR q (NES pushed z standard
                             errors outward) is >= q_margin * q_call; 0 turns this rule off (1.5) */
+    double sig_margin;   /* also stop a set as clearly significant once an upper bound of its FDR q
+                            (NES pulled z standard errors inward) is <= q_call / sig_margin and the
+                            upper bound of its nominal p (posterior mean + z sd, with the model's prior
+                            where it applies) is <= p_sig = (smallest pilot p among the pilot's
+                            non-calls) / sig_margin; its reported NES, NP and FDR then come from the
+                            permutations it received; 0 turns this rule off (2) */
 } gsea_adaptive_params;
 void gsea_adaptive_params_init(gsea_adaptive_params* ap);
 typedef struct gsea_adaptive_report {
@@ -419,17 +425,24 @@ typedef struct gsea_adaptive_report {
     int64_t prior_sets;      /* sets with a finite model prior (model_used) */
     int64_t prior_agreed;    /* of those, sets whose pilot agreed with the prior (kept at the pilot decision) */
     int64_t stopped_q;       /* sets stopped by the FDR bound (q_margin), any round */
+    int64_t stopped_sig;     /* sets stopped as clearly significant (sig_margin), any round */
+    double p_sig;            /* p threshold of the significance rule (0: rule off) */
 } gsea_adaptive_report;
 /* Adaptive permutation test on the plan's inputs, num_perms permutations at
  * most per set: a pilot of pilot_perms permutations for every set, then
- * rounds of growing permutation counts for the sets the rule keeps.  The
+ * rounds of growing permutation counts for the sets the rules keep (the p
+ * rule, the FDR bound q_margin, the significance rule sig_margin).  The
  * plan's ES rows hold counts[k] scores each (the rest of a row is left as
  * it was); its statistics are the ragged statistics of those rows (FWER over
  * the pilot permutations).  model may be NULL (empirical rule only).
- * counts (host, K) and report may be NULL.  Requires perm_offset 0. */
+ * counts (host, K) and report may be NULL.  Requires perm_offset 0.  The
+ * whole test runs as one CUDA graph on the plan's stream (recorded on the
+ * first call with given parameters and model, replayed after): the
+ * decisions are kernels and the host waits only for the report.  The first
+ * call therefore belongs outside any stream capture of the caller's. */
 int gsea_plan_execute_adaptive(gsea_plan p, gsea_model model, const gsea_adaptive_params* ap, int64_t* counts,
                                gsea_adaptive_report* report);
-/* The stopping rule alone (host arrays, no device): set k (counts[k] scores,
+/* The p rule alone (host arrays, no device): set k (counts[k] scores,
  * exceed[k] of them with |S| >= |ES_k|) stops when the Beta posterior
  * Beta(a0 + exceed, b0 + counts - exceed) has mean - z * sd >= stop_p, with
  * a0 = 0.5 + p_model[k] * prior[k], b0 = 0.5 + (1 - p_model[k]) * prior[k]

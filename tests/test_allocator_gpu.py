@@ -157,8 +157,9 @@ def check_against_full(d, res, es_full, st_full, plan):
     for k in flips:
         assert abs(st_full[4][k] - Q_CALL) <= Q_BAND, (k, st_full[4][k], st_a[4][k])
     assert len(flips) <= max(1, d.num_sets // 100), flips
-    # every called set ran the full test
-    assert np.all(counts[sorted(calls)] == P_MAX)
+    # every called set ran the full test or stopped as clearly significant
+    short_calls = [k for k in sorted(calls) if counts[k] < P_MAX]
+    assert len(short_calls) <= res.report["stopped_sig"], (short_calls, res.report)
     return res.report["scores"]
 
 
@@ -322,7 +323,8 @@ def test_adaptive_double_precision_matches_full_test(gpu):
     calls = set(np.where(st_a[4] < Q_CALL)[0])
     for k in sorted(calls ^ calls_f):
         assert abs(st_f[4][k] - Q_CALL) <= Q_BAND, (k, st_f[4][k], st_a[4][k])
-    assert np.all(counts[sorted(calls)] == P_MAX)
+    short_calls = [k for k in sorted(calls) if counts[k] < P_MAX]
+    assert len(short_calls) <= res.report["stopped_sig"], (short_calls, res.report)
 
 
 def test_adaptive_graph_replays_and_matches_the_host_rule(gpu):
@@ -334,17 +336,17 @@ def test_adaptive_graph_replays_and_matches_the_host_rule(gpu):
     d = case(seed=91)
     plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, P_MAX, "twopass_signal2noise")
     plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
-    a = allocator.execute_adaptive(plan, None, pilot_perms=250, q_margin=0.0)
+    a = allocator.execute_adaptive(plan, None, pilot_perms=250, q_margin=0.0, sig_margin=0.0)
     st_a = plan.read(es=False)[1]
-    b = allocator.execute_adaptive(plan, None, pilot_perms=250, q_margin=0.0)
+    b = allocator.execute_adaptive(plan, None, pilot_perms=250, q_margin=0.0, sig_margin=0.0)
     st_b = plan.read(es=False)[1]
     assert np.array_equal(a.counts, b.counts)
     assert all(a.report[k] == b.report[k] or (a.report[k] != a.report[k] and b.report[k] != b.report[k])
                for k in a.report)  # NaN (no model error) on both sides counts as equal
     assert np.array_equal(st_a.view(np.uint32), st_b.view(np.uint32))
-    c = allocator.execute_adaptive(plan, None, pilot_perms=500, q_margin=0.0)
+    c = allocator.execute_adaptive(plan, None, pilot_perms=500, q_margin=0.0, sig_margin=0.0)
     assert c.counts.min() >= 500 and not np.array_equal(c.counts, a.counts)
-    a2 = allocator.execute_adaptive(plan, None, pilot_perms=250, q_margin=0.0)
+    a2 = allocator.execute_adaptive(plan, None, pilot_perms=250, q_margin=0.0, sig_margin=0.0)
     assert np.array_equal(a2.counts, a.counts)
     # the host rule on the final state: every set that stopped short of P_MAX
     # is one the rule stops, given the run's own stop_p
@@ -354,3 +356,26 @@ def test_adaptive_graph_replays_and_matches_the_host_rule(gpu):
     short = a.counts < P_MAX
     assert np.all(stop[short] == 1)
     plan.close()
+
+
+def test_significance_rule_saves_scores_with_the_full_tests_calls(gpu):
+    """Stopping sets whose q is clearly below the call level (and whose p is
+    clearly below every pilot non-call's): the full test's calls, strictly
+    fewer scores than without the rule, every early-stopped call counted in
+    the report; with the learned prior on top, the calls stay the full
+    test's."""
+    d = case(seed=77)
+    plan_f, es_f, st_f = full_run(d)
+    plan_f.close()
+    scores, reports = {}, {}
+    for name, sm, model in (("off", 0.0, None), ("on", 2.0, None), ("learned", 2.0, trained_model())):
+        plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, P_MAX, "twopass_signal2noise")
+        plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+        res = allocator.execute_adaptive(plan, model, pilot_perms=250, sig_margin=sm)
+        scores[name] = check_against_full(d, res, es_f, st_f, plan)
+        reports[name] = res.report
+        plan.close()
+    assert reports["off"]["stopped_sig"] == 0 and reports["off"]["p_sig"] == 0.0
+    assert reports["on"]["stopped_sig"] > 0 and reports["on"]["p_sig"] > 0.0
+    assert scores["on"] < scores["off"], scores
+    assert reports["learned"]["model_used"] == 1
