@@ -156,12 +156,14 @@ def compare(d, cur: FormRun, ref: FormRun, nes_tol: float = NES_TOL, max_sets: i
         members = d.set_genes[d.set_offsets[k]:d.set_offsets[k + 1]]
         order_ok = True
         rank_moves = 0
+        mix_err = 0.0
         if moved.size:
             orders = cur.order.rows(moved)
             w64 = np.abs(ref.keys.rows(moved))
             orders_r = ref.order.rows(moved)
             for i, p in enumerate(moved):
                 e_mix = es_in_order(orders[i], w64[i], members, G)
+                mix_err = max(mix_err, abs(e_mix - es_c[k, p]))
                 if not abs(e_mix - es_c[k, p]) <= ES_ROUND:
                     order_ok = False
                 pc = np.empty(G, np.int64)
@@ -177,6 +179,7 @@ def compare(d, cur: FormRun, ref: FormRun, nes_tol: float = NES_TOL, max_sets: i
         traced.append({"set": int(k), "dNES": float(dnes[k]), "moved_perms": int(moved.size),
                        "observed_moved": bool(0 in moved), "member_rank_moves": rank_moves,
                        "order_explained": bool(order_ok), "residual_dNES": float(residual),
+                       "max_order_mismatch": float(mix_err),
                        "tie_explained": explained})
     if over.size > max_sets:
         explained_all = False  # untraced sets count as unexplained

@@ -74,6 +74,7 @@ def main(argv=None) -> int:
     ap.add_argument("--perms", type=int, default=10000)
     ap.add_argument("--sample", type=int, default=64, help="permutations whose rank orders are compared")
     ap.add_argument("--json", default="")
+    ap.add_argument("--metrics", default="", help="comma-separated metric names (default: all 14)")
     a = ap.parse_args(argv)
     build.build()
     d = workload(a.perms)
@@ -106,9 +107,13 @@ def main(argv=None) -> int:
             cur.close()
         return {"sets_dNES_over_1e-4": rep["sets_over_tol"], "all_tie_explained": rep["all_tie_explained"],
                 "traced_not_explained": sum(1 for e in rep["exceedances"] if not e["tie_explained"]),
+                "not_explained": [e for e in rep["exceedances"] if not e["tie_explained"]][:5],
                 "fdr_call_diffs": rep["fdr_call_diffs"]}
 
+    chosen_names = [x for x in a.metrics.split(",") if x] or api.METRICS
     for m, name in enumerate(api.METRICS):
+        if name not in chosen_names:
+            continue
         ref = run(d, m, 64, N.FORM_PLAIN, a.sample)
         tensor = compare(*run(d, m, 32, N.FORM_CHOSEN, a.sample), *ref)
         tensor64 = compare(*run(d, m, 32, N.FORM_CHOSEN_FP64, a.sample), *ref)
