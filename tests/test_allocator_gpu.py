@@ -138,12 +138,12 @@ def check_against_full(d, res, es_full, st_full, plan):
     es_a, st_a = plan.read()
     st_a = st_a.reshape(5, -1)
     counts = res.counts
-    assert counts.min() >= 250 and counts.max() <= P_MAX
+    assert counts.min() >= 250 and counts.max() <= d.num_perms
     # every score a set received is the full run's score of that permutation
     for k in range(d.num_sets):
         assert np.array_equal(es_a[k, :counts[k]].view(np.uint32), es_full[k, :counts[k]].view(np.uint32)), k
     # sets run to completion: ES, NES, NP identical to the full test
-    full = counts == P_MAX
+    full = counts == d.num_perms
     assert full.any()
     for r in (0, 1, 2):
         assert np.array_equal(st_a[r, full].view(np.uint32), st_full[r, full].view(np.uint32))
@@ -158,7 +158,7 @@ def check_against_full(d, res, es_full, st_full, plan):
         assert abs(st_full[4][k] - Q_CALL) <= Q_BAND, (k, st_full[4][k], st_a[4][k])
     assert len(flips) <= max(1, d.num_sets // 100), flips
     # every called set ran the full test or stopped as clearly significant
-    short_calls = [k for k in sorted(calls) if counts[k] < P_MAX]
+    short_calls = [k for k in sorted(calls) if counts[k] < d.num_perms]
     assert len(short_calls) <= res.report["stopped_sig"], (short_calls, res.report)
     return res.report["scores"]
 
@@ -363,13 +363,16 @@ def test_significance_rule_saves_scores_with_the_full_tests_calls(gpu):
     clearly below every pilot non-call's): the full test's calls, strictly
     fewer scores than without the rule, every early-stopped call counted in
     the report; with the learned prior on top, the calls stay the full
-    test's."""
-    d = case(seed=77)
-    plan_f, es_f, st_f = full_run(d)
+    test's.  16,000 permutations: enough rounds for the rule to act on the
+    Jeffreys posterior alone."""
+    P = 16000
+    d = synthetic.make(3000, 60, 400, P, seed=77, n_class_b=30, sd_range=(0.5, 2.5), n_shift=150,
+                       shift_range=(0.2, 0.8), set_min=15, set_max=250, enriched_frac=0.1)
+    plan_f, es_f, st_f = full_run(d, P)
     plan_f.close()
     scores, reports = {}, {}
     for name, sm, model in (("off", 0.0, None), ("on", 2.0, None), ("learned", 2.0, trained_model())):
-        plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, P_MAX, "twopass_signal2noise")
+        plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, P, "twopass_signal2noise")
         plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
         res = allocator.execute_adaptive(plan, model, pilot_perms=250, sig_margin=sm)
         scores[name] = check_against_full(d, res, es_f, st_f, plan)

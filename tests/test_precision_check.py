@@ -91,3 +91,21 @@ def test_compare_explains_a_near_tie_swap_and_flags_a_wrong_score():
     assert rep2["sets_over_tol"] >= 1 and not rep2["all_tie_explained"]
     bad = {e["set"]: e for e in rep2["exceedances"]}
     assert bad[3]["moved_perms"] == 1 and not bad[3]["order_explained"]
+
+
+def test_sign_tie_of_the_extrema_is_explained():
+    """A score whose maximum and minimum tie in magnitude may come out with
+    either sign; a moved score of the same magnitude and the other sign is
+    explained, a different magnitude is not."""
+    d, keys, order, es, st = _case()
+    ref = _Run(es, st, keys, order)
+    k, p = 2, 0  # the observed score: its sign is the NES's
+    es_flip = es.copy()
+    es_flip[k, p] = -es[k, p]
+    rep = PC.compare(d, _Run(es_flip, oracle.stats(es_flip), keys, order), ref, nes_tol=1e-9)
+    tr = {e["set"]: e for e in rep["exceedances"]}
+    assert tr[k]["order_explained"] and tr[k]["sign_ties"] == 1
+    es_bad = es.copy()
+    es_bad[k, p] = -0.5 * es[k, p]
+    rep2 = PC.compare(d, _Run(es_bad, oracle.stats(es_bad), keys, order), ref, nes_tol=1e-9)
+    assert not {e["set"]: e for e in rep2["exceedances"]}[k]["order_explained"]
