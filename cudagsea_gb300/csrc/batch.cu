@@ -1,18 +1,27 @@
 // batch.cu -- many independent GSEA instances in one CUDA graph.
 //
 // No counterpart in the reference, which runs one problem per call
-// (src/cudaGSEA_wrapper.cu:179-401).  Per execute:
-//   1. every instance's permutation, metric and sort over all its
-//      permutations (its plan holds num_perms x num_genes buffers), the
-//      instances spread over a pool of streams, heaviest first on the least
-//      loaded stream;
-//   2. one persistent enrichment launch per size class (the bitmap words per
+// (src/cudaGSEA_wrapper.cu:179-401).  Per execute, every stage is one launch
+// over all instances (each instance's plan holds num_perms x num_genes
+// buffers), blockIdx.z naming the instance where the work is a grid:
+//   1. the label permutations of every instance: one launch;
+//   2. the metric: in the tensor-core form one launch each of the label
+//      operand and the tcgen05 class statistics per metric family (one
+//      family when all instances share a metric); the plain form per
+//      instance;
+//   3. the sort: one launch per register-resident class (ITEMS keys per
+//      thread, one CTA or a two-CTA cluster per permutation); instances
+//      beyond the register forms (G > 40,960 fp32 / 20,480 fp64) sort on
+//      their own;
+//   4. one persistent enrichment launch per size class (the bitmap words per
 //      lane of the register procedure, fixed by G): its CTAs pull
 //      (instance, permutation) items from a global counter, heaviest
 //      instances first, so uneven instances keep every SM busy to the end;
-//   3. every instance's statistics, again over the stream pool.
-// The first execute captures the three phases into one CUDA graph (fork and
-// join through events); later executes replay the instantiated graph.
+//   5. the statistics of every instance: one launch per step (nine), the
+//      instances whose FDR histogram does not fit shared memory on their own.
+// Every instance's results are those of its solo plan bit for bit.  The
+// first execute captures the stages into one CUDA graph; later executes
+// replay it.
 #include <algorithm>
 #include <map>
 #include <new>
@@ -24,6 +33,14 @@
 
 namespace {
 using gsea::fail;
+
+// one multi-instance launch: its device task table and a host copy
+template <class Task>
+struct Multi {
+    int key = 0;                 // metric family / sort class
+    std::vector<Task> h;
+    Task* d = nullptr;
+};
 
 struct EsClass {
     int wpl = 0;
@@ -47,6 +64,14 @@ struct gsea_batch_s {
     std::vector<EsClass> classes;
     std::map<int, gsea::EsTuning> es_tuning;  // per size class
     unsigned long long* d_counters = nullptr;
+    // the multi-instance launches of the other stages (built with the classes)
+    Multi<gsea::PermTask> perm;
+    std::vector<Multi<gsea::ChosenTask>> chosen;
+    std::vector<Multi<gsea::SortTask>> sorts;
+    std::vector<int64_t> solo_sort;   // instances sorted on their own (tiled sort)
+    Multi<gsea::StatsTask<float>> stats32;
+    Multi<gsea::StatsTask<double>> stats64;
+    std::vector<int64_t> solo_stats;  // instances whose statistics run on their own
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     size_t nodes = 0;
@@ -63,6 +88,21 @@ void drop_graph(gsea_batch_s* b) {
     b->nodes = 0;
 }
 
+template <class Task>
+void free_multi(Multi<Task>& m) {
+    if (m.d) cudaFree(m.d);
+    m.d = nullptr;
+    m.h.clear();
+}
+
+template <class Task>
+cudaError_t upload_multi(Multi<Task>& m) {
+    if (m.h.empty()) return cudaSuccess;
+    cudaError_t e = cudaMalloc((void**)&m.d, sizeof(Task) * m.h.size());
+    if (e == cudaSuccess) e = cudaMemcpy(m.d, m.h.data(), sizeof(Task) * m.h.size(), cudaMemcpyHostToDevice);
+    return e;
+}
+
 void drop_classes(gsea_batch_s* b) {
     for (EsClass& c : b->classes) {
         if (c.d_tasks) cudaFree(c.d_tasks);
@@ -71,12 +111,109 @@ void drop_classes(gsea_batch_s* b) {
     b->classes.clear();
     if (b->d_counters) cudaFree(b->d_counters);
     b->d_counters = nullptr;
+    free_multi(b->perm);
+    for (auto& m : b->chosen) free_multi(m);
+    b->chosen.clear();
+    for (auto& m : b->sorts) free_multi(m);
+    b->sorts.clear();
+    b->solo_sort.clear();
+    free_multi(b->stats32);
+    free_multi(b->stats64);
+    b->solo_stats.clear();
 }
 
-// stage-1 cost model (metric ~ G*S*P, sort ~ G*P*passes) and ES cost (G*K*P)
-double front_cost(const gsea_config& c) {
-    return (double)c.num_genes * c.num_perms * ((double)c.num_samples / 8.0 + (c.precision == 64 ? 8.0 : 4.0));
+// the task tables of the multi-instance stages
+template <class T>
+int build_multi(gsea_batch_s* b, Multi<gsea::StatsTask<T>>& stats) {
+    const bool fp64 = b->precision == 64;
+    std::map<int, size_t> chosen_at, sort_at;
+    for (int64_t i = 0; i < (int64_t)b->plans.size(); i++) {
+        gsea_plan_s* p = b->plans[i];
+        const gsea_config& c = p->cfg;
+        gsea::PermTask pt;
+        pt.labels = p->labels;
+        pt.masks = p->masks;
+        pt.perm_offset = c.perm_offset;
+        pt.num_perms = c.num_perms;
+        pt.seed = c.seed;
+        pt.S = (int)c.num_samples;
+        pt.words = p->words;
+        b->perm.h.push_back(pt);
+        if (c.form != GSEA_FORM_PLAIN) {
+            gsea::ChosenTask ct;
+            ct.A1 = p->opA1;
+            ct.A2 = p->opA2;
+            ct.Bm = p->opB;
+            ct.mu = p->gene_mu;
+            ct.t1 = p->gene_t1;
+            ct.t2 = p->gene_t2;
+            ct.keys = static_cast<float*>(p->keys);
+            ct.masks = p->masks;
+            ct.error_flag = p->dev_error;
+            ct.nA = (float)p->nA;
+            ct.nB = (float)p->nB;
+            ct.G = (int)c.num_genes;
+            ct.S = (int)c.num_samples;
+            ct.num_perms = (int)c.num_perms;
+            ct.chunks = gsea::chosen_chunks(ct.S);
+            ct.words = p->words;
+            ct.comb = gsea::chosen_comb(c.metric);
+            auto it = chosen_at.find(ct.comb);
+            if (it == chosen_at.end()) {
+                it = chosen_at.emplace(ct.comb, b->chosen.size()).first;
+                b->chosen.emplace_back();
+                b->chosen.back().key = ct.comb;
+            }
+            b->chosen[it->second].h.push_back(ct);
+        }
+        const int cls = gsea::sort_multi_class((int)c.num_genes, fp64);
+        if (cls == 0 || !p->ranks16) {
+            b->solo_sort.push_back(i);
+        } else {
+            gsea::SortTask st;
+            st.keys = p->keys;
+            st.ranks = p->ranks;
+            st.sorted = p->sorted;
+            st.order = p->debug ? p->order : nullptr;
+            st.G = (int)c.num_genes;
+            st.num_perms = (int)c.num_perms;
+            st.descending = c.ascending ? 0 : 1;
+            auto it = sort_at.find(cls);
+            if (it == sort_at.end()) {
+                it = sort_at.emplace(cls, b->sorts.size()).first;
+                b->sorts.emplace_back();
+                b->sorts.back().key = cls;
+            }
+            b->sorts[it->second].h.push_back(st);
+        }
+        const int rows = gsea::stats_multi_rows<T>((int)c.num_sets, c.num_perms);
+        if (rows <= 0) {
+            b->solo_stats.push_back(i);
+        } else {
+            gsea::StatsTask<T> t;
+            t.es = static_cast<const T*>(p->es);
+            t.stats = static_cast<T*>(p->stats);
+            t.scratch = p->stats_scratch;
+            t.K = (int)c.num_sets;
+            t.rows = rows;
+            t.P = c.num_perms;
+            stats.h.push_back(t);
+        }
+    }
+    cudaError_t e = upload_multi(b->perm);
+    for (auto& m : b->chosen)
+        if (e == cudaSuccess) e = upload_multi(m);
+    for (auto& m : b->sorts)
+        if (e == cudaSuccess) e = upload_multi(m);
+    if (e == cudaSuccess) e = upload_multi(stats);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return gsea::cuda_fail(e, "batch task tables");
+    }
+    return GSEA_OK;
 }
+
+// enrichment cost of an instance (G*K*P), for the order of the persistent launch
 double es_cost(const gsea_config& c) {
     return (double)c.num_perms * c.num_sets * (double)(c.num_genes / 32 + 64);
 }
@@ -134,7 +271,8 @@ int build_classes(gsea_batch_s* b) {
         }
     }
     GSEA_CUDA(cudaMalloc((void**)&b->d_counters, sizeof(unsigned long long) * b->classes.size()), "batch counters");
-    return GSEA_OK;
+    if constexpr (sizeof(T) == 8) return build_multi<double>(b, b->stats64);
+    return build_multi<float>(b, b->stats32);
 }
 
 template <class T>
@@ -144,43 +282,40 @@ cudaError_t launch_class(gsea_batch_s* b, size_t ci, int64_t nitems, gsea::EsTun
                                     (int)cl.inst.size(), nitems, b->d_counters + ci, cl.Gmax, cl.wpl, tune, st);
 }
 
-// the whole execute on `main`, forking to and joining from the stream pool
+// the whole execute on `main`: one launch per stage over all instances
 template <class T>
 int record(gsea_batch_s* b) {
-    const size_t ns = b->streams.size();
     const int64_t n = (int64_t)b->plans.size();
-    cudaEvent_t* ev = b->events.data();  // [0] fork 1, [1..ns] join 1, [ns+1] fork 2, [ns+2..2ns+1] join 2
+    const bool fp64 = b->precision == 64;
+    cudaStream_t st = b->main;
     int rc;
-    GSEA_CUDA(cudaEventRecord(ev[0], b->main), "fork");
-    for (size_t s = 0; s < ns; s++) GSEA_CUDA(cudaStreamWaitEvent(b->streams[s], ev[0], 0), "fork");
-    std::vector<int64_t> order(n);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [b](int64_t x, int64_t y) {
-        return front_cost(b->plans[x]->cfg) > front_cost(b->plans[y]->cfg);
-    });
-    std::vector<double> load(ns, 0.0);
-    for (int64_t i : order) {
-        const size_t s = std::min_element(load.begin(), load.end()) - load.begin();
-        load[s] += front_cost(b->plans[i]->cfg);
-        if ((rc = gsea::plan_run_stage1(b->plans[i], b->streams[s]))) return rc;
+    GSEA_CUDA(gsea::launch_permute_multi(b->perm.d, b->perm.h.data(), (int)b->perm.h.size(), st), "batched permute");
+    if (b->plans[0]->cfg.form != GSEA_FORM_PLAIN) {
+        const bool fp64var = b->plans[0]->cfg.form == GSEA_FORM_CHOSEN_FP64;
+        for (auto& m : b->chosen)
+            GSEA_CUDA(gsea::launch_chosen_metric_multi(m.d, m.h.data(), (int)m.h.size(), fp64var, st),
+                      "batched tensor-core class statistics");
+    } else {
+        for (int64_t i = 0; i < n; i++)
+            if ((rc = gsea::plan_run_metric(b->plans[i], st))) return rc;
     }
-    for (size_t s = 0; s < ns; s++) {
-        GSEA_CUDA(cudaEventRecord(ev[1 + s], b->streams[s]), "join");
-        GSEA_CUDA(cudaStreamWaitEvent(b->main, ev[1 + s], 0), "join");
-    }
+    for (auto& m : b->sorts)
+        GSEA_CUDA(gsea::launch_sort_multi(m.d, (int)m.h.size(), m.key, fp64, st), "batched sort");
+    for (int64_t i : b->solo_sort)
+        if ((rc = gsea::plan_run_sort(b->plans[i], st))) return rc;
     for (size_t ci = 0; ci < b->classes.size(); ci++) {
         const auto it = b->es_tuning.find(b->classes[ci].wpl);
         const gsea::EsTuning tune = it == b->es_tuning.end() ? gsea::EsTuning() : it->second;
-        GSEA_CUDA(launch_class<T>(b, ci, b->classes[ci].nitems, tune, b->main), "batched enrichment kernel");
+        GSEA_CUDA(launch_class<T>(b, ci, b->classes[ci].nitems, tune, st), "batched enrichment kernel");
     }
-    GSEA_CUDA(cudaEventRecord(ev[ns + 1], b->main), "fork");
-    for (size_t s = 0; s < ns; s++) GSEA_CUDA(cudaStreamWaitEvent(b->streams[s], ev[ns + 1], 0), "fork");
-    for (int64_t i = 0; i < n; i++)
-        if ((rc = gsea::plan_run_stats(b->plans[i], b->streams[i % ns]))) return rc;
-    for (size_t s = 0; s < ns; s++) {
-        GSEA_CUDA(cudaEventRecord(ev[ns + 2 + s], b->streams[s]), "join");
-        GSEA_CUDA(cudaStreamWaitEvent(b->main, ev[ns + 2 + s], 0), "join");
-    }
+    if constexpr (sizeof(T) == 8)
+        GSEA_CUDA(gsea::launch_stats_multi<double>(b->stats64.d, b->stats64.h.data(), (int)b->stats64.h.size(), st),
+                  "batched statistics");
+    else
+        GSEA_CUDA(gsea::launch_stats_multi<float>(b->stats32.d, b->stats32.h.data(), (int)b->stats32.h.size(), st),
+                  "batched statistics");
+    for (int64_t i : b->solo_stats)
+        if ((rc = gsea::plan_run_stats(b->plans[i], st))) return rc;
     return GSEA_OK;
 }
 

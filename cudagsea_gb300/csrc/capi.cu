@@ -378,6 +378,44 @@ int plan_run_stage1(gsea_plan_s* p, cudaStream_t st) {
     return p->cfg.precision == 64 ? run_range_t<double>(p, st, 0, p->cfg.num_perms, nullptr, 0, false)
                                   : run_range_t<float>(p, st, 0, p->cfg.num_perms, nullptr, 0, false);
 }
+int plan_run_metric(gsea_plan_s* p, cudaStream_t st) {
+    const gsea_config& c = p->cfg;
+    const int G = (int)c.num_genes, S = (int)c.num_samples, n = (int)p->pb;
+    if (c.form != GSEA_FORM_PLAIN) {
+        GSEA_CUDA(gsea::launch_chosen_metric(c.metric, c.form == GSEA_FORM_CHOSEN_FP64, p->masks, p->words, G, S, n,
+                                             p->nA, p->nB, p->gene_mu, p->gene_t1, p->gene_t2, p->opA1, p->opA2,
+                                             p->opB, static_cast<float*>(p->keys), p->dev_error, st,
+                                             p->tuning.chosen_tile),
+                  "tensor-core class statistics");
+        return GSEA_OK;
+    }
+    cudaError_t e = c.precision == 64
+                        ? gsea::launch_metric<double>(c.metric, static_cast<const double*>(p->exprs), G, S, p->masks,
+                                                      p->words, n, p->nA, p->nB, static_cast<double*>(p->keys),
+                                                      p->fast_ok, st, p->tuning.metric_pb)
+                        : gsea::launch_metric<float>(c.metric, static_cast<const float*>(p->exprs), G, S, p->masks,
+                                                     p->words, n, p->nA, p->nB, static_cast<float*>(p->keys),
+                                                     p->fast_ok, st, p->tuning.metric_pb);
+    GSEA_CUDA(e, "metric kernel");
+    return GSEA_OK;
+}
+int plan_run_sort(gsea_plan_s* p, cudaStream_t st) {
+    const gsea_config& c = p->cfg;
+    gsea::SortBuffers sb;
+    sb.ranks = p->ranks;
+    sb.ranks16 = p->ranks16;
+    sb.sorted_abs = p->sorted;
+    sb.order = p->debug ? p->order : nullptr;
+    sb.scratch = p->sort_scratch;
+    sb.scratch_bytes = p->sort_scratch_bytes;
+    sb.variant = p->tuning.sort_variant;
+    const int G = (int)c.num_genes, n = (int)p->pb;
+    cudaError_t e = c.precision == 64
+                        ? gsea::launch_sort<double>(static_cast<const double*>(p->keys), G, n, c.ascending != 0, sb, st)
+                        : gsea::launch_sort<float>(static_cast<const float*>(p->keys), G, n, c.ascending != 0, sb, st);
+    GSEA_CUDA(e, "sort kernel");
+    return GSEA_OK;
+}
 int plan_run_stats(gsea_plan_s* p, cudaStream_t st) {
     const int K = (int)p->cfg.num_sets;
     const int64_t P = p->cfg.num_perms;

@@ -41,6 +41,7 @@
 // reference's fixlow floors) is then evaluated in FP32 on centred
 // differences.  The result is the metric of the FP32 inputs to ~1e-6
 // relative, not the reference's operation order: near-tied genes may swap.
+#include <algorithm>
 #include <cuda_bf16.h>
 
 #include <cstdint>
@@ -186,13 +187,14 @@ __device__ __forceinline__ float variance(float ms, float m) {
     return (ms - p) - e;
 }
 
+// one CTA = one tile of BM genes x TN permutations (gt, pt)
 template <int COMB, bool FP64SUB, int TN>
-__global__ void __launch_bounds__(THREADS, TN == 128 ? 2 : 1)
-class_stats_kernel(const unsigned char* __restrict__ A1, const unsigned char* __restrict__ A2,
-                   const unsigned char* __restrict__ B, int chunks, int G, int num_perms,
-                   const float* __restrict__ gene_mu, const double* __restrict__ gene_t1,
-                   const double* __restrict__ gene_t2, float nA, float nB, float* __restrict__ keys,
-                   int* __restrict__ error_flag) {
+__device__ __forceinline__ void
+class_stats_tile(int gt, int pt, const unsigned char* __restrict__ A1, const unsigned char* __restrict__ A2,
+                 const unsigned char* __restrict__ B, int chunks, int G, int num_perms,
+                 const float* __restrict__ gene_mu, const double* __restrict__ gene_t1,
+                 const double* __restrict__ gene_t2, float nA, float nB, float* __restrict__ keys,
+                 int* __restrict__ error_flag) {
     constexpr int STAGES = stages<TN>();
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ __align__(8) uint64_t bar_full[STAGES];
@@ -203,7 +205,6 @@ class_stats_kernel(const unsigned char* __restrict__ A1, const unsigned char* __
     constexpr int TSTAGE = stage_bytes<TN>();
     constexpr int TCOLS = 2 * TN;  // two FP32 accumulators of TN columns
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int gt = blockIdx.x, pt = blockIdx.y;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
@@ -329,6 +330,30 @@ class_stats_kernel(const unsigned char* __restrict__ A1, const unsigned char* __
         fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(TCOLS) : "memory");
     }
+}
+
+template <int COMB, bool FP64SUB, int TN>
+__global__ void __launch_bounds__(THREADS, TN == 128 ? 2 : 1)
+class_stats_kernel(const unsigned char* __restrict__ A1, const unsigned char* __restrict__ A2,
+                   const unsigned char* __restrict__ B, int chunks, int G, int num_perms,
+                   const float* __restrict__ gene_mu, const double* __restrict__ gene_t1,
+                   const double* __restrict__ gene_t2, float nA, float nB, float* __restrict__ keys,
+                   int* __restrict__ error_flag) {
+    class_stats_tile<COMB, FP64SUB, TN>(blockIdx.x, blockIdx.y, A1, A2, B, chunks, G, num_perms, gene_mu, gene_t1,
+                                        gene_t2, nA, nB, keys, error_flag);
+}
+
+// every instance of a batch at once: blockIdx.z = the instance; the tiles
+// beyond an instance's genes or permutations return before any TMEM
+// allocation or barrier
+template <int COMB, bool FP64SUB, int TN>
+__global__ void __launch_bounds__(THREADS, TN == 128 ? 2 : 1)
+class_stats_multi(const ChosenTask* __restrict__ tasks) {
+    const ChosenTask& t = tasks[blockIdx.z];
+    const int G = t.G, P = t.num_perms;
+    if ((int)blockIdx.x * BM >= G || (int)blockIdx.y * TN >= P) return;
+    class_stats_tile<COMB, FP64SUB, TN>(blockIdx.x, blockIdx.y, t.A1, t.A2, t.Bm, t.chunks, G, P, t.mu, t.t1, t.t2,
+                                        t.nA, t.nB, t.keys, t.error_flag);
 }
 
 // ---------------------------------------------------------------------------
@@ -470,11 +495,10 @@ __global__ void split_operands_kernel(const T* __restrict__ X, int G, int S, int
 // parts, in tiles of TN permutations; one thread per (permutation, sample);
 // the buffer is zeroed before.
 template <int TN>
-__global__ void label_operand_kernel(const uint32_t* __restrict__ masks, int words, int S, int num_perms,
-                                     int chunks, unsigned char* __restrict__ Bm) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    const int s = blockIdx.y;
-    if (p >= num_perms) return;
+__device__ __forceinline__ void label_operand_body(int bx, int s, const uint32_t* __restrict__ masks, int words,
+                                                   int S, int num_perms, int chunks, unsigned char* __restrict__ Bm) {
+    const int p = bx * blockDim.x + threadIdx.x;
+    if (p >= num_perms || s >= S) return;
     const bool a = (masks[(size_t)p * words + (s >> 5)] >> (s & 31)) & 1u;
     const __nv_bfloat16 v = __float2bfloat16(a ? 1.f : 0.f);
     const int pt = p / TN, row = p % TN;
@@ -483,6 +507,29 @@ __global__ void label_operand_kernel(const uint32_t* __restrict__ masks, int wor
         const int c = k / BK, kk = k % BK;
         *reinterpret_cast<__nv_bfloat16*>(Bm + ((size_t)pt * chunks + c) * (TN * BK * 2) + core_offset(row, kk)) = v;
     }
+}
+
+template <int TN>
+__global__ void label_operand_kernel(const uint32_t* __restrict__ masks, int words, int S, int num_perms,
+                                     int chunks, unsigned char* __restrict__ Bm) {
+    label_operand_body<TN>(blockIdx.x, blockIdx.y, masks, words, S, num_perms, chunks, Bm);
+}
+
+template <int TN>
+__global__ void label_operand_multi(const ChosenTask* __restrict__ tasks) {
+    const ChosenTask& t = tasks[blockIdx.z];
+    label_operand_body<TN>(blockIdx.x, blockIdx.y, t.masks, t.words, t.S, t.num_perms, t.chunks, t.Bm);
+}
+
+// the B operand of every instance cleared (16-byte stores; a buffer is a
+// whole number of TN x BK x 2-byte chunks)
+template <int TN>
+__global__ void zero_b_multi(const ChosenTask* __restrict__ tasks) {
+    const ChosenTask& t = tasks[blockIdx.z];
+    const size_t n16 = (size_t)((t.num_perms + TN - 1) / TN) * t.chunks * (TN * BK * 2) / 16;
+    uint4* b = reinterpret_cast<uint4*>(t.Bm);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x)
+        b[i] = make_uint4(0u, 0u, 0u, 0u);
 }
 
 }  // namespace chosen
@@ -546,12 +593,55 @@ cudaError_t launch_chosen_tn(int comb, bool fp64_variance, const uint32_t* masks
 }
 }  // namespace
 
+int chosen_comb(int metric) {
+    return metric == 0 || metric == 3 ? 0 : metric == 1 || metric == 4 ? 1 : metric == 2 || metric == 5 ? 2
+         : (metric == 6 || metric == 8 || metric == 10 || metric == 12) ? 3 : 4;
+}
+
+cudaError_t launch_chosen_metric_multi(const ChosenTask* d_tasks, const ChosenTask* h_tasks, int n,
+                                       bool fp64_variance, cudaStream_t st) {
+    using namespace chosen;
+    constexpr int TN = 128;
+    if (n <= 0) return cudaSuccess;
+    if (n > 65535) return cudaErrorInvalidValue;
+    int gmax = 0, pmax = 0, smax = 0;
+    for (int i = 0; i < n; i++) {
+        const ChosenTask& t = h_tasks[i];
+        if (t.comb != h_tasks[0].comb) return cudaErrorInvalidValue;  // one metric family per launch
+        gmax = std::max(gmax, t.G);
+        pmax = std::max(pmax, t.num_perms);
+        smax = std::max(smax, t.S);
+    }
+    const unsigned z = (unsigned)n;
+    zero_b_multi<TN><<<dim3(152, 1, z), 256, 0, st>>>(d_tasks);
+    label_operand_multi<TN><<<dim3((unsigned)((pmax + 127) / 128), (unsigned)smax, z), 128, 0, st>>>(d_tasks);
+    const dim3 grid((unsigned)((gmax + BM - 1) / BM), (unsigned)((pmax + TN - 1) / TN), z);
+    const size_t smem = (size_t)stages<TN>() * stage_bytes<TN>();
+    cudaError_t e = cudaSuccess;
+#define GSEA_CHOSEN_MULTI(C)                                                                                    \
+    {                                                                                                           \
+        auto kern = fp64_variance ? class_stats_multi<C, true, TN> : class_stats_multi<C, false, TN>;          \
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);                 \
+        if (e != cudaSuccess) return e;                                                                         \
+        kern<<<grid, THREADS, smem, st>>>(d_tasks);                                                             \
+    }
+    switch (h_tasks[0].comb) {
+        case 0: GSEA_CHOSEN_MULTI(0) break;
+        case 1: GSEA_CHOSEN_MULTI(1) break;
+        case 2: GSEA_CHOSEN_MULTI(2) break;
+        case 3: GSEA_CHOSEN_MULTI(3) break;
+        default: GSEA_CHOSEN_MULTI(4) break;
+    }
+#undef GSEA_CHOSEN_MULTI
+    launches_add(3);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_chosen_metric(int metric, bool fp64_variance, const uint32_t* masks, int words, int G, int S,
                                  int num_perms, int64_t nA, int64_t nB, const float* mu, const double* t1,
                                  const double* t2, const unsigned char* A1, const unsigned char* A2,
                                  unsigned char* Bm, float* keys, int* error_flag, cudaStream_t st, int tile_n) {
-    const int comb = metric == 0 || metric == 3 ? 0 : metric == 1 || metric == 4 ? 1 : metric == 2 || metric == 5 ? 2
-                   : (metric == 6 || metric == 8 || metric == 10 || metric == 12) ? 3 : 4;
+    const int comb = chosen_comb(metric);
     // default (0): the 128-permutation tile, two CTAs per SM
     if (tile_n == 0 || tile_n == 128)
         return launch_chosen_tn<128>(comb, fp64_variance, masks, words, G, S, num_perms, nA, nB, mu, t1, t2, A1, A2,

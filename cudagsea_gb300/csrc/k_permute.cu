@@ -57,12 +57,12 @@ constexpr int kPermThreads = 32;
 
 // one thread per permutation; the label vector of each thread lives in
 // shared memory, interleaved by thread
-__global__ void __launch_bounds__(kPermThreads)
-permute_kernel(const uint8_t* __restrict__ labels, int S, int64_t num_perms, int64_t perm_offset,
-               uint32_t seed, uint32_t* __restrict__ masks, int words) {
+__device__ __forceinline__ void permute_body(int64_t bx, const uint8_t* __restrict__ labels, int S, int64_t num_perms,
+                                             int64_t perm_offset, uint32_t seed, uint32_t* __restrict__ masks,
+                                             int words) {
     extern __shared__ uint8_t lab[];  // [S][kPermThreads]
     const int t = threadIdx.x;
-    const int64_t p = (int64_t)blockIdx.x * kPermThreads + t;
+    const int64_t p = bx * kPermThreads + t;
     for (int s = 0; s < S; s++) lab[s * kPermThreads + t] = labels[s];
     if (p >= num_perms) return;
     const uint64_t q = (uint64_t)(perm_offset + p);
@@ -86,6 +86,19 @@ permute_kernel(const uint8_t* __restrict__ labels, int S, int64_t num_perms, int
             m |= (uint32_t)(lab[s * kPermThreads + t] == 0) << (s - w * 32);
         out[w] = m;
     }
+}
+
+__global__ void __launch_bounds__(kPermThreads)
+permute_kernel(const uint8_t* __restrict__ labels, int S, int64_t num_perms, int64_t perm_offset,
+               uint32_t seed, uint32_t* __restrict__ masks, int words) {
+    permute_body(blockIdx.x, labels, S, num_perms, perm_offset, seed, masks, words);
+}
+
+// every instance of a batch at once: blockIdx.z = the instance
+__global__ void __launch_bounds__(kPermThreads) permute_multi(const PermTask* __restrict__ tasks) {
+    const PermTask t = tasks[blockIdx.z];
+    if ((int64_t)blockIdx.x * kPermThreads >= t.num_perms) return;
+    permute_body(blockIdx.x, t.labels, t.S, t.num_perms, t.perm_offset, t.seed, t.masks, t.words);
 }
 
 // fast_ok stays 1 unless some value is not finite or has |x| >= 2^60
@@ -126,6 +139,25 @@ cudaError_t launch_permute(const uint8_t* labels, int S, int64_t num_perms, int6
     const int64_t blocks = (num_perms + kPermThreads - 1) / kPermThreads;
     permute_kernel<<<(unsigned)blocks, kPermThreads, smem, st>>>(labels, S, num_perms, perm_offset,
                                                                seed, masks, words);
+    launches_add(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_permute_multi(const PermTask* d_tasks, const PermTask* h_tasks, int n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (n > 65535) return cudaErrorInvalidValue;
+    int64_t pmax = 0;
+    int smax = 0;
+    for (int i = 0; i < n; i++) {
+        pmax = pmax > h_tasks[i].num_perms ? pmax : h_tasks[i].num_perms;
+        smax = smax > h_tasks[i].S ? smax : h_tasks[i].S;
+    }
+    const size_t smem = (size_t)smax * kPermThreads;
+    if (smem > 200 * 1024) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(permute_multi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int64_t blocks = (pmax + kPermThreads - 1) / kPermThreads;
+    permute_multi<<<dim3((unsigned)blocks, 1, (unsigned)n), kPermThreads, smem, st>>>(d_tasks);
     launches_add(1);
     return cudaGetLastError();
 }

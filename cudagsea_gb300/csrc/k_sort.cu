@@ -148,9 +148,9 @@ __device__ __forceinline__ uint32_t cnt16_add(uint32_t* words, uint32_t dig, uin
 // each (key, gene id) pair as one 8-byte slot through the exchange buffer:
 // one scatter, one gather, two barriers.
 template <class T, class RankT, int ITEMS>
-__global__ void __launch_bounds__(kThreads, 1)
-sort_regs_kernel(const T* __restrict__ keys, int G, int num_perms, bool descending,
-                 RankT* __restrict__ ranks, T* __restrict__ sorted_abs, uint32_t* __restrict__ order) {
+__device__ __forceinline__ void
+sort_regs_body(int bx, int gx, const T* __restrict__ keys, int G, int num_perms, bool descending,
+               RankT* __restrict__ ranks, T* __restrict__ sorted_abs, uint32_t* __restrict__ order) {
     using U = typename RadixKey<T>::U;
     static_assert(sizeof(U) == 4, "register sort: fp32 keys");
     constexpr int TILE = kThreads * ITEMS;
@@ -169,7 +169,7 @@ sort_regs_kernel(const T* __restrict__ keys, int G, int num_perms, bool descendi
     if (threadIdx.x == 0) *flag = 0u;
     __syncthreads();
 
-    for (int p = blockIdx.x; p < num_perms; p += gridDim.x) {
+    for (int p = bx; p < num_perms; p += gx) {
         const T* kp = keys + (int64_t)p * G;
         U key[ITEMS];
         uint32_t val[ITEMS];
@@ -262,6 +262,23 @@ sort_regs_kernel(const T* __restrict__ keys, int G, int num_perms, bool descendi
     }
 }
 
+template <class T, class RankT, int ITEMS>
+__global__ void __launch_bounds__(kThreads, 1)
+sort_regs_kernel(const T* __restrict__ keys, int G, int num_perms, bool descending,
+                 RankT* __restrict__ ranks, T* __restrict__ sorted_abs, uint32_t* __restrict__ order) {
+    sort_regs_body<T, RankT, ITEMS>(blockIdx.x, gridDim.x, keys, G, num_perms, descending, ranks, sorted_abs, order);
+}
+
+// every instance of a batch (same ITEMS class) at once: blockIdx.z = the
+// instance, its gridDim.x CTAs share its permutations
+template <class T, class RankT, int ITEMS>
+__global__ void __launch_bounds__(kThreads, 1) sort_regs_multi(const SortTask* __restrict__ tasks) {
+    const SortTask& t = tasks[blockIdx.z];
+    sort_regs_body<T, RankT, ITEMS>(blockIdx.x, gridDim.x, static_cast<const T*>(t.keys), t.G, t.num_perms,
+                                    t.descending != 0, static_cast<RankT*>(t.ranks), static_cast<T*>(t.sorted),
+                                    t.order);
+}
+
 template <class T, int ITEMS>
 size_t regs_smem_bytes() {
     return 10 * (size_t)kThreads * ITEMS + sizeof(uint16_t) * kWarps * 256 + sizeof(uint32_t) * (256 + 8 + 4);
@@ -285,9 +302,9 @@ template <class T, int ITEMS>
 constexpr bool cluster_packed() { return sizeof(typename RadixKey<T>::U) == 4 && ITEMS <= 16; }
 
 template <class T, class RankT, int ITEMS, int CL>
-__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kThreads, 1)
-sort_cluster_kernel(const T* __restrict__ keys, int G, int num_perms, bool descending,
-                    RankT* __restrict__ ranks, T* __restrict__ sorted_abs, uint32_t* __restrict__ order) {
+__device__ __forceinline__ void
+sort_cluster_body(int bx, int gx, const T* __restrict__ keys, int G, int num_perms, bool descending,
+                  RankT* __restrict__ ranks, T* __restrict__ sorted_abs, uint32_t* __restrict__ order) {
     using U = typename RadixKey<T>::U;
     constexpr bool PACK = cluster_packed<T, ITEMS>();
     using E = typename std::conditional<PACK, unsigned long long, U>::type;  // exchange slot
@@ -309,9 +326,9 @@ sort_cluster_kernel(const T* __restrict__ keys, int G, int num_perms, bool desce
     const uint32_t lt = lanemask_lt();
     const int my0 = warp * 32 * ITEMS + lane;  // slot of item i: my0 + 32*i
     const int first = rank * TILE;              // global position of slot 0
-    const int clusters = gridDim.x / CL;
+    const int clusters = gx / CL;
 
-    for (int p = blockIdx.x / CL; p < num_perms; p += clusters) {
+    for (int p = bx / CL; p < num_perms; p += clusters) {
         const T* kp = keys + (int64_t)p * G;
         U key[ITEMS];
         uint32_t val[ITEMS];
@@ -438,6 +455,23 @@ sort_cluster_kernel(const T* __restrict__ keys, int G, int num_perms, bool desce
         for (int g = first + threadIdx.x; g < g_end; g += kThreads) ranks[obase + g] = s_rk[g - first];
         cluster.sync();  // the staging is reused by the next permutation
     }
+}
+
+template <class T, class RankT, int ITEMS, int CL>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kThreads, 1)
+sort_cluster_kernel(const T* __restrict__ keys, int G, int num_perms, bool descending,
+                    RankT* __restrict__ ranks, T* __restrict__ sorted_abs, uint32_t* __restrict__ order) {
+    sort_cluster_body<T, RankT, ITEMS, CL>(blockIdx.x, gridDim.x, keys, G, num_perms, descending, ranks, sorted_abs,
+                                           order);
+}
+
+template <class T, class RankT, int ITEMS, int CL>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kThreads, 1)
+sort_cluster_multi(const SortTask* __restrict__ tasks) {
+    const SortTask& t = tasks[blockIdx.z];
+    sort_cluster_body<T, RankT, ITEMS, CL>(blockIdx.x, gridDim.x, static_cast<const T*>(t.keys), t.G, t.num_perms,
+                                           t.descending != 0, static_cast<RankT*>(t.ranks), static_cast<T*>(t.sorted),
+                                           t.order);
 }
 
 template <class T, int ITEMS>
@@ -664,7 +698,70 @@ cudaError_t launch_sort_t(const T* keys, int G, int P, bool desc, const SortBuff
     return cudaGetLastError();
 }
 
+template <class T, class RankT, int ITEMS>
+cudaError_t launch_regs_multi(const SortTask* d, int n, cudaStream_t st) {
+    const size_t smem = regs_smem_bytes<T, ITEMS>();
+    auto kern = sort_regs_multi<T, RankT, ITEMS>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int per = (2 * num_sms() + n - 1) / n;  // CTAs per instance: about two waves over the SMs in all
+    kern<<<dim3((unsigned)(per > 0 ? per : 1), 1, (unsigned)n), kThreads, smem, st>>>(d);
+    launches_add(1);
+    return cudaGetLastError();
+}
+
+template <class T, class RankT, int ITEMS, int CL>
+cudaError_t launch_cluster_multi(const SortTask* d, int n, cudaStream_t st) {
+    const size_t smem = cluster_smem_bytes<T, ITEMS>();
+    auto kern = sort_cluster_multi<T, RankT, ITEMS, CL>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int per = (2 * num_sms() / CL + n - 1) / n;  // clusters per instance
+    kern<<<dim3((unsigned)(CL * (per > 0 ? per : 1)), 1, (unsigned)n), kThreads, smem, st>>>(d);
+    launches_add(1);
+    return cudaGetLastError();
+}
+
 }  // namespace
+
+int sort_multi_class(int G, bool fp64) {
+    if (G <= 0 || G > 65536) return 0;
+    if (!fp64) {
+        for (int items : {4, 8, 12, 16, 20})
+            if (G <= kThreads * items) return items;
+        if (G <= 2 * kThreads * 16) return 116;
+        if (G <= 2 * kThreads * 20) return 120;
+        return 0;
+    }
+    if (G <= kThreads * 4) return 204;
+    if (G <= kThreads * 10) return 210;
+    if (G <= 2 * kThreads * 10) return 310;
+    return 0;
+}
+
+cudaError_t launch_sort_multi(const SortTask* d_tasks, int n, int cls, bool fp64, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (n > 65535) return cudaErrorInvalidValue;
+    using R = uint16_t;  // batch instances have at most 65,536 genes
+    if (!fp64) {
+        switch (cls) {
+            case 4: return launch_regs_multi<float, R, 4>(d_tasks, n, st);
+            case 8: return launch_regs_multi<float, R, 8>(d_tasks, n, st);
+            case 12: return launch_regs_multi<float, R, 12>(d_tasks, n, st);
+            case 16: return launch_regs_multi<float, R, 16>(d_tasks, n, st);
+            case 20: return launch_regs_multi<float, R, 20>(d_tasks, n, st);
+            case 116: return launch_cluster_multi<float, R, 16, 2>(d_tasks, n, st);
+            case 120: return launch_cluster_multi<float, R, 20, 2>(d_tasks, n, st);
+            default: return cudaErrorInvalidValue;
+        }
+    }
+    switch (cls) {
+        case 204: return launch_cluster_multi<double, R, 4, 1>(d_tasks, n, st);
+        case 210: return launch_cluster_multi<double, R, 10, 1>(d_tasks, n, st);
+        case 310: return launch_cluster_multi<double, R, 10, 2>(d_tasks, n, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
 
 template <class T>
 size_t sort_scratch_bytes(int G, int num_perms) {

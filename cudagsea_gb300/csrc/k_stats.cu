@@ -24,6 +24,7 @@
 // in the FDR null every set carries the same total weight, each of its
 // n_k - 1 null scores counting (ld - 1) / (n_k - 1).  With n_k = ld for all
 // sets the weights are exactly 1 and the ragged form is the dense one.
+#include <algorithm>
 #include "common.cuh"
 #include "kernels.h"
 
@@ -40,9 +41,9 @@ struct StatsScratch {
 
 // one warp per set: factor, NES, NP
 template <class T>
-__global__ void stats_set_kernel(const T* __restrict__ es, int K, int64_t ld, const int64_t* __restrict__ counts,
+__device__ __forceinline__ void stats_set_kernel_body(int bx, const T* __restrict__ es, int K, int64_t ld, const int64_t* __restrict__ counts,
                                  T* __restrict__ out, T* __restrict__ fac) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    const int warp = (bx * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= K) return;
     const T* row = es + (int64_t)warp * ld;
     const int64_t P = counts ? counts[warp] : ld;
@@ -97,13 +98,13 @@ __global__ void stats_set_kernel(const T* __restrict__ es, int K, int64_t ld, co
 // max) and all-ones ("empty" for the min) belong only to NaN bit patterns.
 constexpr int kExtremaSets = 16;
 template <class T>
-__global__ void stats_extrema_kernel(const T* __restrict__ es, int K, int64_t ld, int64_t P, const T* __restrict__ fac,
+__device__ __forceinline__ void stats_extrema_kernel_body(int bx, int by, const T* __restrict__ es, int K, int64_t ld, int64_t P, const T* __restrict__ fac,
                                      typename RadixKey<T>::U* __restrict__ mx,
                                      typename RadixKey<T>::U* __restrict__ mn) {
     using U = typename RadixKey<T>::U;
-    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t p = (int64_t)bx * blockDim.x + threadIdx.x;
     if (p >= P) return;
-    const int k0 = blockIdx.y * kExtremaSets, k1 = min(K, k0 + kExtremaSets);
+    const int k0 = by * kExtremaSets, k1 = min(K, k0 + kExtremaSets);
     T hi = -INFINITY, lo = INFINITY;
     for (int k = k0; k < k1; k++) {
         const T v = Exact<T>::mul(es[(int64_t)k * ld + p], fac[k]);
@@ -129,9 +130,9 @@ __device__ __forceinline__ double radix_value<double>(unsigned long long u) {
 
 // one warp per set: FWER
 template <class T>
-__global__ void stats_fwer_kernel(int K, int64_t P, const typename RadixKey<T>::U* __restrict__ mx,
+__device__ __forceinline__ void stats_fwer_kernel_body(int bx, int K, int64_t P, const typename RadixKey<T>::U* __restrict__ mx,
                                   const typename RadixKey<T>::U* __restrict__ mn, T* __restrict__ out) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    const int warp = (bx * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= K) return;
     const T score = out[K + warp];
     unsigned long long c = 0;
@@ -169,10 +170,10 @@ __device__ __forceinline__ int side_of(T s) { return s > T(0) ? 0 : (s <= T(0) ?
 // one warp per set; the lanes stride over the other sets and the counts are
 // warp-reduced
 template <class T>
-__global__ void stats_fdr_obs_kernel(int K, const T* __restrict__ out, unsigned long long* __restrict__ cnt_obs,
+__device__ __forceinline__ void stats_fdr_obs_kernel_body(int bx, int K, const T* __restrict__ out, unsigned long long* __restrict__ cnt_obs,
                                      unsigned long long* __restrict__ lcount, T* __restrict__ sorted_pos,
                                      T* __restrict__ sorted_neg, unsigned long long* __restrict__ totals) {
-    const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    const int k = (bx * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (k >= K) return;
     const T s = out[K + k];
     // membership in the two sorted arrays: o >= 0 (positive), o <= 0 (negative)
@@ -299,8 +300,8 @@ constexpr int kDenseHistThreads = 512;
 constexpr size_t kDenseHistPartialBytes = size_t(1) << 20;
 constexpr size_t kDenseHistSmemMax = 96 * 1024;
 template <class T>
-__global__ void __launch_bounds__(kDenseHistThreads)
-stats_fdr_hist_dense_kernel(const T* __restrict__ es, int K, int64_t ld, const T* __restrict__ fac,
+__device__ __forceinline__ void
+stats_fdr_hist_dense_kernel_body(int bx, int gx, const T* __restrict__ es, int K, int64_t ld, const T* __restrict__ fac,
                             const T* __restrict__ sorted_pos, const T* __restrict__ sorted_neg,
                             const unsigned long long* __restrict__ totals, unsigned* __restrict__ partial) {
     extern __shared__ __align__(16) unsigned char dense_smem[];
@@ -315,7 +316,7 @@ stats_fdr_hist_dense_kernel(const T* __restrict__ es, int K, int64_t ld, const T
     __syncthreads();
     const int64_t cols = ld - 1;
     const int64_t total = (int64_t)K * cols;
-    const int64_t lo = total * blockIdx.x / gridDim.x, hi = total * (blockIdx.x + 1) / gridDim.x;
+    const int64_t lo = total * bx / gx, hi = total * (bx + 1) / gx;
     unsigned cpos = 0, cneg = 0;
     int64_t k = lo / cols;
     int64_t c = lo - k * cols;  // column - 1 within row k
@@ -348,16 +349,16 @@ stats_fdr_hist_dense_kernel(const T* __restrict__ es, int K, int64_t ld, const T
         if (cneg) atomicAdd(&h[W - 1], cneg);
     }
     __syncthreads();
-    unsigned* out = partial + (size_t)blockIdx.x * W;
+    unsigned* out = partial + (size_t)bx * W;
     for (int i = threadIdx.x; i < W; i += kDenseHistThreads) out[i] = h[i];
 }
 
 // column sums of the partial histograms: H_pos, H_neg (contiguous, 2(K+2)
 // doubles) and the null counts per side (totals[4], [5] as doubles)
-__global__ void stats_fdr_hist_sum_kernel(const unsigned* __restrict__ partial, int rows, int K,
+__device__ __forceinline__ void stats_fdr_hist_sum_kernel_body(int bx, const unsigned* __restrict__ partial, int rows, int K,
                                           double* __restrict__ hist, unsigned long long* __restrict__ totals) {
     const int W = 2 * (K + 2) + 2;
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = bx * blockDim.x + threadIdx.x;
     if (j >= W) return;
     unsigned long long s = 0;
     for (int r = 0; r < rows; r++) s += partial[(size_t)r * W + j];
@@ -381,10 +382,10 @@ int dense_hist_rows(int K, int sms) {
 }
 
 // in-place suffix sums of the two histograms (one block each)
-__global__ void stats_fdr_suffix_kernel(double* __restrict__ hpos, double* __restrict__ hneg,
+__device__ __forceinline__ void stats_fdr_suffix_kernel_body(int bx, double* __restrict__ hpos, double* __restrict__ hneg,
                                         const unsigned long long* __restrict__ totals) {
-    double* h = blockIdx.x == 0 ? hpos : hneg;
-    const unsigned n = (unsigned)totals[2 + blockIdx.x] + 1;  // bins 0..m
+    double* h = bx == 0 ? hpos : hneg;
+    const unsigned n = (unsigned)totals[2 + bx] + 1;  // bins 0..m
     __shared__ double carry;
     __shared__ double wsum[32];
     if (threadIdx.x == 0) carry = 0.0;
@@ -414,11 +415,11 @@ __global__ void stats_fdr_suffix_kernel(double* __restrict__ hpos, double* __res
 }
 
 template <class T>
-__global__ void stats_fdr_final_kernel(int K, const unsigned long long* __restrict__ cnt_obs,
+__device__ __forceinline__ void stats_fdr_final_kernel_body(int bx, int K, const unsigned long long* __restrict__ cnt_obs,
                                        const unsigned long long* __restrict__ lcount,
                                        const double* __restrict__ spos, const double* __restrict__ sneg,
                                        const unsigned long long* __restrict__ totals, T* __restrict__ out) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = bx * blockDim.x + threadIdx.x;
     if (k >= K) return;
     const T s = out[K + k];
     T q;
@@ -455,7 +456,7 @@ struct RaggedLayout {
     double* hneg;
     unsigned long long* totals;
     unsigned* partial;
-    RaggedLayout(void* scratch, int K, int64_t p_fwer) {
+    __host__ __device__ RaggedLayout(void* scratch, int K, int64_t p_fwer) {
         unsigned char* s = static_cast<unsigned char*>(scratch);
         auto align16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
         fac = reinterpret_cast<T*>(s);
@@ -474,6 +475,119 @@ struct RaggedLayout {
         partial = reinterpret_cast<unsigned*>(s + align16(off + sizeof(double) * (2 * ((size_t)K + 2) + 8)));
     }
 };
+
+// ---- the kernels of one statistics run (solo) --------------------------------
+template <class T>
+__global__ void stats_set_kernel(const T* __restrict__ es, int K, int64_t ld, const int64_t* __restrict__ counts,
+                                 T* __restrict__ out, T* __restrict__ fac) {
+    stats_set_kernel_body<T>(blockIdx.x, es, K, ld, counts, out, fac);
+}
+template <class T>
+__global__ void stats_extrema_kernel(const T* __restrict__ es, int K, int64_t ld, int64_t P, const T* __restrict__ fac,
+                                     typename RadixKey<T>::U* __restrict__ mx, typename RadixKey<T>::U* __restrict__ mn) {
+    stats_extrema_kernel_body<T>(blockIdx.x, blockIdx.y, es, K, ld, P, fac, mx, mn);
+}
+template <class T>
+__global__ void stats_fwer_kernel(int K, int64_t P, const typename RadixKey<T>::U* __restrict__ mx,
+                                  const typename RadixKey<T>::U* __restrict__ mn, T* __restrict__ out) {
+    stats_fwer_kernel_body<T>(blockIdx.x, K, P, mx, mn, out);
+}
+template <class T>
+__global__ void stats_fdr_obs_kernel(int K, const T* __restrict__ out, unsigned long long* __restrict__ cnt_obs,
+                                     unsigned long long* __restrict__ lcount, T* __restrict__ sorted_pos,
+                                     T* __restrict__ sorted_neg, unsigned long long* __restrict__ totals) {
+    stats_fdr_obs_kernel_body<T>(blockIdx.x, K, out, cnt_obs, lcount, sorted_pos, sorted_neg, totals);
+}
+template <class T>
+__global__ void __launch_bounds__(kDenseHistThreads)
+stats_fdr_hist_dense_kernel(const T* __restrict__ es, int K, int64_t ld, const T* __restrict__ fac,
+                            const T* __restrict__ sorted_pos, const T* __restrict__ sorted_neg,
+                            const unsigned long long* __restrict__ totals, unsigned* __restrict__ partial) {
+    stats_fdr_hist_dense_kernel_body<T>(blockIdx.x, gridDim.x, es, K, ld, fac, sorted_pos, sorted_neg, totals, partial);
+}
+__global__ void stats_fdr_hist_sum_kernel(const unsigned* __restrict__ partial, int rows, int K,
+                                          double* __restrict__ hist, unsigned long long* __restrict__ totals) {
+    stats_fdr_hist_sum_kernel_body(blockIdx.x, partial, rows, K, hist, totals);
+}
+__global__ void stats_fdr_suffix_kernel(double* __restrict__ hpos, double* __restrict__ hneg,
+                                        const unsigned long long* __restrict__ totals) {
+    stats_fdr_suffix_kernel_body(blockIdx.x, hpos, hneg, totals);
+}
+template <class T>
+__global__ void stats_fdr_final_kernel(int K, const unsigned long long* __restrict__ cnt_obs,
+                                       const unsigned long long* __restrict__ lcount,
+                                       const double* __restrict__ spos, const double* __restrict__ sneg,
+                                       const unsigned long long* __restrict__ totals, T* __restrict__ out) {
+    stats_fdr_final_kernel_body<T>(blockIdx.x, K, cnt_obs, lcount, spos, sneg, totals, out);
+}
+
+// ---- the same kernels over many instances at once ----------------------------
+// blockIdx.z = the instance; every instance has all its columns (the dense
+// form); grids are sized for the largest instance and the blocks beyond an
+// instance's own extent return at once.  Each instance's results are those
+// of its solo run bit for bit: the same bodies, the same block decomposition.
+template <class T>
+__global__ void stats_init_multi(const StatsTask<T>* __restrict__ tasks) {
+    using U = typename RadixKey<T>::U;
+    const StatsTask<T> t = tasks[blockIdx.z];
+    const RaggedLayout<T> L(t.scratch, t.K, t.P);
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 2 * ((int64_t)t.K + 2) + 8) L.hpos[i] = 0.0;  // H_pos | H_neg | totals
+    if (i < t.P) {
+        L.mx[i] = U(0);
+        L.mn[i] = ~U(0);
+    }
+}
+template <class T>
+__global__ void stats_set_multi(const StatsTask<T>* __restrict__ tasks) {
+    const StatsTask<T> t = tasks[blockIdx.z];
+    const RaggedLayout<T> L(t.scratch, t.K, t.P);
+    stats_set_kernel_body<T>(blockIdx.x, t.es, t.K, t.P, nullptr, t.stats, L.fac);
+}
+template <class T>
+__global__ void stats_extrema_multi(const StatsTask<T>* __restrict__ tasks) {
+    const StatsTask<T> t = tasks[blockIdx.z];
+    const RaggedLayout<T> L(t.scratch, t.K, t.P);
+    stats_extrema_kernel_body<T>(blockIdx.x, blockIdx.y, t.es, t.K, t.P, t.P, L.fac, L.mx, L.mn);
+}
+template <class T>
+__global__ void stats_fwer_multi(const StatsTask<T>* __restrict__ tasks) {
+    const StatsTask<T> t = tasks[blockIdx.z];
+    const RaggedLayout<T> L(t.scratch, t.K, t.P);
+    stats_fwer_kernel_body<T>(blockIdx.x, t.K, t.P, L.mx, L.mn, t.stats);
+}
+template <class T>
+__global__ void stats_fdr_obs_multi(const StatsTask<T>* __restrict__ tasks) {
+    const StatsTask<T> t = tasks[blockIdx.z];
+    const RaggedLayout<T> L(t.scratch, t.K, t.P);
+    stats_fdr_obs_kernel_body<T>(blockIdx.x, t.K, t.stats, L.cnt_obs, L.lcount, L.sorted_pos, L.sorted_neg, L.totals);
+}
+template <class T>
+__global__ void __launch_bounds__(kDenseHistThreads) stats_fdr_hist_dense_multi(const StatsTask<T>* __restrict__ tasks) {
+    const StatsTask<T> t = tasks[blockIdx.z];
+    if ((int)blockIdx.x >= t.rows) return;  // the whole block: before any barrier
+    const RaggedLayout<T> L(t.scratch, t.K, t.P);
+    stats_fdr_hist_dense_kernel_body<T>(blockIdx.x, t.rows, t.es, t.K, t.P, L.fac, L.sorted_pos, L.sorted_neg,
+                                        L.totals, L.partial);
+}
+template <class T>
+__global__ void stats_fdr_hist_sum_multi(const StatsTask<T>* __restrict__ tasks) {
+    const StatsTask<T> t = tasks[blockIdx.z];
+    const RaggedLayout<T> L(t.scratch, t.K, t.P);
+    stats_fdr_hist_sum_kernel_body(blockIdx.x, L.partial, t.rows, t.K, L.hpos, L.totals);
+}
+template <class T>
+__global__ void stats_fdr_suffix_multi(const StatsTask<T>* __restrict__ tasks) {
+    const StatsTask<T> t = tasks[blockIdx.z];
+    const RaggedLayout<T> L(t.scratch, t.K, t.P);
+    stats_fdr_suffix_kernel_body(blockIdx.x, L.hpos, L.hneg, L.totals);
+}
+template <class T>
+__global__ void stats_fdr_final_multi(const StatsTask<T>* __restrict__ tasks) {
+    const StatsTask<T> t = tasks[blockIdx.z];
+    const RaggedLayout<T> L(t.scratch, t.K, t.P);
+    stats_fdr_final_kernel_body<T>(blockIdx.x, t.K, L.cnt_obs, L.lcount, L.hpos, L.hneg, L.totals, t.stats);
+}
 
 // Lower bound of every set's FDR q after the statistics (adaptive stopping):
 // the set's |NES| may lie anywhere in [|NES|, key], key = |NES| (1 + z cv /
@@ -646,6 +760,56 @@ template cudaError_t launch_stats_ragged<float>(const float*, int, int64_t, cons
                                                 cudaStream_t, int64_t);
 template cudaError_t launch_stats_ragged<double>(const double*, int, int64_t, const int64_t*, int64_t, double*, void*,
                                                  cudaStream_t, int64_t);
+
+template <class T>
+int stats_multi_rows(int K, int64_t P) {
+    if (K <= 0 || P < 2) return 0;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return dense_hist_rows<T>(K, sms);
+}
+template int stats_multi_rows<float>(int, int64_t);
+template int stats_multi_rows<double>(int, int64_t);
+
+template <class T>
+cudaError_t launch_stats_multi(const StatsTask<T>* d_tasks, const StatsTask<T>* h_tasks, int n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (n > 65535) return cudaErrorInvalidValue;
+    int Kmax = 0, rows = 0;
+    int64_t Pmax = 0, init = 0;
+    size_t smem = 0;
+    for (int i = 0; i < n; i++) {
+        const StatsTask<T>& t = h_tasks[i];
+        if (t.rows <= 0 || t.P < 2) return cudaErrorInvalidValue;  // the dense form only
+        Kmax = std::max(Kmax, t.K);
+        Pmax = std::max(Pmax, t.P);
+        rows = std::max(rows, t.rows);
+        init = std::max(init, std::max(2 * ((int64_t)t.K + 2) + 8, t.P));
+        smem = std::max(smem, dense_hist_smem<T>(t.K));
+    }
+    const unsigned z = (unsigned)n;
+    const int wpb = 8;
+    const unsigned set_blocks = (unsigned)((Kmax + wpb - 1) / wpb);
+    stats_init_multi<T><<<dim3((unsigned)((init + 255) / 256), 1, z), 256, 0, st>>>(d_tasks);
+    stats_set_multi<T><<<dim3(set_blocks, 1, z), wpb * 32, 0, st>>>(d_tasks);
+    stats_extrema_multi<T><<<dim3((unsigned)((Pmax + 127) / 128), (unsigned)((Kmax + kExtremaSets - 1) / kExtremaSets), z),
+                             128, 0, st>>>(d_tasks);
+    stats_fwer_multi<T><<<dim3(set_blocks, 1, z), wpb * 32, 0, st>>>(d_tasks);
+    stats_fdr_obs_multi<T><<<dim3(set_blocks, 1, z), wpb * 32, 0, st>>>(d_tasks);
+    cudaError_t e = cudaFuncSetAttribute(stats_fdr_hist_dense_multi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    stats_fdr_hist_dense_multi<T><<<dim3((unsigned)rows, 1, z), kDenseHistThreads, smem, st>>>(d_tasks);
+    const int Wmax = 2 * (Kmax + 2) + 2;
+    stats_fdr_hist_sum_multi<T><<<dim3((unsigned)((Wmax + 255) / 256), 1, z), 256, 0, st>>>(d_tasks);
+    stats_fdr_suffix_multi<T><<<dim3(2, 1, z), 1024, 0, st>>>(d_tasks);
+    stats_fdr_final_multi<T><<<dim3((unsigned)((Kmax + 255) / 256), 1, z), 256, 0, st>>>(d_tasks);
+    launches_add(9);
+    return cudaGetLastError();
+}
+template cudaError_t launch_stats_multi<float>(const StatsTask<float>*, const StatsTask<float>*, int, cudaStream_t);
+template cudaError_t launch_stats_multi<double>(const StatsTask<double>*, const StatsTask<double>*, int, cudaStream_t);
 
 template <class T>
 cudaError_t launch_stats(const T* es, int K, int64_t P, T* stats, void* scratch, cudaStream_t st) {

@@ -107,6 +107,55 @@ template <class T>
 cudaError_t launch_stats_ragged(const T* es, int K, int64_t ld, const int64_t* counts, int64_t p_fwer, T* stats,
                                 void* scratch, cudaStream_t st, int64_t hist_cols = 0);
 
+// Sorts of many instances at once (batched form): all instances of one
+// register-resident class (sort_multi_class of their G and precision; 0: the
+// class has no multi form, the instance takes its solo launch_sort), one
+// launch, blockIdx.z = instance; ranks (16-bit), weights and order those of
+// the solo sort.
+struct SortTask {
+    const void* keys;   // [P][G] T
+    void* ranks;        // [P][G] uint16
+    void* sorted;       // [P][G] T
+    uint32_t* order;    // [P][G] or null
+    int G;
+    int num_perms;
+    int descending;
+};
+int sort_multi_class(int G, bool fp64);
+cudaError_t launch_sort_multi(const SortTask* d_tasks, int n, int cls, bool fp64, cudaStream_t st);
+
+// Label permutations of many instances at once (batched form), blockIdx.z =
+// instance; each instance's masks those of its solo launch_permute.
+struct PermTask {
+    const uint8_t* labels;
+    uint32_t* masks;
+    int64_t perm_offset;
+    int64_t num_perms;
+    uint32_t seed;
+    int S;
+    int words;
+};
+cudaError_t launch_permute_multi(const PermTask* d_tasks, const PermTask* h_tasks, int n, cudaStream_t st);
+
+// Statistics of many instances at once (batched form): one launch per step
+// over all instances (blockIdx.z = instance), each instance's results those
+// of its solo launch_stats bit for bit.  Dense form only: every instance has
+// P >= 2 columns and rows = stats_multi_rows<T>(K, P) > 0 (its FDR
+// histogram fits shared memory).
+template <class T>
+struct StatsTask {
+    const T* es;    // [K][P]
+    T* stats;       // [5][K]
+    void* scratch;  // stats_scratch_bytes<T>(K, P)
+    int K;
+    int rows;       // stats_multi_rows<T>(K, P)
+    int64_t P;
+};
+template <class T>
+int stats_multi_rows(int K, int64_t P);
+template <class T>
+cudaError_t launch_stats_multi(const StatsTask<T>* d_tasks, const StatsTask<T>* h_tasks, int n, cudaStream_t st);
+
 // Chosen form (tcgen05 class statistics, fp32 inputs).  Operand buffers:
 // A1/A2 chosen_a_bytes(G, S) each, B chosen_b_bytes(P_batch, S).
 int chosen_chunks(int S);
@@ -125,6 +174,27 @@ cudaError_t launch_chosen_metric(int metric, bool fp64_variance, const uint32_t*
                                  int tile_n = 0);
 // (tile_n: permutations per tensor-core tile, 128 or 256; 0 = 256.  The B
 // buffer of chosen_b_bytes fits either.)
+// metric id -> its combiner family (the class statistics kernel's template)
+int chosen_comb(int metric);
+// Many instances at once (batched form): one launch each of the B clearing,
+// the label operand and the tensor-core class statistics (128-permutation
+// tiles) over every instance, blockIdx.z = instance; all tasks of one call
+// share `comb`.  Keys identical to the solo launch_chosen_metric's.
+struct ChosenTask {
+    const unsigned char* A1;
+    const unsigned char* A2;
+    unsigned char* Bm;
+    const float* mu;
+    const double* t1;
+    const double* t2;
+    float* keys;
+    const uint32_t* masks;
+    int* error_flag;
+    float nA, nB;
+    int G, S, num_perms, chunks, words, comb;
+};
+cudaError_t launch_chosen_metric_multi(const ChosenTask* d_tasks, const ChosenTask* h_tasks, int n,
+                                       bool fp64_variance, cudaStream_t st);
 
 // mean, standard deviation and skewness (biased, in double) of keys[0..G)
 template <class T>

@@ -126,6 +126,10 @@ int plan_check_error(gsea_plan_s* p);
 // the enrichment kernel; and the statistics of the plan's ES matrix
 int plan_run_stage1(gsea_plan_s* p, cudaStream_t st);
 int plan_run_stats(gsea_plan_s* p, cudaStream_t st);
+// the metric (plain or tensor-core form) and the sort of every permutation
+// of a plan with one device batch, each on its own (batched-form fallbacks)
+int plan_run_metric(gsea_plan_s* p, cudaStream_t st);
+int plan_run_sort(gsea_plan_s* p, cudaStream_t st);
 // autotune the metric and sort stages of a plan on n permutations (tune.cu)
 int plan_autotune_front(gsea_plan_s* p, int64_t n);
 }  // namespace gsea

@@ -304,17 +304,23 @@ int gsea_plan_autotune(gsea_plan plan, int64_t sample_perms, gsea_tuning* best, 
  *      Many independent GSEA problems run together.  No counterpart in the
  *      reference (one problem per call).  Instances share precision and
  *      form; each has its own genes, samples, sets, permutations and metric
- *      (num_genes <= 65,536).  An execute runs, for every instance, the
- *      permutation, metric and sort of all its permutations (one device
- *      batch: num_perms x num_genes buffers per instance) spread over a pool
- *      of streams; then one persistent enrichment launch per size class
- *      (bitmap words per lane) over every (instance, permutation) item,
- *      largest instances first; then every instance's statistics.  The
- *      first execute captures all of it into one CUDA graph; later executes
- *      replay that graph (gsea_batch_set_inputs or gsea_batch_autotune
- *      make the next execute capture again).                               */
+ *      (num_genes <= 65,536).  An execute runs each stage as one launch
+ *      over every instance (one device batch: num_perms x num_genes buffers
+ *      per instance): the permutations; the metric (tensor-core form: one
+ *      launch set per metric family); the sort (one launch per
+ *      register-resident class; instances beyond the register forms sort on
+ *      their own); one persistent enrichment launch per size class (bitmap
+ *      words per lane) whose CTAs pull (instance, permutation) items,
+ *      largest instances first; the statistics (nine launches).  Every
+ *      instance's results are its solo plan's bit for bit.  The first
+ *      execute captures all of it into one CUDA graph; later executes
+ *      replay that graph (gsea_batch_set_inputs or gsea_batch_autotune make
+ *      the next execute capture again).  gsea_batch_autotune tunes the
+ *      enrichment launch per size class (the other stages have one launch
+ *      shape in the batched form).                                        */
 typedef struct gsea_batch_s* gsea_batch;
-/* streams: size of the stream pool (0 = 16) */
+/* streams: size of a stream pool (0 = 16) kept by the batch; the execute
+ * issues its launches on one stream */
 int gsea_batch_create(int64_t num_instances, const gsea_config* cfgs, int streams, gsea_batch* out);
 int gsea_batch_destroy(gsea_batch b);
 int gsea_batch_set_inputs(gsea_batch b, int64_t instance, const void* exprs, const uint8_t* labels,

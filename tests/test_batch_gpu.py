@@ -1,7 +1,7 @@
-"""Batched instances: uneven GSEA problems run together (stream pool, one
-persistent enrichment launch per size class, one CUDA graph) give exactly the
-results of running each instance on its own plan; the graph replays; the
-batch autotuner keeps the results."""
+"""Batched instances: uneven GSEA problems run together (one launch per
+stage over every instance, one persistent enrichment launch per size class,
+one CUDA graph) give exactly the results of running each instance on its own
+plan; the graph replays; the batch autotuner keeps the results."""
 import numpy as np
 import pytest
 
@@ -57,8 +57,35 @@ def test_batch_matches_solo_plans(gpu, precision, form):
             assert same(st, ref[i][1]), (rep, i)
     info = b.info()
     assert info["es_classes"] >= 5
-    assert info["graph_nodes"] > 4 * len(ds)
     assert info["launches"] > 0
+    if form == N.FORM_CHOSEN:
+        # permute 1 + metric 3 + sort classes + ES classes + statistics 9
+        assert info["launches"] <= 1 + 3 + 7 + info["es_classes"] + 9, info
+    b.close()
+
+
+def test_batch_of_40_uneven_instances_matches_solo_plans(gpu):
+    """40 instances with genes U[1,000, 30,000], samples U[20, 200], sets
+    U[10, 300] and permutations U[64, 600] (tensor-core form, one metric): the
+    batched execute equals every solo plan bit for bit, and issues a handful
+    of launches -- one per stage (and per sort / enrichment class), not one
+    per instance."""
+    ds = synthetic.batch_instances(40, seed=5, num_perms=64, genes=(1000, 30000), samples=(20, 200),
+                                   sets=(10, 300), set_size=(15, 200))
+    rs = np.random.RandomState(9)
+    for d in ds:
+        d.num_perms = int(rs.randint(64, 601))
+    ref = [solo(d, "twopass_signal2noise", 32, N.FORM_CHOSEN) for d in ds]
+    b = api.Batch(ds, "twopass_signal2noise", precision=32, form=N.FORM_CHOSEN)
+    for rep in range(2):
+        b.execute()
+        b.synchronize()
+        for i in range(len(ds)):
+            es, st = b.read(i)
+            assert same(es, ref[i][0]), (rep, i)
+            assert same(st, ref[i][1]), (rep, i)
+    info = b.info()
+    assert info["launches"] <= 1 + 3 + 7 + info["es_classes"] + 9, info
     b.close()
 
 
