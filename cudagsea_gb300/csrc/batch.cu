@@ -299,15 +299,39 @@ int record(gsea_batch_s* b) {
         for (int64_t i = 0; i < n; i++)
             if ((rc = gsea::plan_run_metric(b->plans[i], st))) return rc;
     }
+    // the sort classes (and the instances that sort on their own), then the
+    // enrichment size classes, each set of launches spread over the stream
+    // pool so that one launch's tail overlaps the next one's start
+    const size_t ns = b->streams.size();
+    cudaEvent_t* ev = b->events.data();  // [0] fork 1, [1..ns] join 1, [ns+1] fork 2, [ns+2..2ns+1] join 2
+    auto fork = [&](cudaEvent_t e) -> int {
+        GSEA_CUDA(cudaEventRecord(e, st), "fork");
+        for (size_t k = 0; k < ns; k++) GSEA_CUDA(cudaStreamWaitEvent(b->streams[k], e, 0), "fork");
+        return GSEA_OK;
+    };
+    auto join = [&](cudaEvent_t* es) -> int {
+        for (size_t k = 0; k < ns; k++) {
+            GSEA_CUDA(cudaEventRecord(es[k], b->streams[k]), "join");
+            GSEA_CUDA(cudaStreamWaitEvent(st, es[k], 0), "join");
+        }
+        return GSEA_OK;
+    };
+    if ((rc = fork(ev[0]))) return rc;
+    size_t lane = 0;
     for (auto& m : b->sorts)
-        GSEA_CUDA(gsea::launch_sort_multi(m.d, (int)m.h.size(), m.key, fp64, st), "batched sort");
+        GSEA_CUDA(gsea::launch_sort_multi(m.d, (int)m.h.size(), m.key, fp64, b->streams[lane++ % ns]),
+                  "batched sort");
     for (int64_t i : b->solo_sort)
-        if ((rc = gsea::plan_run_sort(b->plans[i], st))) return rc;
+        if ((rc = gsea::plan_run_sort(b->plans[i], b->streams[lane++ % ns]))) return rc;
+    if ((rc = join(ev + 1))) return rc;
+    if ((rc = fork(ev[ns + 1]))) return rc;
     for (size_t ci = 0; ci < b->classes.size(); ci++) {
         const auto it = b->es_tuning.find(b->classes[ci].wpl);
         const gsea::EsTuning tune = it == b->es_tuning.end() ? gsea::EsTuning() : it->second;
-        GSEA_CUDA(launch_class<T>(b, ci, b->classes[ci].nitems, tune, st), "batched enrichment kernel");
+        GSEA_CUDA(launch_class<T>(b, ci, b->classes[ci].nitems, tune, b->streams[ci % ns]),
+                  "batched enrichment kernel");
     }
+    if ((rc = join(ev + ns + 2))) return rc;
     if constexpr (sizeof(T) == 8)
         GSEA_CUDA(gsea::launch_stats_multi<double>(b->stats64.d, b->stats64.h.data(), (int)b->stats64.h.size(), st),
                   "batched statistics");

@@ -319,8 +319,8 @@ int gsea_plan_autotune(gsea_plan plan, int64_t sample_perms, gsea_tuning* best, 
  *      enrichment launch per size class (the other stages have one launch
  *      shape in the batched form).                                        */
 typedef struct gsea_batch_s* gsea_batch;
-/* streams: size of a stream pool (0 = 16) kept by the batch; the execute
- * issues its launches on one stream */
+/* streams: size of the stream pool (0 = 16) over which an execute spreads
+ * the sort classes and the enrichment size classes */
 int gsea_batch_create(int64_t num_instances, const gsea_config* cfgs, int streams, gsea_batch* out);
 int gsea_batch_destroy(gsea_batch b);
 int gsea_batch_set_inputs(gsea_batch b, int64_t instance, const void* exprs, const uint8_t* labels,
