@@ -7,8 +7,9 @@
 //   1. the label permutations of every instance: one launch;
 //   2. the metric: in the tensor-core form one launch each of the label
 //      operand and the tcgen05 class statistics per metric family (one
-//      family when all instances share a metric); the plain form per
-//      instance;
+//      family when all instances share a metric); in the plain form one
+//      launch per metric and kernel path (exact, or packed with 4 or 8
+//      permutations per thread);
 //   3. the sort: one launch per register-resident class (ITEMS keys per
 //      thread, one CTA or a two-CTA cluster per permutation); instances
 //      beyond the register forms (G > 40,960 fp32 / 20,480 fp64) sort on
@@ -67,6 +68,8 @@ struct gsea_batch_s {
     // the multi-instance launches of the other stages (built with the classes)
     Multi<gsea::PermTask> perm;
     std::vector<Multi<gsea::ChosenTask>> chosen;
+    std::vector<Multi<gsea::MetricTask<float>>> metric32;   // plain form
+    std::vector<Multi<gsea::MetricTask<double>>> metric64;
     std::vector<Multi<gsea::SortTask>> sorts;
     std::vector<int64_t> solo_sort;   // instances sorted on their own (tiled sort)
     Multi<gsea::StatsTask<float>> stats32;
@@ -114,6 +117,10 @@ void drop_classes(gsea_batch_s* b) {
     free_multi(b->perm);
     for (auto& m : b->chosen) free_multi(m);
     b->chosen.clear();
+    for (auto& m : b->metric32) free_multi(m);
+    b->metric32.clear();
+    for (auto& m : b->metric64) free_multi(m);
+    b->metric64.clear();
     for (auto& m : b->sorts) free_multi(m);
     b->sorts.clear();
     b->solo_sort.clear();
@@ -122,11 +129,18 @@ void drop_classes(gsea_batch_s* b) {
     b->solo_stats.clear();
 }
 
+template <class T>
+std::vector<Multi<gsea::MetricTask<T>>>& metric_groups(gsea_batch_s* b) {
+    if constexpr (sizeof(T) == 8) return b->metric64;
+    else return b->metric32;
+}
+
 // the task tables of the multi-instance stages
 template <class T>
 int build_multi(gsea_batch_s* b, Multi<gsea::StatsTask<T>>& stats) {
     const bool fp64 = b->precision == 64;
-    std::map<int, size_t> chosen_at, sort_at;
+    std::map<int, size_t> chosen_at, sort_at, metric_at;
+    auto& metrics = metric_groups<T>(b);
     for (int64_t i = 0; i < (int64_t)b->plans.size(); i++) {
         gsea_plan_s* p = b->plans[i];
         const gsea_config& c = p->cfg;
@@ -165,6 +179,27 @@ int build_multi(gsea_batch_s* b, Multi<gsea::StatsTask<T>>& stats) {
                 b->chosen.back().key = ct.comb;
             }
             b->chosen[it->second].h.push_back(ct);
+        } else {
+            gsea::MetricTask<T> mt;
+            mt.X = static_cast<const T*>(p->exprs);
+            mt.masks = p->masks;
+            mt.keys = static_cast<T*>(p->keys);
+            mt.fast_ok = p->fast_ok;
+            mt.G = (int)c.num_genes;
+            mt.S = (int)c.num_samples;
+            mt.words = p->words;
+            mt.num_perms = (int)p->pb;
+            mt.nA = (T)p->nA;
+            mt.nB = (T)p->nB;
+            const int key = gsea::metric_multi_key<T>(c.metric, mt.S, mt.words, p->fast_ok != nullptr,
+                                                      p->tuning.metric_pb);
+            auto it = metric_at.find(key);
+            if (it == metric_at.end()) {
+                it = metric_at.emplace(key, metrics.size()).first;
+                metrics.emplace_back();
+                metrics.back().key = key;
+            }
+            metrics[it->second].h.push_back(mt);
         }
         const int cls = gsea::sort_multi_class((int)c.num_genes, fp64);
         if (cls == 0 || !p->ranks16) {
@@ -202,6 +237,8 @@ int build_multi(gsea_batch_s* b, Multi<gsea::StatsTask<T>>& stats) {
     }
     cudaError_t e = upload_multi(b->perm);
     for (auto& m : b->chosen)
+        if (e == cudaSuccess) e = upload_multi(m);
+    for (auto& m : metrics)
         if (e == cudaSuccess) e = upload_multi(m);
     for (auto& m : b->sorts)
         if (e == cudaSuccess) e = upload_multi(m);
@@ -285,7 +322,6 @@ cudaError_t launch_class(gsea_batch_s* b, size_t ci, int64_t nitems, gsea::EsTun
 // the whole execute on `main`: one launch per stage over all instances
 template <class T>
 int record(gsea_batch_s* b) {
-    const int64_t n = (int64_t)b->plans.size();
     const bool fp64 = b->precision == 64;
     cudaStream_t st = b->main;
     int rc;
@@ -296,8 +332,8 @@ int record(gsea_batch_s* b) {
             GSEA_CUDA(gsea::launch_chosen_metric_multi(m.d, m.h.data(), (int)m.h.size(), fp64var, st),
                       "batched tensor-core class statistics");
     } else {
-        for (int64_t i = 0; i < n; i++)
-            if ((rc = gsea::plan_run_metric(b->plans[i], st))) return rc;
+        for (auto& m : metric_groups<T>(b))
+            GSEA_CUDA(gsea::launch_metric_multi<T>(m.key, m.d, m.h.data(), (int)m.h.size(), st), "batched metric");
     }
     // the sort classes (and the instances that sort on their own), then the
     // enrichment size classes, each set of launches spread over the stream

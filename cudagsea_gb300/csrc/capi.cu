@@ -260,6 +260,7 @@ int run_range_t(gsea_plan_s* p, cudaStream_t st, int64_t lo, int64_t hi, const i
     sb.order = p->debug ? p->order : nullptr;
     sb.scratch = p->sort_scratch;
     sb.scratch_bytes = p->sort_scratch_bytes;
+    sb.error_flag = p->dev_error;
     sb.variant = p->tuning.sort_variant;
     gsea::EsTuning et;
     et.warps = p->tuning.es_warps;
@@ -408,6 +409,7 @@ int plan_run_sort(gsea_plan_s* p, cudaStream_t st) {
     sb.order = p->debug ? p->order : nullptr;
     sb.scratch = p->sort_scratch;
     sb.scratch_bytes = p->sort_scratch_bytes;
+    sb.error_flag = p->dev_error;
     sb.variant = p->tuning.sort_variant;
     const int G = (int)c.num_genes, n = (int)p->pb;
     cudaError_t e = c.precision == 64

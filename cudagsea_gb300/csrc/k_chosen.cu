@@ -46,6 +46,7 @@
 
 #include <cstdint>
 
+#include "bulk.cuh"
 #include "common.cuh"
 #include "kernels.h"
 
@@ -65,16 +66,11 @@ constexpr int stages() { return TN == 128 ? 2 : 3; }
 template <int TN>
 constexpr int stage_bytes() { return 2 * A_CHUNK + TN * BK * 2; }
 constexpr int THREADS = 256;     // 8 warps: two per TMEM lane quarter in the epilogue
-constexpr long long kWaitCycles = 2000000000ll;  // ~1 s at 2 GHz
 
 // byte offset of element (row, k) inside a chunk laid out as 8x8 core
 // matrices: core (row/8, k/8) at ((row/8)*8 + k/8)*128, row-major inside
 __host__ __device__ __forceinline__ uint32_t core_offset(int row, int k) {
     return (uint32_t)((((row >> 3) * (BK / 8) + (k >> 3)) << 7) + ((row & 7) << 4) + ((k & 7) << 1));
-}
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
 }
 
 // shared-memory matrix descriptor, no swizzle, K-major
@@ -97,34 +93,6 @@ __host__ __device__ constexpr uint32_t make_idesc(int m, int n) {
            | ((uint32_t)(m >> 4) << 24);   // M / 16
 }
 
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// bounded wait; false after ~1 s
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-    const long long t0 = clock64();
-    while (!mbar_try(bar, parity)) {
-        if (clock64() - t0 > kWaitCycles) return false;
-    }
-    return true;
-}
-__device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-                 "l"(src), "r"(bytes), "r"(bar)
-                 : "memory");
-}
 __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                          uint32_t accumulate) {
     asm volatile(

@@ -21,6 +21,7 @@
 // permutation is a warp-uniform bit of a shared-memory mask word, so the
 // class selection never diverges.
 #pragma once
+#include <algorithm>
 #include <type_traits>
 
 #include "common.cuh"
@@ -186,20 +187,38 @@ __device__ __forceinline__ void metric_exact(const T* __restrict__ X, int G, int
     }
 }
 
+// one CTA of the exact form: genes bx*128.., permutations by*PB..
 template <int ACC, int COMB, class T, int PB>
-__global__ void __launch_bounds__(128)
-metric_kernel(const T* __restrict__ X, int G, int S, const uint32_t* __restrict__ masks, int words,
-              int num_perms, T nA, T nB, T* __restrict__ keys) {
+__device__ __forceinline__ void metric_exact_block(const T* __restrict__ X, int G, int S,
+                                                   const uint32_t* __restrict__ masks, int words, int num_perms,
+                                                   T nA, T nB, T* __restrict__ keys, int bx, int by) {
     extern __shared__ uint32_t sm_masks[];  // [PB][words]
-    const int p0 = blockIdx.y * PB;
+    const int p0 = by * PB;
     for (int i = threadIdx.x; i < PB * words; i += blockDim.x) {
         const int j = i / words, w = i - j * words;
         sm_masks[i] = (p0 + j < num_perms) ? masks[(int64_t)(p0 + j) * words + w] : 0u;
     }
     __syncthreads();
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int g = bx * blockDim.x + threadIdx.x;
     if (g >= G) return;
     metric_exact<ACC, COMB, T, PB>(X, G, S, sm_masks, words, num_perms, p0, nA, nB, keys, g);
+}
+
+template <int ACC, int COMB, class T, int PB>
+__global__ void __launch_bounds__(128)
+metric_kernel(const T* __restrict__ X, int G, int S, const uint32_t* __restrict__ masks, int words,
+              int num_perms, T nA, T nB, T* __restrict__ keys) {
+    metric_exact_block<ACC, COMB, T, PB>(X, G, S, masks, words, num_perms, nA, nB, keys, blockIdx.x, blockIdx.y);
+}
+
+// every instance of a batch group in one launch (blockIdx.z = instance; the
+// grid covers the largest instance, CTAs beyond an instance's extent leave)
+template <int ACC, int COMB, class T, int PB>
+__global__ void __launch_bounds__(128) metric_multi(const MetricTask<T>* __restrict__ tasks) {
+    const MetricTask<T> t = tasks[blockIdx.z];
+    if ((int)blockIdx.x * 128 >= t.G || (int)blockIdx.y * PB >= t.num_perms) return;
+    metric_exact_block<ACC, COMB, T, PB>(t.X, t.G, t.S, t.masks, t.words, t.num_perms, t.nA, t.nB, t.keys,
+                                         blockIdx.x, blockIdx.y);
 }
 
 // ---------------------------------------------------------------------------
@@ -240,16 +259,18 @@ __device__ __forceinline__ unsigned long long f2_mul(unsigned long long a, unsig
     return d;
 }
 
+// one CTA of the packed form: genes bx*128.., permutations by*PB..
 template <int ACC, int COMB, int PB>
-__global__ void __launch_bounds__(128, 8)
-metric_fast_kernel(const float* __restrict__ X, int G, int S, const uint32_t* __restrict__ masks, int words,
-                   int num_perms, float nA, float nB, float* __restrict__ keys, const int* __restrict__ fast_ok) {
+__device__ __forceinline__ void metric_fast_block(const float* __restrict__ X, int G, int S,
+                                                  const uint32_t* __restrict__ masks, int words, int num_perms,
+                                                  float nA, float nB, float* __restrict__ keys,
+                                                  const int* __restrict__ fast_ok, int bx, int by) {
     static_assert(PB % 2 == 0, "permutations are processed in pairs");
     constexpr int PAIRS = PB / 2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ulonglong2* lab = reinterpret_cast<ulonglong2*>(smem_raw);                       // [S][PAIRS]
     uint32_t* sm_masks = reinterpret_cast<uint32_t*>(lab + (size_t)S * PAIRS);        // [PB][words]
-    const int p0 = blockIdx.y * PB;
+    const int p0 = by * PB;
     for (int i = threadIdx.x; i < PB * words; i += blockDim.x) {
         const int j = i / words, w = i - j * words;
         sm_masks[i] = (p0 + j < num_perms) ? masks[(int64_t)(p0 + j) * words + w] : 0u;
@@ -266,7 +287,7 @@ metric_fast_kernel(const float* __restrict__ X, int G, int S, const uint32_t* __
         }
     }
     __syncthreads();
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int g = bx * blockDim.x + threadIdx.x;
     if (g >= G) return;
     if (!fast) {
         metric_exact<ACC, COMB, float, PB>(X, G, S, sm_masks, words, num_perms, p0, nA, nB, keys, g);
@@ -369,6 +390,22 @@ metric_fast_kernel(const float* __restrict__ X, int G, int S, const uint32_t* __
 }
 
 template <int ACC, int COMB, int PB>
+__global__ void __launch_bounds__(128, 8)
+metric_fast_kernel(const float* __restrict__ X, int G, int S, const uint32_t* __restrict__ masks, int words,
+                   int num_perms, float nA, float nB, float* __restrict__ keys, const int* __restrict__ fast_ok) {
+    metric_fast_block<ACC, COMB, PB>(X, G, S, masks, words, num_perms, nA, nB, keys, fast_ok, blockIdx.x,
+                                     blockIdx.y);
+}
+
+template <int ACC, int COMB, int PB>
+__global__ void __launch_bounds__(128, 8) metric_fast_multi(const MetricTask<float>* __restrict__ tasks) {
+    const MetricTask<float> t = tasks[blockIdx.z];
+    if ((int)blockIdx.x * 128 >= t.G || (int)blockIdx.y * PB >= t.num_perms) return;
+    metric_fast_block<ACC, COMB, PB>(t.X, t.G, t.S, t.masks, t.words, t.num_perms, t.nA, t.nB, t.keys, t.fast_ok,
+                                     blockIdx.x, blockIdx.y);
+}
+
+template <int ACC, int COMB, int PB>
 cudaError_t launch_metric_fast_pb(const float* X, int G, int S, const uint32_t* masks, int words, int num_perms,
                                   int64_t nA, int64_t nB, float* keys, const int* fast_ok, cudaStream_t st) {
     const int threads = 128;
@@ -450,6 +487,115 @@ cudaError_t launch_metric_impl(int metric, const T* X, int G, int S, const uint3
             return cudaErrorInvalidValue;
     }
 #undef GSEA_M
+}
+
+// Batched instances: the group key of an instance (instances with equal keys
+// share one launch) -- the metric and the path launch_metric_impl takes for
+// it (exact, or packed with 4 or 8 permutations per thread).
+template <class T>
+int metric_multi_key_impl(int metric, int S, int words, bool fast_ok, int pb) {
+    bool fast = false;
+    if constexpr (std::is_same<T, float>::value)
+        fast = fast_ok && (size_t)S * 4 * 16 + 32 * (size_t)words <= 100 * 1024 &&
+               (metric <= 2 || (metric >= 6 && metric <= 9));
+    return metric * 4 + (fast ? (pb == 4 ? 1 : 2) : 0);
+}
+
+// grid over the largest instance of a group; PB permutations per thread,
+// `lab` bytes of packed class weights per sample (0 for the exact form)
+template <class T>
+void multi_extent(const MetricTask<T>* h, int n, int PB, size_t lab, dim3& grid, size_t& smem) {
+    unsigned gx = 1, gy = 1;
+    smem = 0;
+    for (int i = 0; i < n; i++) {
+        gx = std::max(gx, (unsigned)((h[i].G + 127) / 128));
+        gy = std::max(gy, (unsigned)((h[i].num_perms + PB - 1) / PB));
+        smem = std::max(smem, lab * (size_t)h[i].S + sizeof(uint32_t) * PB * (size_t)h[i].words);
+    }
+    grid = dim3(gx, gy, (unsigned)n);
+}
+
+template <int ACC, int COMB, int PB>
+cudaError_t launch_fast_multi_pb(const MetricTask<float>* d, const MetricTask<float>* h, int n, cudaStream_t st) {
+    dim3 grid;
+    size_t smem;
+    multi_extent<float>(h, n, PB, sizeof(ulonglong2) * (PB / 2), grid, smem);
+    auto kern = metric_fast_multi<ACC, COMB, PB>;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    kern<<<grid, 128, smem, st>>>(d);
+    launches_add(1);
+    return cudaGetLastError();
+}
+
+template <int ACC, int COMB, class T>
+cudaError_t launch_exact_multi(const MetricTask<T>* d, const MetricTask<T>* h, int n, cudaStream_t st) {
+    constexpr int PB = 8;
+    dim3 grid;
+    size_t smem;
+    multi_extent<T>(h, n, PB, 0, grid, smem);
+    auto kern = metric_multi<ACC, COMB, T, PB>;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    kern<<<grid, 128, smem, st>>>(d);
+    launches_add(1);
+    return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_metric_multi_impl(int key, const MetricTask<T>* d, const MetricTask<T>* h, int n,
+                                     cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (n > 65535) return cudaErrorInvalidValue;
+    for (int i = 0; i < n; i++)
+        if ((h[i].num_perms + 7) / 8 > 65535) return cudaErrorInvalidValue;
+    const int metric = key / 4, path = key % 4;
+    if constexpr (std::is_same<T, float>::value) {
+        if (path != 0) {
+#define GSEA_F(ID, A, C)                                                                   \
+    case ID:                                                                              \
+        return path == 1 ? launch_fast_multi_pb<A, C, 4>(d, h, n, st) : launch_fast_multi_pb<A, C, 8>(d, h, n, st);
+            switch (metric) {
+                GSEA_F(0, ACC_NAIVE, COMB_DIFF)
+                GSEA_F(1, ACC_NAIVE, COMB_RATIO)
+                GSEA_F(2, ACC_NAIVE, COMB_LOG2)
+                GSEA_F(6, ACC_ONEPASS, COMB_S2N)
+                GSEA_F(7, ACC_ONEPASS, COMB_TTEST)
+                GSEA_F(8, ACC_TWOPASS, COMB_S2N)
+                GSEA_F(9, ACC_TWOPASS, COMB_TTEST)
+                default:
+                    return cudaErrorInvalidValue;
+            }
+#undef GSEA_F
+        }
+    }
+    if (path != 0) return cudaErrorInvalidValue;
+#define GSEA_X(ID, A, C) \
+    case ID:             \
+        return launch_exact_multi<A, C, T>(d, h, n, st);
+    switch (metric) {
+        GSEA_X(0, ACC_NAIVE, COMB_DIFF)
+        GSEA_X(1, ACC_NAIVE, COMB_RATIO)
+        GSEA_X(2, ACC_NAIVE, COMB_LOG2)
+        GSEA_X(3, ACC_KAHAN, COMB_DIFF)
+        GSEA_X(4, ACC_KAHAN, COMB_RATIO)
+        GSEA_X(5, ACC_KAHAN, COMB_LOG2)
+        GSEA_X(6, ACC_ONEPASS, COMB_S2N)
+        GSEA_X(7, ACC_ONEPASS, COMB_TTEST)
+        GSEA_X(8, ACC_TWOPASS, COMB_S2N)
+        GSEA_X(9, ACC_TWOPASS, COMB_TTEST)
+        GSEA_X(10, ACC_KNUTH, COMB_S2N)
+        GSEA_X(11, ACC_KNUTH, COMB_TTEST)
+        GSEA_X(12, ACC_OVERKILL, COMB_S2N)
+        GSEA_X(13, ACC_OVERKILL, COMB_TTEST)
+        default:
+            return cudaErrorInvalidValue;
+    }
+#undef GSEA_X
 }
 
 }  // namespace gsea

@@ -22,8 +22,10 @@
 //                      exchanged separately), one CTA up to 10,240 genes,
 //                      two up to 20,480.
 //   sort_tiled_kernel  any key width and any G: the segment ping-pongs
-//                      between two per-CTA global (L2-resident) buffers and
-//                      each pass streams it in tiles of 4,096 items.
+//                      between two per-CTA global buffers; one read counts
+//                      the digits of every pass, and each pass streams the
+//                      segment in tiles of 4,096 items staged in shared
+//                      memory by double-buffered bulk copies.
 //
 // Outputs per permutation: ranks[g] (position of gene g), sorted_abs[r]
 // (|metric| of the gene at position r, the running-sum weight of
@@ -31,6 +33,7 @@
 #include <cooperative_groups.h>
 #include <type_traits>
 
+#include "bulk.cuh"
 #include "common.cuh"
 #include "kernels.h"
 
@@ -85,50 +88,57 @@ __device__ __forceinline__ void emit(int64_t base, int pos, uint32_t gene, T v, 
     if (order) order[base + pos] = gene;
 }
 
-// Digit-major exclusive scan of cnt[w][d] (w < kWarps, d < 256).  On return
-// cnt[w][d] is the first destination of warp w's items with digit d and
-// tot[d] the digit total.  With base == nullptr the destinations are those of
-// a sort of this tile alone (digit prefix + earlier warps); with base they are
-// base[d] + earlier warps, base[d] being the running output offset of digit d.
-// Must be called by all threads; contains __syncthreads().
-__device__ void scan_counters(uint32_t (*cnt)[256], uint32_t* tot, const uint32_t* base,
-                              uint32_t* warp_sums) {
-    const int tid = threadIdx.x;
+// Offsets of a tile's items (all 1,024 threads; four __syncthreads()).  In:
+// cnt[w][d], the count of warp w's items with digit d (w < 32, d < 256); base[d],
+// the running output offset of digit d.  Out: cnt[w][d] = the tile-local
+// position of warp w's first item with digit d (digit-major: the digit's
+// start in the tile plus the earlier warps' items), delta[d] = base[d] - the
+// digit's start in the tile (a tile position + delta is the destination),
+// base[d] advanced by the tile's count.  Thread (q, d) scans warps 8q..8q+7 of
+// digit d; warps 0-7 scan the 256 digit totals.
+__device__ __forceinline__ void tile_offsets(uint32_t (*cnt)[256], uint32_t (*qsum)[256], uint32_t* warp_sums,
+                                             uint32_t* toff, uint32_t* delta, uint32_t* base) {
+    static_assert(kWarps == 32, "four quarters of eight warps");
+    const int d = threadIdx.x & 255, q = threadIdx.x >> 8, lane = threadIdx.x & 31;
+    uint32_t c[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) c[i] = cnt[8 * q + i][d];
     uint32_t run = 0;
-    if (tid < 256) {
-        for (int w = 0; w < kWarps; w++) {
-            const uint32_t c = cnt[w][tid];
-            cnt[w][tid] = run;
-            run += c;
-        }
-        tot[tid] = run;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const uint32_t x = c[i];
+        c[i] = run;
+        run += x;
     }
-    if (base) {
-        if (tid < 256) {
-            const uint32_t b = base[tid];
-            for (int w = 0; w < kWarps; w++) cnt[w][tid] += b;
-        }
-        __syncthreads();
-        return;
-    }
-    // exclusive scan of the 256 totals (8 warps of 32)
-    uint32_t incl = run;
-    if (tid < 256) {
-        const int lane = tid & 31;
+    qsum[q][d] = run;
+    __syncthreads();
+    uint32_t off = 0;
+    for (int j = 0; j < q; j++) off += qsum[j][d];
+    if (q == 0) {  // warps 0-7: exclusive scan of the digit totals
+        const uint32_t total = qsum[0][d] + qsum[1][d] + qsum[2][d] + qsum[3][d];
+        uint32_t incl = total;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t y = __shfl_up_sync(kFullMask, incl, o);
             if (lane >= o) incl += y;
         }
-        if (lane == 31) warp_sums[tid >> 5] = incl;
+        if (lane == 31) warp_sums[d >> 5] = incl;
+        toff[d] = incl - total;  // within its group of 32 digits; groups added below
+        delta[d] = total;        // the digit total, until the groups are added
     }
     __syncthreads();
-    if (tid < 256) {
+    if (q == 0) {
         uint32_t before = 0;
-        for (int w = 0; w < (tid >> 5); w++) before += warp_sums[w];
-        const uint32_t excl = before + incl - run;
-        for (int w = 0; w < kWarps; w++) cnt[w][tid] += excl;
+        for (int w = 0; w < (d >> 5); w++) before += warp_sums[w];
+        const uint32_t start = toff[d] + before, total = delta[d];
+        toff[d] = start;
+        delta[d] = base[d] - start;
+        base[d] += total;
     }
+    __syncthreads();
+    off += toff[d];
+#pragma unroll
+    for (int i = 0; i < 8; i++) cnt[8 * q + i][d] = c[i] + off;
     __syncthreads();
 }
 
@@ -482,48 +492,112 @@ size_t cluster_smem_bytes() {
 }
 
 // ---------------------------------------------------------------------------
+// Tiled form (any key width, any G).  Each CTA owns two global ping-pong
+// buffers of (radix key, gene id) with rows of Gp = G rounded up to a
+// multiple of 4 items, so that every tile starts and ends on a 16-byte
+// boundary.  Per permutation: one read of its metric values writes the radix
+// keys into buffer A and counts the digits of every pass at once (one
+// histogram per digit position); then every pass whose digit is not uniform
+// streams buffer A in tiles of 4,096 items.  Each tile is staged in shared
+// memory by bulk copies (keys, gene ids) into one of three stage buffers --
+// the next two tiles' copies in flight while it is ranked -- ranked within
+// its warps, put in digit order in the stage buffer it came from, and written
+// to buffer B in runs of equal digits (consecutive threads, consecutive
+// destinations).  The first pass that moves anything takes the gene ids as
+// the identity and copies keys only.
 constexpr int kTileItems = 4;
 constexpr int kTile = kThreads * kTileItems;
+
+__host__ __device__ __forceinline__ int tiled_row(int G) { return (G + 3) & ~3; }
+template <class U>
+__host__ __device__ __forceinline__ size_t tiled_cta_bytes(int G) {
+    return (sizeof(U) + sizeof(uint32_t)) * 2 * (size_t)tiled_row(G);
+}
+// the stage buffers (keys, then gene ids): two tiles in flight while one is
+// ranked
+constexpr int kStages = 3;
+template <class U>
+constexpr size_t tiled_stage_bytes() { return kStages * (size_t)kTile * (sizeof(U) + sizeof(uint32_t)); }
+
+// tile t of a (key, gene id) buffer into stage buffer b, completing on
+// bar[b] (one thread); sizes rounded up to 16 bytes stay inside the
+// tiled_row(G)-item rows.  With ident the gene ids are not copied.
+template <class U>
+__device__ __forceinline__ void tiled_issue(U* s_key, uint32_t* s_val, unsigned long long* bar, const U* kA,
+                                            const uint32_t* vA, bool ident, int G, int t, int b) {
+    const int t0 = t * kTile;
+    const int n = min(kTile, G - t0);
+    const uint32_t kbytes = (uint32_t)(((size_t)n * sizeof(U) + 15) & ~(size_t)15);
+    const uint32_t vbytes = ident ? 0u : (uint32_t)(((size_t)n * 4 + 15) & ~(size_t)15);
+    const uint32_t bb = smem_u32(&bar[b]);
+    fence_proxy_async();
+    mbar_expect_tx(bb, kbytes + vbytes);
+    bulk_copy(smem_u32(s_key + (size_t)b * kTile), kA + t0, kbytes, bb);
+    if (vbytes) bulk_copy(smem_u32(s_val + (size_t)b * kTile), vA + t0, vbytes, bb);
+}
 
 template <class T, class RankT>
 __global__ void __launch_bounds__(kThreads, 1)
 sort_tiled_kernel(const T* __restrict__ keys, int G, int num_perms, bool descending,
                   RankT* __restrict__ ranks, T* __restrict__ sorted_abs, uint32_t* __restrict__ order,
-                  unsigned char* __restrict__ scratch, bool stage_ranks) {
+                  unsigned char* __restrict__ scratch, bool stage_ranks, int* __restrict__ error_flag) {
     using U = typename RadixKey<T>::U;
-    extern __shared__ __align__(16) unsigned char dyn_smem[];  // [G] RankT when stage_ranks
+    constexpr int NPASS = (int)sizeof(U);
+    // stage buffers [2][kTile] keys and [2][kTile] gene ids; after the
+    // passes, the ranks by gene when stage_ranks
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    U* const s_key = reinterpret_cast<U*>(dyn_smem);
+    uint32_t* const s_val = reinterpret_cast<uint32_t*>(dyn_smem + kStages * (size_t)kTile * sizeof(U));
     __shared__ uint32_t cnt[kWarps][256];
-    __shared__ uint32_t hist[256];
+    __shared__ uint32_t qsum[4][256];
+    __shared__ uint32_t hist[NPASS][256];
     __shared__ uint32_t base[256];
-    __shared__ uint32_t tot[256];
+    __shared__ uint32_t toff[256];
+    __shared__ uint32_t delta[256];
     __shared__ uint32_t warp_sums[8];
-    __shared__ uint32_t skip_flag;
+    __shared__ int failed;
+    __shared__ __align__(8) unsigned long long bar[kStages];
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t lt = lanemask_lt();
-    const size_t per_cta = (sizeof(U) + sizeof(uint32_t)) * 2 * (size_t)G;
-    unsigned char* mine = scratch + per_cta * blockIdx.x;
-    U* kA = reinterpret_cast<U*>(mine);
-    U* kB = kA + G;
-    uint32_t* vA = reinterpret_cast<uint32_t*>(kB + G);
-    uint32_t* vB = vA + G;
+    const int Gp = tiled_row(G);
+    U* const k0 = reinterpret_cast<U*>(scratch + tiled_cta_bytes<U>(G) * blockIdx.x);
+    uint32_t* const v0 = reinterpret_cast<uint32_t*>(k0 + 2 * (size_t)Gp);
+    if (tid == 0) {
+        for (int b = 0; b < kStages; b++) mbar_init(smem_u32(&bar[b]), 1);
+        fence_mbar_init();
+        failed = 0;
+    }
+    __syncthreads();
+    uint32_t phases = 0u;  // bit b: parity of stage buffer b's barrier (the same in every thread)
+    const int ntiles = (G + kTile - 1) / kTile;
 
     for (int p = blockIdx.x; p < num_perms; p += gridDim.x) {
+        int a_off = 0;  // buffer A = rows at a_off, buffer B = rows at Gp - a_off
+        bool ident = true;  // buffer A's gene ids are the identity (not yet written)
         const T* kp = keys + (int64_t)p * G;
-        for (int i = tid; i < G; i += kThreads) {
-            kA[i] = RadixKey<T>::from(kp[i], descending);
-            vA[i] = (uint32_t)i;
-        }
+        for (int i = tid; i < NPASS * 256; i += kThreads) (&hist[0][0])[i] = 0u;
         __syncthreads();
-        for (int shift = 0; shift < 8 * (int)sizeof(U); shift += 8) {
-            if (tid < 256) hist[tid] = 0;
-            if (tid == 0) skip_flag = 0;
-            __syncthreads();
-            for (int i = tid; i < G; i += kThreads) atomicAdd(&hist[digit_of(kA[i], shift)], 1u);
-            __syncthreads();
-            // exclusive scan of hist into base
+#pragma unroll 4
+        for (int i = tid; i < G; i += kThreads) {
+            const U k = RadixKey<T>::from(kp[i], descending);
+            k0[i] = k;
+#pragma unroll
+            for (int s = 0; s < NPASS; s++) atomicAdd(&hist[s][digit_of(k, 8 * s)], 1u);
+        }
+        for (int s = 0; s < NPASS; s++) {
+            // histograms complete / the previous pass's scatter done; a
+            // uniform digit moves nothing
+            if (__syncthreads_or(tid < 256 && hist[s][tid] == (uint32_t)G)) continue;
+            const int shift = 8 * s;
+            if (tid == 0) {  // the first two tiles
+                tiled_issue<U>(s_key, s_val, bar, k0 + a_off, v0 + a_off, ident, G, 0, 0);
+                if (ntiles > 1) tiled_issue<U>(s_key, s_val, bar, k0 + a_off, v0 + a_off, ident, G, 1, 1);
+            }
+            // exclusive scan of this position's digit counts into base
             {
-                uint32_t v = tid < 256 ? hist[tid] : 0u, incl = v;
+                const uint32_t v = tid < 256 ? hist[s][tid] : 0u;
+                uint32_t incl = v;
                 if (tid < 256) {
 #pragma unroll
                     for (int o = 1; o < 32; o <<= 1) {
@@ -531,7 +605,6 @@ sort_tiled_kernel(const T* __restrict__ keys, int G, int num_perms, bool descend
                         if (lane >= o) incl += y;
                     }
                     if (lane == 31) warp_sums[warp] = incl;
-                    if (v == (uint32_t)G) skip_flag = 1;
                 }
                 __syncthreads();
                 if (tid < 256) {
@@ -539,22 +612,24 @@ sort_tiled_kernel(const T* __restrict__ keys, int G, int num_perms, bool descend
                     for (int w = 0; w < warp; w++) before += warp_sums[w];
                     base[tid] = before + incl - v;
                 }
-                __syncthreads();
             }
-            const bool skip = skip_flag != 0u;
-            __syncthreads();  // every thread has read the flag before it is reset
-            if (skip) continue;  // uniform: every key has the same digit
-            for (int t0 = 0; t0 < G; t0 += kTile) {
+            for (int t = 0, buf = 0; t < ntiles; t++, buf = buf == kStages - 1 ? 0 : buf + 1) {
+                const int t0 = t * kTile;
+                const int n = min(kTile, G - t0);
                 for (int d = lane; d < 256; d += 32) cnt[warp][d] = 0;
+                if (!mbar_wait(smem_u32(&bar[buf]), (phases >> buf) & 1u)) failed = 1;
+                phases ^= 1u << buf;
                 __syncwarp();
+                U* tk = s_key + (size_t)buf * kTile;
+                uint32_t* tv = s_val + (size_t)buf * kTile;
                 U k[kTileItems];
                 uint32_t v[kTileItems], r[kTileItems], dg[kTileItems];
 #pragma unroll
                 for (int i = 0; i < kTileItems; i++) {
-                    const int pos = t0 + warp * 32 * kTileItems + 32 * i + lane;
-                    const bool valid = pos < G;
-                    k[i] = valid ? kA[pos] : U(0);
-                    v[i] = valid ? vA[pos] : 0u;
+                    const int l = warp * 32 * kTileItems + 32 * i + lane;
+                    const bool valid = l < n;
+                    k[i] = valid ? tk[l] : U(0);
+                    v[i] = valid ? (ident ? (uint32_t)(t0 + l) : tv[l]) : 0u;
                     dg[i] = valid ? digit_of(k[i], shift) : 256u;
                     const uint32_t peers = match_digit<9>(dg[i]);
                     const int leader = __ffs(peers) - 1;
@@ -563,29 +638,61 @@ sort_tiled_kernel(const T* __restrict__ keys, int G, int num_perms, bool descend
                     before = __shfl_sync(kFullMask, before, leader);
                     r[i] = before + __popc(peers & lt);
                 }
-                __syncthreads();
-                scan_counters(cnt, tot, base, warp_sums);
+                __syncthreads();  // counters complete; both stage buffers read
+                if (failed) {  // uniform: written before the barrier
+                    if (tid == 0) {
+                        // let the copies still in flight land before leaving
+                        mbar_wait(smem_u32(&bar[buf]), ((phases >> buf) & 1u) ^ 1u);
+                        const int nb = buf == kStages - 1 ? 0 : buf + 1;
+                        if (t + 1 < ntiles) mbar_wait(smem_u32(&bar[nb]), (phases >> nb) & 1u);
+                        if (error_flag) atomicExch(error_flag, 1);
+                    }
+                    return;
+                }
+                // tile t + 2's copies, into the buffer the previous tile used
+                if (tid == 0 && t + 2 < ntiles)
+                    tiled_issue<U>(s_key, s_val, bar, k0 + a_off, v0 + a_off, ident, G, t + 2,
+                                   buf == 0 ? kStages - 1 : buf - 1);
+                tile_offsets(cnt, qsum, warp_sums, toff, delta, base);
+                // the tile in digit order, in the stage buffer it came from ...
 #pragma unroll
                 for (int i = 0; i < kTileItems; i++) {
                     if (dg[i] < 256u) {
-                        const uint32_t d = cnt[warp][dg[i]] + r[i];
-                        kB[d] = k[i];
-                        vB[d] = v[i];
+                        const uint32_t lp = cnt[warp][dg[i]] + r[i];
+                        tk[lp] = k[i];
+                        tv[lp] = v[i];
                     }
                 }
-                if (tid < 256) base[tid] += tot[tid];
                 __syncthreads();
+                // ... then out in runs of equal digits: consecutive threads
+                // write consecutive destinations within a run
+                U* const kB = k0 + (Gp - a_off);
+                uint32_t* const vB = v0 + (Gp - a_off);
+#pragma unroll
+                for (int i = 0; i < kTileItems; i++) {
+                    const int lp = tid + i * kThreads;
+                    if (lp < n) {
+                        const U key = tk[lp];
+                        const uint32_t dst = delta[digit_of(key, shift)] + (uint32_t)lp;
+                        kB[dst] = key;
+                        vB[dst] = tv[lp];
+                    }
+                }
             }
-            __syncthreads();
-            U* tk = kA; kA = kB; kB = tk;
-            uint32_t* tv = vA; vA = vB; vB = tv;
+            a_off = Gp - a_off;
+            ident = false;
         }
+        __syncthreads();
         const int64_t b = (int64_t)p * G;
+        const U* kA = k0 + a_off;
+        const uint32_t* vA = v0 + a_off;
         if (stage_ranks) {
-            // ranks by gene gathered in shared memory, then written coalesced
+            // ranks by gene gathered in shared memory (over the stage
+            // buffers, idle now), then written coalesced
             RankT* s_rk = reinterpret_cast<RankT*>(dyn_smem);
+#pragma unroll 4
             for (int pos = tid; pos < G; pos += kThreads) {
-                const uint32_t gene = vA[pos];
+                const uint32_t gene = ident ? (uint32_t)pos : vA[pos];
                 s_rk[gene] = (RankT)pos;
                 sorted_abs[b + pos] = cuabs(value_of<T>(kA[pos], descending));
                 if (order) order[b + pos] = gene;
@@ -593,15 +700,12 @@ sort_tiled_kernel(const T* __restrict__ keys, int G, int num_perms, bool descend
             __syncthreads();
             for (int g = tid; g < G; g += kThreads) ranks[b + g] = s_rk[g];
         } else {
+#pragma unroll 4
             for (int pos = tid; pos < G; pos += kThreads)
-                emit<RankT, T>(b, pos, vA[pos], value_of<T>(kA[pos], descending), ranks, sorted_abs, order);
+                emit<RankT, T>(b, pos, ident ? (uint32_t)pos : vA[pos], value_of<T>(kA[pos], descending), ranks,
+                               sorted_abs, order);
         }
         __syncthreads();
-        // restore the buffer roles for the next permutation
-        kA = reinterpret_cast<U*>(mine);
-        kB = kA + G;
-        vA = reinterpret_cast<uint32_t*>(kB + G);
-        vB = vA + G;
     }
 }
 
@@ -681,19 +785,22 @@ cudaError_t launch_sort_t(const T* keys, int G, int P, bool desc, const SortBuff
         if (G <= 2 * kThreads * 20) return launch_cluster<T, RankT, 20, 2>(keys, G, P, desc, o, st);
       }
     }
+    using U = typename RadixKey<T>::U;
     const int grid = P < num_sms() ? P : num_sms();
     if (o.scratch_bytes < sort_scratch_bytes<T>(G, P)) return cudaErrorInvalidValue;
-    // stage the ranks by gene in shared memory when they fit beside the
-    // kernel's static counters (~33 KB)
+    // the bulk copies read the scratch rows from 16-byte boundaries
+    if (reinterpret_cast<uintptr_t>(o.scratch) & 15u) return cudaErrorInvalidValue;
+    // stage the ranks by gene in shared memory (over the stage buffers) when
+    // they fit beside the kernel's static counters (~42 KB)
     const size_t rbytes = sizeof(RankT) * (size_t)G;
     const bool stage = rbytes <= 160 * 1024;
-    const size_t dyn = stage ? rbytes : 0;
+    const size_t dyn = stage && rbytes > tiled_stage_bytes<U>() ? rbytes : tiled_stage_bytes<U>();
     auto kern = sort_tiled_kernel<T, RankT>;
-    // opt in every time: static (~35 KB) + dynamic may pass the 48 KB default
+    // opt in every time: static + dynamic pass the 48 KB default
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     if (e != cudaSuccess) return e;
     kern<<<grid, kThreads, dyn, st>>>(keys, G, P, desc, static_cast<RankT*>(o.ranks), static_cast<T*>(o.sorted_abs),
-                                      o.order, static_cast<unsigned char*>(o.scratch), stage);
+                                      o.order, static_cast<unsigned char*>(o.scratch), stage, o.error_flag);
     launches_add(1);
     return cudaGetLastError();
 }
@@ -768,7 +875,7 @@ size_t sort_scratch_bytes(int G, int num_perms) {
     using U = typename RadixKey<T>::U;
     // sized for the tiled variant, which any G may be tuned to
     const int grid = num_perms < num_sms() ? num_perms : num_sms();
-    return (sizeof(U) + sizeof(uint32_t)) * 2 * (size_t)G * (size_t)(grid > 0 ? grid : 1);
+    return tiled_cta_bytes<U>(G) * (size_t)(grid > 0 ? grid : 1);
 }
 template size_t sort_scratch_bytes<float>(int, int);
 template size_t sort_scratch_bytes<double>(int, int);

@@ -20,6 +20,27 @@ cudaError_t launch_metric(int metric, const T* exprs, int G, int S, const uint32
                           const int* fast_ok, cudaStream_t st, int pb = 0);
 // (pb: permutations per thread of the packed fp32 form, 4 or 8; 0 = 8)
 
+// Batched instances: one launch of the metric over every instance of a group
+// (blockIdx.z = instance), keys bit-identical to launch_metric's.  Instances
+// share a group when metric_multi_key agrees (metric, and the path -- exact or
+// packed with pb permutations per thread -- that launch_metric takes; fast_ok:
+// the instance has a finite-check flag).  At most 65,535 instances and
+// 524,280 permutations per instance.
+template <class T>
+struct MetricTask {
+    const T* X;
+    const uint32_t* masks;
+    T* keys;
+    const int* fast_ok;
+    int G, S, words, num_perms;
+    T nA, nB;
+};
+template <class T>
+int metric_multi_key(int metric, int S, int words, bool fast_ok, int pb);
+template <class T>
+cudaError_t launch_metric_multi(int key, const MetricTask<T>* d_tasks, const MetricTask<T>* h_tasks, int n,
+                                cudaStream_t st);
+
 // fast_ok = 1 if every expression value is finite with |x| < 2^60, else 0
 template <class T>
 cudaError_t launch_finite_check(const T* exprs, int64_t n, int* fast_ok, cudaStream_t st);
@@ -36,6 +57,7 @@ struct SortBuffers {
     void* scratch;        // per-CTA ping-pong buffers for the tiled variant
     size_t scratch_bytes;
     int variant = 0;      // 0 automatic, 1 register radix sort (fp32, G <= 40,960; two-CTA clusters above 20,480), 2 tiled
+    int* error_flag = nullptr;  // set to 1 when a bounded wait of the tiled sort expires
 };
 template <class T>
 size_t sort_scratch_bytes(int G, int num_perms);

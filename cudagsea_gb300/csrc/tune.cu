@@ -105,6 +105,7 @@ int autotune_t(gsea_plan_s* p, int64_t n64, unsigned stages, gsea_tuning* best_o
     sb.order = nullptr;
     sb.scratch = p->sort_scratch;
     sb.scratch_bytes = p->sort_scratch_bytes;
+    sb.error_flag = p->dev_error;
     float sbest = 1e30f;
     std::vector<int> sc = {1, 2};
     if (!(stages & kSort)) sc = {best.sort_variant};

@@ -4,7 +4,7 @@ one kernel stays small.  Used by the commands recorded under profiles/.
 
     python -m cudagsea_gb300.profile_case [--perms 152] [--reps 2]
         [--precision 32|64] [--form plain|chosen|chosen64] [--batch 0]
-        [--model 0] [--genes 20000] [--adaptive 0]
+        [--model 0] [--genes 20000] [--adaptive 0] [--sort-variant 0]
 
 --batch N   runs N uneven instances through gsea_batch instead (the
             persistent multi-instance enrichment kernel)
@@ -12,6 +12,8 @@ one kernel stays small.  Used by the commands recorded under profiles/.
             run (the model kernels)
 --genes G   the same data with G genes (the large-G sort and enrichment
             variants: two-CTA cluster sort, ranks-only staging)
+--sort-variant V
+            1 register / cluster sort, 2 tiled sort (0: the automatic choice)
 --adaptive P0
             one adaptive test (both stopping rules, no model) with a pilot of
             P0 permutations on the allocator workload (20,000 sets, 100,000
@@ -37,6 +39,7 @@ def main(argv=None) -> int:
     ap.add_argument("--model", type=int, default=0)
     ap.add_argument("--genes", type=int, default=20000)
     ap.add_argument("--adaptive", type=int, default=0)
+    ap.add_argument("--sort-variant", type=int, default=0)
     a = ap.parse_args(argv)
     build.build()
     if a.adaptive:
@@ -66,6 +69,8 @@ def main(argv=None) -> int:
                            clamp=1e-3, name=f"full_{a.genes}x200_K1000_P{a.perms}")
     plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, a.perms, "twopass_signal2noise",
                     precision=a.precision, form=FORMS[a.form])
+    if a.sort_variant:
+        plan.set_tuning(sort_variant=a.sort_variant)
     plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
     plan.set_profiling(True)
     for i in range(a.reps):

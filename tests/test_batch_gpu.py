@@ -61,22 +61,26 @@ def test_batch_matches_solo_plans(gpu, precision, form):
     if form == N.FORM_CHOSEN:
         # permute 1 + metric 3 + sort classes + ES classes + statistics 9
         assert info["launches"] <= 1 + 3 + 7 + info["es_classes"] + 9, info
+    else:
+        # permute 1 + one metric launch per metric + sort classes (+ the fp64
+        # instance beyond the register sort) + ES classes + statistics 9
+        assert info["launches"] <= 1 + len(set(metrics)) + 7 + 1 + info["es_classes"] + 9, info
     b.close()
 
 
-def test_batch_of_40_uneven_instances_matches_solo_plans(gpu):
+@pytest.mark.parametrize("form", [N.FORM_CHOSEN, N.FORM_PLAIN])
+def test_batch_of_40_uneven_instances_matches_solo_plans(gpu, form):
     """40 instances with genes U[1,000, 30,000], samples U[20, 200], sets
-    U[10, 300] and permutations U[64, 600] (tensor-core form, one metric): the
-    batched execute equals every solo plan bit for bit, and issues a handful
-    of launches -- one per stage (and per sort / enrichment class), not one
-    per instance."""
+    U[10, 300] and permutations U[64, 600] (one metric): the batched execute
+    equals every solo plan bit for bit, and issues a handful of launches --
+    one per stage (and per sort / enrichment class), not one per instance."""
     ds = synthetic.batch_instances(40, seed=5, num_perms=64, genes=(1000, 30000), samples=(20, 200),
                                    sets=(10, 300), set_size=(15, 200))
     rs = np.random.RandomState(9)
     for d in ds:
         d.num_perms = int(rs.randint(64, 601))
-    ref = [solo(d, "twopass_signal2noise", 32, N.FORM_CHOSEN) for d in ds]
-    b = api.Batch(ds, "twopass_signal2noise", precision=32, form=N.FORM_CHOSEN)
+    ref = [solo(d, "twopass_signal2noise", 32, form) for d in ds]
+    b = api.Batch(ds, "twopass_signal2noise", precision=32, form=form)
     for rep in range(2):
         b.execute()
         b.synchronize()

@@ -25,10 +25,13 @@ from tests.golden import make_golden as MG
 pytestmark = pytest.mark.gpu
 
 
-def run_plan(d, metric, double=False, P=None, perm_offset=0, perm_batch=0, ascending=False, debug=True):
+def run_plan(d, metric, double=False, P=None, perm_offset=0, perm_batch=0, ascending=False, debug=True,
+             tuning=None):
     P = P or d.num_perms
     plan = api.Plan(d.num_genes, d.num_samples, d.num_sets, P, metric, precision=64 if double else 32,
                     ascending=ascending, perm_offset=perm_offset, perm_batch=perm_batch)
+    if tuning:
+        plan.set_tuning(**tuning)
     if debug:
         plan.set_debug(True)
     plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
@@ -159,6 +162,37 @@ def test_sort_sizes(gpu, G, double):
     sk, order = check_sort(r["keys"], r["order"], r["ranks"], r["sorted"])
     es_o = oracle.es(sk, order, d.set_offsets, d.set_genes)
     assert H.es_close(r["es"], es_o, double).all()
+
+
+@pytest.mark.parametrize("G", [4095, 4097, 8194, 12289, 41003])
+@pytest.mark.parametrize("double", [False, True], ids=["f32", "f64"])
+def test_tiled_sort_edge_keys(gpu, G, double):
+    """The tiled sort (tiles of 4,096 keys staged in shared memory by bulk
+    copies, one digit count for every pass) on tied, infinite and NaN keys,
+    with tile boundaries and rows whose length is not a multiple of 4, and 160
+    permutations so that each CTA sorts several permutations in turn: order,
+    ranks and weights equal the oracle's stable sort, ES the oracle's."""
+    d = synthetic.make(G, 10, 4, 160, seed=G, n_class_b=5, set_min=5, set_max=min(300, G))
+    t = G // 3
+    d.exprs[:, :t] = d.exprs[:, [t + 100]]  # a third of the genes tie
+    d.exprs[:, t:t + 40] = 0.0              # 0 / 0
+    d.exprs[:4, t + 40:t + 80] = 0.0        # zero means in some permutations' classes
+    for metric in ("naive_ratio_of_classes", "twopass_signal2noise"):
+        r = run_plan(d, metric, double=double, tuning=dict(sort_variant=2))
+        sk, order = check_sort(r["keys"], r["order"], r["ranks"], r["sorted"])
+        es_o = oracle.es(sk, order, d.set_offsets, d.set_genes)
+        assert H.es_close(r["es"], es_o, double).all(), metric
+
+
+@pytest.mark.parametrize("double", [False, True], ids=["f32", "f64"])
+def test_tiled_sort_all_keys_equal(gpu, double):
+    """Every gene identical: every radix digit is uniform, no pass moves a key,
+    and the order is the identity (stable)."""
+    d = synthetic.make(9000, 10, 3, 20, seed=4, n_class_b=5, set_min=5, set_max=200)
+    d.exprs[:] = d.exprs[:, [0]]
+    r = run_plan(d, "twopass_signal2noise", double=double, tuning=dict(sort_variant=2))
+    sk, order = check_sort(r["keys"], r["order"], r["ranks"], r["sorted"])
+    assert (order == np.arange(d.num_genes)[None, :]).all()
 
 
 def test_ascending_order(gpu):
