@@ -13,16 +13,16 @@
 // Operands: x' and x'^2 are split into three BF16 parts each (hi + mid + lo
 // carries ~24 significant bits) stacked along K, the labels are exact 0/1 in
 // BF16 and repeated for each part, so one BF16 x BF16 -> FP32 GEMM of depth
-// 3*S gives each sum.  A CTA owns 128 genes x 128 (two CTAs per SM, 2
-// stages, the default) or 256 permutations (one CTA per SM, 3 stages):
+// 3*S gives each sum.  A CTA owns 128 genes x 128 (two CTAs per SM, 4
+// stages, the default) or 256 permutations (one CTA per SM, 6 stages):
 //   * two FP32 accumulators in tensor memory (SA in the first TN columns,
 //     SA2 in the next TN), allocated with tcgen05.alloc;
 //   * the operands are pre-arranged in the canonical no-swizzle K-major
-//     layout (8x8 core matrices of 128 bytes), 64 K-elements per chunk, so a
-//     chunk of A (16 KB), A2 (16 KB) and B (32 KB) is one contiguous 1-D TMA
-//     bulk copy each (cp.async.bulk) completing on an mbarrier; two or three
-//     stages in flight, a stage refilled as soon as the MMAs of its chunk
-//     retired;
+//     layout (8x8 core matrices of 128 bytes), 32 K-elements per chunk, so a
+//     chunk of A (8 KB), A2 (8 KB) and B (8 or 16 KB) is one contiguous 1-D
+//     TMA bulk copy each (cp.async.bulk) completing on an mbarrier; three or
+//     five stages in flight while one is multiplied, a stage refilled as
+//     soon as the MMAs of its chunk retired;
 //   * one thread issues tcgen05.mma (M=128, N=TN, K=16) with shared-memory
 //     descriptors and tcgen05.commit to the stage's mbarrier (the sums are
 //     the same MMA chain per element for either tile);
@@ -55,14 +55,15 @@ namespace chosen {
 
 constexpr int BM = 128;          // genes per CTA (TMEM lanes)
 constexpr int BN = 256;          // permutations per CTA (the default tile; 128 is the other)
-constexpr int BK = 64;           // K elements per chunk
-constexpr int A_CHUNK = BM * BK * 2;   // 16 KB
-constexpr int B_CHUNK = BN * BK * 2;   // 32 KB (a 128-permutation tile uses half)
-// pipeline stages: 3 for the 256-permutation tile (192 KB, one CTA per SM);
-// 2 for the 128-permutation tile (96 KB and 256 TMEM columns: two CTAs per
-// SM, so one CTA's epilogue runs beside the other's loads and MMAs)
+constexpr int BK = 32;           // K elements per chunk
+constexpr int A_CHUNK = BM * BK * 2;   // 8 KB
+constexpr int B_CHUNK = BN * BK * 2;   // 16 KB (a 128-permutation tile uses half)
+// pipeline stages: 6 for the 256-permutation tile (192 KB, one CTA per SM);
+// 4 for the 128-permutation tile (96 KB and 256 TMEM columns: two CTAs per
+// SM, so one CTA's epilogue runs beside the other's loads and MMAs).  Small
+// chunks keep several stages' copies in flight while one is multiplied.
 template <int TN>
-constexpr int stages() { return TN == 128 ? 2 : 3; }
+constexpr int stages() { return TN == 128 ? 4 : 6; }
 template <int TN>
 constexpr int stage_bytes() { return 2 * A_CHUNK + TN * BK * 2; }
 constexpr int THREADS = 256;     // 8 warps: two per TMEM lane quarter in the epilogue

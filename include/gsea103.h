@@ -307,7 +307,8 @@ int gsea_plan_autotune(gsea_plan plan, int64_t sample_perms, gsea_tuning* best, 
  *      (num_genes <= 65,536).  An execute runs each stage as one launch
  *      over every instance (one device batch: num_perms x num_genes buffers
  *      per instance): the permutations; the metric (tensor-core form: one
- *      launch set per metric family); the sort (one launch per
+ *      launch set per metric family; plain form: one launch per metric and
+ *      kernel path); the sort (one launch per
  *      register-resident class; instances beyond the register forms sort on
  *      their own); one persistent enrichment launch per size class (bitmap
  *      words per lane) whose CTAs pull (instance, permutation) items,
@@ -315,9 +316,9 @@ int gsea_plan_autotune(gsea_plan plan, int64_t sample_perms, gsea_tuning* best, 
  *      instance's results are its solo plan's bit for bit.  The first
  *      execute captures all of it into one CUDA graph; later executes
  *      replay that graph (gsea_batch_set_inputs or gsea_batch_autotune make
- *      the next execute capture again).  gsea_batch_autotune tunes the
- *      enrichment launch per size class (the other stages have one launch
- *      shape in the batched form).                                        */
+ *      the next execute capture again).  gsea_batch_autotune tunes every
+ *      instance's plain metric (permutations per thread, which picks its
+ *      launch group) and the enrichment launch per size class.            */
 typedef struct gsea_batch_s* gsea_batch;
 /* streams: size of the stream pool (0 = 16) over which an execute spreads
  * the sort classes and the enrichment size classes */
