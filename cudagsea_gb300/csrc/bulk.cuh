@@ -25,6 +25,9 @@ __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
 __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
@@ -39,6 +42,15 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     const long long t0 = clock64();
     while (!mbar_try(bar, parity)) {
         if (clock64() - t0 > kWaitCycles) return false;
+    }
+    return true;
+}
+// bounded wait that also gives up when another role of the CTA recorded a
+// failure in *failed
+__device__ __forceinline__ bool mbar_wait_or_fail(uint32_t bar, uint32_t parity, const volatile int* failed) {
+    const long long t0 = clock64();
+    while (!mbar_try(bar, parity)) {
+        if (*failed || clock64() - t0 > kWaitCycles) return false;
     }
     return true;
 }

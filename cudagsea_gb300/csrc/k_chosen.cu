@@ -156,6 +156,46 @@ __device__ __forceinline__ float variance(float ms, float m) {
     return (ms - p) - e;
 }
 
+// Epilogue of one warp: TMEM lane quarter `quarter` (genes 32*quarter..+31 of
+// gene tile gt), the 16-column blocks part, part + PARTS, ... of the two
+// accumulators at `acc` (SA in columns [0, TN), SA2 in [TN, 2*TN)): class
+// means, variances and the metric, keys[p][g] stored coalesced (a warp writes
+// 32 consecutive genes of one permutation at a time).
+template <int COMB, bool FP64SUB, int TN, int PARTS>
+__device__ __forceinline__ void tile_epilogue(uint32_t acc, int quarter, int part, int lane, int gt, int pt, int G,
+                                              int num_perms, const float* __restrict__ gene_mu,
+                                              const double* __restrict__ gene_t1,
+                                              const double* __restrict__ gene_t2, float nA, float nB,
+                                              float* __restrict__ keys) {
+    const int row = quarter * 32 + lane;   // TMEM lane = gene within the tile
+    const int g = gt * BM + row;
+    const bool gv = g < G;
+    const float mu = gv ? gene_mu[g] : 0.f;
+    const float t1 = gv ? (float)gene_t1[g] : 0.f, t2 = gv ? (float)gene_t2[g] : 0.f;
+    const float inA = 1.f / nA, inB = 1.f / nB;
+    const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+    for (int cb = part; cb < TN / 16; cb += PARTS) {
+        uint32_t va[16], vq[16];
+        tmem_ld16(acc + lane_base + cb * 16, va);
+        tmem_ld16(acc + lane_base + TN + cb * 16, vq);
+        tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+            const int p = pt * TN + cb * 16 + j;
+            const float sA = __uint_as_float(va[j]), sA2 = __uint_as_float(vq[j]);
+            // class means and mean squares (centred); B from the totals
+            const float mAc = sA * inA;
+            const float mBc = (t1 - sA) * inB;
+            const float eA = sA2 * inA;
+            const float eB = (t2 - sA2) * inB;
+            const float vA = variance<FP64SUB>(eA, mAc);
+            const float vB = variance<FP64SUB>(eB, mBc);
+            const float key = finalize<COMB>(mAc, mBc, mu, vA, vB, nA, nB);
+            if (gv && p < num_perms) keys[(size_t)p * G + g] = canonical_nan_f(key);
+        }
+    }
+}
+
 // one CTA = one tile of BM genes x TN permutations (gt, pt)
 template <int COMB, bool FP64SUB, int TN>
 __device__ __forceinline__ void
@@ -262,37 +302,9 @@ class_stats_tile(int gt, int pt, const unsigned char* __restrict__ A1, const uns
     __syncthreads();
     fence_after();
 
-    if (!failed) {
-        const int quarter = warp & 3;          // TMEM lanes 32*quarter .. +31
-        const int half = warp >> 2;            // column half handled by this warp
-        const int row = quarter * 32 + lane;   // TMEM lane = gene within the tile
-        const int g = gt * BM + row;
-        const bool gv = g < G;
-        const float mu = gv ? gene_mu[g] : 0.f;
-        const float t1 = gv ? (float)gene_t1[g] : 0.f, t2 = gv ? (float)gene_t2[g] : 0.f;
-        const float inA = 1.f / nA, inB = 1.f / nB;
-        const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
-        for (int cb = half * (TN / 32); cb < (half + 1) * (TN / 32); cb++) {
-            uint32_t va[16], vq[16];
-            tmem_ld16(tmem + lane_base + cb * 16, va);
-            tmem_ld16(tmem + lane_base + TN + cb * 16, vq);
-            tmem_wait_ld();
-#pragma unroll
-            for (int j = 0; j < 16; j++) {
-                const int p = pt * TN + cb * 16 + j;
-                const float sA = __uint_as_float(va[j]), sA2 = __uint_as_float(vq[j]);
-                // class means and mean squares (centred); B from the totals
-                const float mAc = sA * inA;
-                const float mBc = (t1 - sA) * inB;
-                const float eA = sA2 * inA;
-                const float eB = (t2 - sA2) * inB;
-                const float vA = variance<FP64SUB>(eA, mAc);
-                const float vB = variance<FP64SUB>(eB, mBc);
-                const float key = finalize<COMB>(mAc, mBc, mu, vA, vB, nA, nB);
-                if (gv && p < num_perms) keys[(size_t)p * G + g] = canonical_nan_f(key);
-            }
-        }
-    }
+    if (!failed)
+        tile_epilogue<COMB, FP64SUB, TN, 2>(tmem, warp & 3, warp >> 2, lane, gt, pt, G, num_perms, gene_mu, gene_t1,
+                                         gene_t2, nA, nB, keys);
     fence_before();
     __syncthreads();
     if (warp == 0) {
@@ -323,6 +335,185 @@ class_stats_multi(const ChosenTask* __restrict__ tasks) {
     if ((int)blockIdx.x * BM >= G || (int)blockIdx.y * TN >= P) return;
     class_stats_tile<COMB, FP64SUB, TN>(blockIdx.x, blockIdx.y, t.A1, t.A2, t.Bm, t.chunks, G, P, t.mu, t.t1, t.t2,
                                         t.nA, t.nB, t.keys, t.error_flag);
+}
+
+// ---------------------------------------------------------------------------
+// Persistent form of the 128-permutation tile (the default): one CTA per SM
+// walks the tiles t = blockIdx.x, blockIdx.x + gridDim.x, ... (gene tile
+// t / ptiles, permutation tile t % ptiles: neighbouring CTAs share operand
+// tiles in L2) with three roles:
+//   warp 0, one thread: the bulk copies of every chunk of every tile into a
+//     ring of PSTAGES shared-memory stages, a stage refilled as soon as the
+//     MMAs that read it retired (their commit arrives on the stage's `empty`);
+//   warp 1, one thread: the MMAs of each tile into one of two accumulator
+//     pairs in TMEM (2 x 2 x 128 columns = all 512), alternating, each
+//     chunk's commit freeing its stage and the tile's last commit handing
+//     the pair to the epilogue (`acc_full`);
+//   warps 2-17: the epilogue of the tile whose pair is full (four warps per
+//     TMEM lane quarter, each taking every fourth 16-column block) while the
+//     MMAs of the next
+//     tile run on the other pair; each warp hands the pair back with one
+//     arrival on `acc_empty` once its TMEM loads completed.
+// The MMA chain per key is the same as the one-tile form's, so the keys are
+// identical.  Every wait is bounded and also ends when another role has
+// failed; the failing role records the error flag, the MMA thread then waits
+// (bounded) for its MMAs and the copy thread for its copies before the CTA
+// frees its tensor memory.
+constexpr int PSTAGES = 8;              // 8 x 24 KB stages
+constexpr int PEPI = 16;                // epilogue warps: four per TMEM lane quarter
+constexpr int PTHREADS = 32 * (2 + PEPI);
+constexpr int PTN = 128;
+
+template <int COMB, bool FP64SUB>
+__global__ void __launch_bounds__(PTHREADS, 1)
+class_stats_persistent(const unsigned char* __restrict__ A1, const unsigned char* __restrict__ A2,
+                       const unsigned char* __restrict__ B, int chunks, int G, int num_perms,
+                       const float* __restrict__ gene_mu, const double* __restrict__ gene_t1,
+                       const double* __restrict__ gene_t2, float nA, float nB, float* __restrict__ keys,
+                       int* __restrict__ error_flag) {
+    constexpr int TB_CHUNK = PTN * BK * 2;
+    constexpr int TSTAGE = stage_bytes<PTN>();
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ __align__(8) uint64_t full[PSTAGES];
+    __shared__ __align__(8) uint64_t empty[PSTAGES];
+    __shared__ __align__(8) uint64_t acc_full[2];
+    __shared__ __align__(8) uint64_t acc_empty[2];
+    __shared__ __align__(8) uint64_t drain;
+    __shared__ uint32_t tmem_slot;
+    __shared__ volatile int failed;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int ptiles = (num_perms + PTN - 1) / PTN;
+    const int ntiles = ((G + BM - 1) / BM) * ptiles;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(&tmem_slot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 32) {
+        for (int s = 0; s < PSTAGES; s++) {
+            mbar_init(smem_u32(&full[s]), 1);
+            mbar_init(smem_u32(&empty[s]), 1);
+        }
+        for (int b = 0; b < 2; b++) {
+            mbar_init(smem_u32(&acc_full[b]), 1);
+            mbar_init(smem_u32(&acc_empty[b]), PEPI);
+        }
+        mbar_init(smem_u32(&drain), 1);
+        failed = 0;
+        fence_mbar_init();
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {  // copies
+            uint32_t n = 0;  // chunk loads issued: stage n % PSTAGES, its (n / PSTAGES)-th use
+            for (int t = blockIdx.x; t < ntiles && !failed; t += gridDim.x) {
+                const int gt = t / ptiles, pt = t - gt * ptiles;
+                for (int c = 0; c < chunks; c++, n++) {
+                    const int s = (int)(n % PSTAGES);
+                    const uint32_t k = n / PSTAGES;
+                    if (k > 0 && !mbar_wait_or_fail(smem_u32(&empty[s]), (k - 1) & 1u, &failed)) {
+                        failed = 1;
+                        break;
+                    }
+                    unsigned char* st = smem + (size_t)s * TSTAGE;
+                    const uint32_t bar = smem_u32(&full[s]);
+                    mbar_expect_tx(bar, TSTAGE);
+                    bulk_copy(smem_u32(st), A1 + ((size_t)gt * chunks + c) * A_CHUNK, A_CHUNK, bar);
+                    bulk_copy(smem_u32(st + A_CHUNK), A2 + ((size_t)gt * chunks + c) * A_CHUNK, A_CHUNK, bar);
+                    bulk_copy(smem_u32(st + 2 * A_CHUNK), B + ((size_t)pt * chunks + c) * TB_CHUNK, TB_CHUNK, bar);
+                }
+            }
+            if (failed) {
+                atomicExch(error_flag, 1);
+                // the last copies issued into each stage land before the CTA leaves
+                for (uint32_t m = n > PSTAGES ? n - PSTAGES : 0; m < n; m++)
+                    mbar_wait(smem_u32(&full[m % PSTAGES]), (m / PSTAGES) & 1u);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {  // MMAs
+            const uint32_t idesc = make_idesc(BM, PTN);
+            uint32_t n = 0;  // chunks consumed
+            int j = 0;       // tiles of this CTA
+            for (int t = blockIdx.x; t < ntiles && !failed; t += gridDim.x, j++) {
+                const int b = j & 1;
+                const uint32_t kb = (uint32_t)j >> 1;
+                if (kb > 0 && !mbar_wait_or_fail(smem_u32(&acc_empty[b]), (kb - 1) & 1u, &failed)) {
+                    failed = 1;
+                    break;
+                }
+                fence_after();
+                const uint32_t d = tmem + (uint32_t)(b * 2 * PTN);
+                bool ok = true;
+                for (int c = 0; c < chunks; c++, n++) {
+                    const int s = (int)(n % PSTAGES);
+                    if (!mbar_wait_or_fail(smem_u32(&full[s]), (n / PSTAGES) & 1u, &failed)) {
+                        ok = false;
+                        break;
+                    }
+                    fence_after();
+                    const uint32_t a1 = smem_u32(smem + (size_t)s * TSTAGE), a2 = a1 + A_CHUNK, bb = a1 + 2 * A_CHUNK;
+#pragma unroll
+                    for (int kk = 0; kk < BK / 16; kk++) {
+                        const uint32_t koff = kk * 256;
+                        const uint64_t da1 = make_desc(a1 + koff, 128, (BK / 8) * 128);
+                        const uint64_t da2 = make_desc(a2 + koff, 128, (BK / 8) * 128);
+                        const uint64_t db = make_desc(bb + koff, 128, (BK / 8) * 128);
+                        const uint32_t acc = (c > 0 || kk > 0) ? 1u : 0u;
+                        mma_bf16(d, da1, db, idesc, acc);
+                        mma_bf16(d + PTN, da2, db, idesc, acc);
+                    }
+                    mma_commit(smem_u32(&empty[s]));
+                }
+                if (!ok) {
+                    failed = 1;
+                    break;
+                }
+                mma_commit(smem_u32(&acc_full[b]));
+            }
+            if (failed) atomicExch(error_flag, 1);
+            // every MMA issued has retired before TMEM is freed
+            mma_commit(smem_u32(&drain));
+            mbar_wait(smem_u32(&drain), 0);
+        }
+    } else {  // epilogue
+        const int e = warp - 2;
+        const int quarter = warp & 3;  // the TMEM lane quarter this warp may read
+        const int part = e >> 2;
+        int j = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, j++) {
+            const int b = j & 1;
+            const uint32_t kb = (uint32_t)j >> 1;
+            int ok = 0;
+            if (lane == 0) ok = mbar_wait_or_fail(smem_u32(&acc_full[b]), kb & 1u, &failed) ? 1 : 0;
+            ok = __shfl_sync(kFullMask, ok, 0);
+            if (!ok) {
+                if (lane == 0) {
+                    failed = 1;
+                    atomicExch(error_flag, 1);
+                }
+                break;
+            }
+            fence_after();
+            const int gt = t / ptiles, pt = t - gt * ptiles;
+            tile_epilogue<COMB, FP64SUB, PTN, PEPI / 4>(tmem + (uint32_t)(b * 2 * PTN), quarter, part, lane, gt,
+                                                        pt, G, num_perms, gene_mu, gene_t1, gene_t2, nA, nB, keys);
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&acc_empty[b]));
+        }
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -528,6 +719,18 @@ template cudaError_t launch_chosen_prepare<float>(const float*, int, int, float*
                                                   unsigned char*, cudaStream_t);
 
 namespace {
+int sm_count() {
+    static int cached[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int& n = cached[dev & 63];
+    if (n <= 0) {
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
 template <int TN>
 cudaError_t launch_chosen_tn(int comb, bool fp64_variance, const uint32_t* masks, int words, int G, int S,
                              int num_perms, int64_t nA, int64_t nB, const float* mu, const double* t1,
@@ -539,15 +742,24 @@ cudaError_t launch_chosen_tn(int comb, bool fp64_variance, const uint32_t* masks
     cudaError_t e = cudaMemsetAsync(Bm, 0, bbytes, st);
     if (e != cudaSuccess) return e;
     label_operand_kernel<TN><<<dim3((num_perms + 127) / 128, S), 128, 0, st>>>(masks, words, S, num_perms, chunks, Bm);
-    const dim3 grid((G + BM - 1) / BM, (num_perms + TN - 1) / TN);
-    const size_t smem = (size_t)stages<TN>() * stage_bytes<TN>();
-#define GSEA_CHOSEN(C)                                                                                        \
-    {                                                                                                         \
-        auto kern = fp64_variance ? class_stats_kernel<C, true, TN> : class_stats_kernel<C, false, TN>;      \
-        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);               \
-        if (e != cudaSuccess) return e;                                                                       \
-        kern<<<grid, THREADS, smem, st>>>(A1, A2, Bm, chunks, G, num_perms, mu, t1, t2, (float)nA, (float)nB, \
-                                          keys, error_flag);                                                  \
+    dim3 grid((G + BM - 1) / BM, (num_perms + TN - 1) / TN);
+    size_t smem = (size_t)stages<TN>() * stage_bytes<TN>();
+    int threads = THREADS;
+    if (TN == PTN) {  // persistent: one CTA per SM over all tiles
+        const int tiles = (int)(grid.x * grid.y);
+        const int sms = sm_count();
+        grid = dim3((unsigned)(tiles < sms ? tiles : sms));
+        smem = (size_t)PSTAGES * stage_bytes<PTN>();
+        threads = PTHREADS;
+    }
+#define GSEA_CHOSEN(C)                                                                                         \
+    {                                                                                                          \
+        auto kern = TN == PTN ? (fp64_variance ? class_stats_persistent<C, true> : class_stats_persistent<C, false>) \
+                              : (fp64_variance ? class_stats_kernel<C, true, TN> : class_stats_kernel<C, false, TN>); \
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);                \
+        if (e != cudaSuccess) return e;                                                                        \
+        kern<<<grid, threads, smem, st>>>(A1, A2, Bm, chunks, G, num_perms, mu, t1, t2, (float)nA, (float)nB,  \
+                                          keys, error_flag);                                                   \
     }
     switch (comb) {
         case 0: GSEA_CHOSEN(0) break;
