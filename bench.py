@@ -264,8 +264,8 @@ def peaks():
 # the stage's kernel profile and what bounds it (read off that profile)
 STAGE_PROFILES = {"es": ("es_kernel_full_20000x200_K1000_152perms.md", "instruction issue"),
                   "sort": ("sort_regs_kernel_full_20000x200_152perms.md", "latency (barriers, ballots)"),
-                  ("metric", "chosen"): ("class_stats_kernel_full_20000x200_152perms.md",
-                                         "latency (epilogue, pipeline)"),
+                  ("metric", "chosen"): ("class_stats_persistent_full_20000x200_152perms.md",
+                                         "latency (epilogue)"),
                   ("metric", "plain"): ("metric_fast_kernel_full_20000x200_152perms.md", "latency (L2 loads)")}
 
 
