@@ -324,19 +324,6 @@ class_stats_kernel(const unsigned char* __restrict__ A1, const unsigned char* __
                                         gene_t2, nA, nB, keys, error_flag);
 }
 
-// every instance of a batch at once: blockIdx.z = the instance; the tiles
-// beyond an instance's genes or permutations return before any TMEM
-// allocation or barrier
-template <int COMB, bool FP64SUB, int TN>
-__global__ void __launch_bounds__(THREADS, TN == 128 ? 2 : 1)
-class_stats_multi(const ChosenTask* __restrict__ tasks) {
-    const ChosenTask& t = tasks[blockIdx.z];
-    const int G = t.G, P = t.num_perms;
-    if ((int)blockIdx.x * BM >= G || (int)blockIdx.y * TN >= P) return;
-    class_stats_tile<COMB, FP64SUB, TN>(blockIdx.x, blockIdx.y, t.A1, t.A2, t.Bm, t.chunks, G, P, t.mu, t.t1, t.t2,
-                                        t.nA, t.nB, t.keys, t.error_flag);
-}
-
 // ---------------------------------------------------------------------------
 // Persistent form of the 128-permutation tile (the default): one CTA per SM
 // walks the tiles t = blockIdx.x, blockIdx.x + gridDim.x, ... (gene tile
@@ -354,8 +341,9 @@ class_stats_multi(const ChosenTask* __restrict__ tasks) {
 //     MMAs of the next
 //     tile run on the other pair; each warp hands the pair back with one
 //     arrival on `acc_empty` once its TMEM loads completed.
-// The MMA chain per key is the same as the one-tile form's, so the keys are
-// identical.  Every wait is bounded and also ends when another role has
+// The same body serves a batch (class_stats_persistent_multi: the tiles of
+// every instance, instance after instance).  The MMA chain per key is the
+// same as the one-tile form's, so the keys are identical.  Every wait is bounded and also ends when another role has
 // failed; the failing role records the error flag, the MMA thread then waits
 // (bounded) for its MMAs and the copy thread for its copies before the CTA
 // frees its tensor memory.
@@ -364,15 +352,67 @@ constexpr int PEPI = 16;                // epilogue warps: four per TMEM lane qu
 constexpr int PTHREADS = 32 * (2 + PEPI);
 constexpr int PTN = 128;
 
-template <int COMB, bool FP64SUB>
-__global__ void __launch_bounds__(PTHREADS, 1)
-class_stats_persistent(const unsigned char* __restrict__ A1, const unsigned char* __restrict__ A2,
-                       const unsigned char* __restrict__ B, int chunks, int G, int num_perms,
-                       const float* __restrict__ gene_mu, const double* __restrict__ gene_t1,
-                       const double* __restrict__ gene_t2, float nA, float nB, float* __restrict__ keys,
-                       int* __restrict__ error_flag) {
-    constexpr int TB_CHUNK = PTN * BK * 2;
+// one tile's operands and outputs
+struct TileJob {
+    const unsigned char* A1;
+    const unsigned char* A2;
+    const unsigned char* B;
+    const float* mu;
+    const double* t1;
+    const double* t2;
+    float* keys;
+    float nA, nB;
+    int chunks, G, num_perms, gt, pt;
+};
+
+// the tiles of one problem: tile t = gene tile t / ptiles, permutation tile t % ptiles
+struct SoloTiles {
+    const unsigned char* A1;
+    const unsigned char* A2;
+    const unsigned char* B;
+    const float* mu;
+    const double* t1;
+    const double* t2;
+    float* keys;
+    int* error_flag;
+    float nA, nB;
+    int chunks, G, num_perms, total;
+    __device__ __forceinline__ TileJob job(int t) {
+        const int ptiles = (num_perms + PTN - 1) / PTN;
+        const int gt = t / ptiles;
+        return TileJob{A1, A2, B, mu, t1, t2, keys, nA, nB, chunks, G, num_perms, gt, t - gt * ptiles};
+    }
+    __device__ __forceinline__ int* flag() const { return error_flag; }
+};
+
+// the tiles of every instance of a batch, instance after instance; a role
+// walks them in increasing order, so its cursor only moves forward
+struct MultiTiles {
+    const ChosenTask* tasks;
+    int ntasks, total;
+    int i = 0, base = 0;  // cursor: instance i's tiles start at tile `base`
+    __device__ __forceinline__ TileJob job(int t) {
+        int ptiles, n;
+        for (;;) {
+            const ChosenTask& k = tasks[i];
+            ptiles = (k.num_perms + PTN - 1) / PTN;
+            n = ((k.G + BM - 1) / BM) * ptiles;
+            if (t < base + n || i + 1 >= ntasks) break;
+            base += n;
+            ++i;
+        }
+        const ChosenTask& k = tasks[i];
+        const int lt = t - base, gt = lt / ptiles;
+        return TileJob{k.A1, k.A2, k.Bm, k.mu, k.t1, k.t2, k.keys, k.nA, k.nB, k.chunks, k.G, k.num_perms, gt,
+                       lt - gt * ptiles};
+    }
+    __device__ __forceinline__ int* flag() const { return tasks[0].error_flag; }
+};
+
+template <int COMB, bool FP64SUB, class Tiles>
+__device__ __forceinline__ void persistent_body(Tiles src) {
     constexpr int TSTAGE = stage_bytes<PTN>();
+    constexpr int TB_CHUNK = PTN * BK * 2;
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ __align__(8) uint64_t full[PSTAGES];
     __shared__ __align__(8) uint64_t empty[PSTAGES];
@@ -382,8 +422,7 @@ class_stats_persistent(const unsigned char* __restrict__ A1, const unsigned char
     __shared__ uint32_t tmem_slot;
     __shared__ volatile int failed;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int ptiles = (num_perms + PTN - 1) / PTN;
-    const int ntiles = ((G + BM - 1) / BM) * ptiles;
+    const int ntiles = src.total;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(&tmem_slot))
@@ -410,10 +449,11 @@ class_stats_persistent(const unsigned char* __restrict__ A1, const unsigned char
 
     if (warp == 0) {
         if (lane == 0) {  // copies
+            Tiles tiles = src;
             uint32_t n = 0;  // chunk loads issued: stage n % PSTAGES, its (n / PSTAGES)-th use
             for (int t = blockIdx.x; t < ntiles && !failed; t += gridDim.x) {
-                const int gt = t / ptiles, pt = t - gt * ptiles;
-                for (int c = 0; c < chunks; c++, n++) {
+                const TileJob jb = tiles.job(t);
+                for (int c = 0; c < jb.chunks; c++, n++) {
                     const int s = (int)(n % PSTAGES);
                     const uint32_t k = n / PSTAGES;
                     if (k > 0 && !mbar_wait_or_fail(smem_u32(&empty[s]), (k - 1) & 1u, &failed)) {
@@ -423,13 +463,15 @@ class_stats_persistent(const unsigned char* __restrict__ A1, const unsigned char
                     unsigned char* st = smem + (size_t)s * TSTAGE;
                     const uint32_t bar = smem_u32(&full[s]);
                     mbar_expect_tx(bar, TSTAGE);
-                    bulk_copy(smem_u32(st), A1 + ((size_t)gt * chunks + c) * A_CHUNK, A_CHUNK, bar);
-                    bulk_copy(smem_u32(st + A_CHUNK), A2 + ((size_t)gt * chunks + c) * A_CHUNK, A_CHUNK, bar);
-                    bulk_copy(smem_u32(st + 2 * A_CHUNK), B + ((size_t)pt * chunks + c) * TB_CHUNK, TB_CHUNK, bar);
+                    bulk_copy(smem_u32(st), jb.A1 + ((size_t)jb.gt * jb.chunks + c) * A_CHUNK, A_CHUNK, bar);
+                    bulk_copy(smem_u32(st + A_CHUNK), jb.A2 + ((size_t)jb.gt * jb.chunks + c) * A_CHUNK, A_CHUNK,
+                              bar);
+                    bulk_copy(smem_u32(st + 2 * A_CHUNK), jb.B + ((size_t)jb.pt * jb.chunks + c) * TB_CHUNK,
+                              TB_CHUNK, bar);
                 }
             }
             if (failed) {
-                atomicExch(error_flag, 1);
+                atomicExch(src.flag(), 1);
                 // the last copies issued into each stage land before the CTA leaves
                 for (uint32_t m = n > PSTAGES ? n - PSTAGES : 0; m < n; m++)
                     mbar_wait(smem_u32(&full[m % PSTAGES]), (m / PSTAGES) & 1u);
@@ -437,10 +479,12 @@ class_stats_persistent(const unsigned char* __restrict__ A1, const unsigned char
         }
     } else if (warp == 1) {
         if (lane == 0) {  // MMAs
+            Tiles tiles = src;
             const uint32_t idesc = make_idesc(BM, PTN);
             uint32_t n = 0;  // chunks consumed
             int j = 0;       // tiles of this CTA
             for (int t = blockIdx.x; t < ntiles && !failed; t += gridDim.x, j++) {
+                const int chunks = tiles.job(t).chunks;
                 const int b = j & 1;
                 const uint32_t kb = (uint32_t)j >> 1;
                 if (kb > 0 && !mbar_wait_or_fail(smem_u32(&acc_empty[b]), (kb - 1) & 1u, &failed)) {
@@ -476,12 +520,13 @@ class_stats_persistent(const unsigned char* __restrict__ A1, const unsigned char
                 }
                 mma_commit(smem_u32(&acc_full[b]));
             }
-            if (failed) atomicExch(error_flag, 1);
+            if (failed) atomicExch(src.flag(), 1);
             // every MMA issued has retired before TMEM is freed
             mma_commit(smem_u32(&drain));
             mbar_wait(smem_u32(&drain), 0);
         }
     } else {  // epilogue
+        Tiles tiles = src;
         const int e = warp - 2;
         const int quarter = warp & 3;  // the TMEM lane quarter this warp may read
         const int part = e >> 2;
@@ -495,14 +540,15 @@ class_stats_persistent(const unsigned char* __restrict__ A1, const unsigned char
             if (!ok) {
                 if (lane == 0) {
                     failed = 1;
-                    atomicExch(error_flag, 1);
+                    atomicExch(src.flag(), 1);
                 }
                 break;
             }
             fence_after();
-            const int gt = t / ptiles, pt = t - gt * ptiles;
-            tile_epilogue<COMB, FP64SUB, PTN, PEPI / 4>(tmem + (uint32_t)(b * 2 * PTN), quarter, part, lane, gt,
-                                                        pt, G, num_perms, gene_mu, gene_t1, gene_t2, nA, nB, keys);
+            const TileJob jb = tiles.job(t);
+            tile_epilogue<COMB, FP64SUB, PTN, PEPI / 4>(tmem + (uint32_t)(b * 2 * PTN), quarter, part, lane, jb.gt,
+                                                        jb.pt, jb.G, jb.num_perms, jb.mu, jb.t1, jb.t2, jb.nA, jb.nB,
+                                                        jb.keys);
             fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(smem_u32(&acc_empty[b]));
@@ -514,6 +560,30 @@ class_stats_persistent(const unsigned char* __restrict__ A1, const unsigned char
         fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
     }
+}
+
+template <int COMB, bool FP64SUB>
+__global__ void __launch_bounds__(PTHREADS, 1)
+class_stats_persistent(const unsigned char* __restrict__ A1, const unsigned char* __restrict__ A2,
+                       const unsigned char* __restrict__ B, int chunks, int G, int num_perms,
+                       const float* __restrict__ gene_mu, const double* __restrict__ gene_t1,
+                       const double* __restrict__ gene_t2, float nA, float nB, float* __restrict__ keys,
+                       int* __restrict__ error_flag) {
+    const int total = ((G + BM - 1) / BM) * ((num_perms + PTN - 1) / PTN);
+    persistent_body<COMB, FP64SUB>(SoloTiles{A1, A2, B, gene_mu, gene_t1, gene_t2, keys, error_flag, nA, nB, chunks, G,
+                                             num_perms, total});
+}
+
+// every instance of a batch (one metric family): the tiles of all
+// instances, instance after instance, over one CTA per SM
+template <int COMB, bool FP64SUB>
+__global__ void __launch_bounds__(PTHREADS, 1)
+class_stats_persistent_multi(const ChosenTask* __restrict__ tasks, int ntasks, int total) {
+    MultiTiles src;
+    src.tasks = tasks;
+    src.ntasks = ntasks;
+    src.total = total;
+    persistent_body<COMB, FP64SUB>(src);
 }
 
 // ---------------------------------------------------------------------------
@@ -796,15 +866,21 @@ cudaError_t launch_chosen_metric_multi(const ChosenTask* d_tasks, const ChosenTa
     const unsigned z = (unsigned)n;
     zero_b_multi<TN><<<dim3(152, 1, z), 256, 0, st>>>(d_tasks);
     label_operand_multi<TN><<<dim3((unsigned)((pmax + 127) / 128), (unsigned)smax, z), 128, 0, st>>>(d_tasks);
-    const dim3 grid((unsigned)((gmax + BM - 1) / BM), (unsigned)((pmax + TN - 1) / TN), z);
-    const size_t smem = (size_t)stages<TN>() * stage_bytes<TN>();
+    // the persistent kernel over the tiles of every instance
+    int64_t total = 0;
+    for (int i = 0; i < n; i++)
+        total += (int64_t)((h_tasks[i].G + BM - 1) / BM) * ((h_tasks[i].num_perms + PTN - 1) / PTN);
+    if (total > INT32_MAX) return cudaErrorInvalidValue;
+    const int sms = sm_count();
+    const dim3 grid((unsigned)(total < sms ? total : sms));
+    const size_t smem = (size_t)PSTAGES * stage_bytes<PTN>();
     cudaError_t e = cudaSuccess;
 #define GSEA_CHOSEN_MULTI(C)                                                                                    \
     {                                                                                                           \
-        auto kern = fp64_variance ? class_stats_multi<C, true, TN> : class_stats_multi<C, false, TN>;          \
+        auto kern = fp64_variance ? class_stats_persistent_multi<C, true> : class_stats_persistent_multi<C, false>; \
         e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);                 \
         if (e != cudaSuccess) return e;                                                                         \
-        kern<<<grid, THREADS, smem, st>>>(d_tasks);                                                             \
+        kern<<<grid, PTHREADS, smem, st>>>(d_tasks, n, (int)total);                                             \
     }
     switch (h_tasks[0].comb) {
         case 0: GSEA_CHOSEN_MULTI(0) break;
