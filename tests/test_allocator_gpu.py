@@ -382,3 +382,63 @@ def test_significance_rule_saves_scores_with_the_full_tests_calls(gpu):
     assert reports["off"]["stopped_sig"] == 0 and reports["off"]["p_sig"] == 0.0
     assert reports["on"]["stopped_sig"] > 0 and reports["on"]["p_sig"] > 0.0
     assert scores["on"] < scores["off"], scores
+
+
+def test_learned_allocator_at_full_scale(gpu):
+    """The allocator workload itself: 20,000 genes x 200 samples, 20,000 sets
+    (5 % enriched, the rest null), up to 100,000 permutations per set, the
+    network trained on a 2,000-set calibration run.  Judged against the full
+    tensor-core test: the same FDR < 0.25 calls (flips only within the
+    estimator's band), ES / NES / NP bit-identical for every set that ran all
+    permutations, every score a sampled set received equal to the full test's
+    score of that permutation, and the learned prior computing fewer scores
+    than the same rules without it."""
+    from cudagsea_gb300.precision_check import _DeviceRows
+    d = synthetic.learned()
+    K, P = d.num_sets, d.num_perms
+    full = api.Plan(d.num_genes, d.num_samples, K, P, "twopass_signal2noise", form=N.FORM_CHOSEN)
+    full.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+    full.execute()
+    st_f = full.read(es=False)[1].reshape(5, -1)
+    rows_f = _DeviceRows(full, N.BUF_ES, np.float32, P)
+    cal = synthetic.learned(seed=6262, num_sets=2000, num_perms=4000)
+    cp = api.Plan(cal.num_genes, cal.num_samples, cal.num_sets, cal.num_perms, "twopass_signal2noise",
+                  form=N.FORM_CHOSEN)
+    cp.set_inputs(cal.exprs, cal.labels, cal.set_offsets, cal.set_genes)
+    cp.execute()
+    model, _ = allocator.train_model(cp, seed=5, queries=24, steps=3000)
+    cp.close()
+    calls_full = set(np.where(st_f[4] < Q_CALL)[0])
+    assert len(calls_full) > 100
+    sample = np.random.RandomState(3).choice(K, 300, replace=False)
+    reports = {}
+    for name, m in (("rules", None), ("learned", model)):
+        plan = api.Plan(d.num_genes, d.num_samples, K, P, "twopass_signal2noise", form=N.FORM_CHOSEN)
+        plan.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+        res = allocator.execute_adaptive(plan, m, pilot_perms=1000)
+        st_a = plan.read(es=False)[1].reshape(5, -1)
+        counts = res.counts
+        assert counts.min() >= 1000 and counts.max() <= P
+        calls = set(np.where(st_a[4] < Q_CALL)[0])
+        flips = sorted(calls ^ calls_full)
+        for k in flips:
+            assert abs(st_f[4][k] - Q_CALL) <= Q_BAND, (name, k, st_f[4][k], st_a[4][k])
+        assert len(flips) <= K // 100, (name, flips)
+        done = counts == P
+        assert done.any()
+        for r in (0, 1, 2):
+            assert np.array_equal(st_a[r, done].view(np.uint32), st_f[r, done].view(np.uint32)), (name, r)
+        got = _DeviceRows(plan, N.BUF_ES, np.float32, P).rows(sample)
+        ref = rows_f.rows(sample)
+        for i, k in enumerate(sample):
+            n = counts[k]
+            assert np.array_equal(got[i, :n].view(np.uint32), ref[i, :n].view(np.uint32)), (name, k)
+        short_calls = [k for k in sorted(calls) if counts[k] < P]
+        assert len(short_calls) <= res.report["stopped_sig"], (name, res.report)
+        assert res.report["scores"] < 0.1 * K * P, (name, res.report)
+        reports[name] = res.report
+        plan.close()
+    model.close()
+    full.close()
+    assert reports["learned"]["model_used"] == 1
+    assert reports["learned"]["scores"] < reports["rules"]["scores"], reports
