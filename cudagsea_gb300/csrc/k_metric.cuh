@@ -105,22 +105,30 @@ __device__ __forceinline__ void metric_exact(const T* __restrict__ X, int G, int
                     const T kk = E::sub(E::sub(beta, acc), alpha);
                     if (l) { cA[j] = kk; mA[j] = beta; } else { cB[j] = kk; mB[j] = beta; }
                 } else if (ACC == ACC_ONEPASS) {
-                    if (l) { mA[j] = E::add(mA[j], x); vA[j] = E::add(vA[j], xx); }
-                    else   { mB[j] = E::add(mB[j], x); vB[j] = E::add(vB[j], xx); }
+                    // one add into the selected accumulator (the same rounding
+                    // as the reference's conditional add, one FP64 / FP32 op)
+                    const T m = E::add(l ? mA[j] : mB[j], x);
+                    const T v = E::add(l ? vA[j] : vB[j], xx);
+                    mA[j] = l ? m : mA[j];
+                    mB[j] = l ? mB[j] : m;
+                    vA[j] = l ? v : vA[j];
+                    vB[j] = l ? vB[j] : v;
                 } else if (ACC == ACC_TWOPASS) {
-                    if (l) mA[j] = E::add(mA[j], x); else mB[j] = E::add(mB[j], x);
-                } else {  // ACC_KNUTH
-                    if (l) {
-                        iA[j]++;
-                        const T d = E::sub(x, mA[j]);
-                        mA[j] = E::add(mA[j], E::div(d, (T)iA[j]));
-                        vA[j] = E::add(vA[j], E::mul(d, E::sub(x, mA[j])));
-                    } else {
-                        iB[j]++;
-                        const T d = E::sub(x, mB[j]);
-                        mB[j] = E::add(mB[j], E::div(d, (T)iB[j]));
-                        vB[j] = E::add(vB[j], E::mul(d, E::sub(x, mB[j])));
-                    }
+                    const T m = E::add(l ? mA[j] : mB[j], x);
+                    mA[j] = l ? m : mA[j];
+                    mB[j] = l ? mB[j] : m;
+                } else {  // ACC_KNUTH: the update of the selected class
+                    const int it = (l ? iA[j] : iB[j]) + 1;
+                    const T mo = l ? mA[j] : mB[j];
+                    const T d = E::sub(x, mo);
+                    const T mn = E::add(mo, E::div(d, (T)it));
+                    const T vn = E::add(l ? vA[j] : vB[j], E::mul(d, E::sub(x, mn)));
+                    iA[j] = l ? it : iA[j];
+                    iB[j] = l ? iB[j] : it;
+                    mA[j] = l ? mn : mA[j];
+                    mB[j] = l ? mB[j] : mn;
+                    vA[j] = l ? vn : vA[j];
+                    vB[j] = l ? vB[j] : vn;
                 }
             }
         }
@@ -155,13 +163,14 @@ __device__ __forceinline__ void metric_exact(const T* __restrict__ X, int G, int
                     const bool l = (mw[j] >> t) & 1u;
                     const T d = E::sub(x, l ? mA[j] : mB[j]);
                     const T dd = E::mul(d, d);
-                    if (l) {
-                        if (ACC == ACC_OVERKILL) cA[j] = E::add(cA[j], d);
-                        vA[j] = E::add(vA[j], dd);
-                    } else {
-                        if (ACC == ACC_OVERKILL) cB[j] = E::add(cB[j], d);
-                        vB[j] = E::add(vB[j], dd);
+                    if (ACC == ACC_OVERKILL) {
+                        const T c = E::add(l ? cA[j] : cB[j], d);
+                        cA[j] = l ? c : cA[j];
+                        cB[j] = l ? cB[j] : c;
                     }
+                    const T v = E::add(l ? vA[j] : vB[j], dd);
+                    vA[j] = l ? v : vA[j];
+                    vB[j] = l ? vB[j] : v;
                 }
             }
         }
