@@ -227,14 +227,16 @@ class Batch:
     """Many independent GSEA instances run together in one CUDA graph
     (gsea_batch in the C ABI).  `instances`: GseaInput-like objects (exprs,
     labels, set_offsets, set_genes, num_perms); one metric / precision / form
-    for all, or a metric per instance."""
+    for all, or a metric (and a sort direction) per instance."""
 
     def __init__(self, instances, metric: Union[str, int, Sequence] = "twopass_signal2noise", precision: int = 32,
-                 form: int = N.FORM_PLAIN, streams: int = 0, seed: int = 42, device: int = -1):
+                 form: int = N.FORM_PLAIN, streams: int = 0, seed: int = 42, device: int = -1,
+                 ascending: Union[bool, Sequence[bool]] = False):
         L = N.lib()
         n = len(instances)
         cfgs = (N.Config * n)()
         metrics = list(metric) if isinstance(metric, (list, tuple)) else [metric] * n
+        asc = list(ascending) if isinstance(ascending, (list, tuple)) else [ascending] * n
         for i, d in enumerate(instances):
             c = cfgs[i]
             L.gsea_config_init(ctypes.byref(c))
@@ -243,6 +245,7 @@ class Batch:
             c.num_perms = d.num_perms
             c.metric = metric_id(metrics[i])
             c.precision, c.form, c.seed, c.device = precision, form, seed, device
+            c.ascending = 1 if asc[i] else 0
         h = ctypes.c_void_p()
         N.check(L.gsea_batch_create(n, cfgs, streams, ctypes.byref(h)))
         self._h = h

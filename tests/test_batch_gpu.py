@@ -122,6 +122,29 @@ def test_batch_rejects_mixed_precision(gpu):
     assert L.gsea_batch_create(2, cfgs, 0, ctypes.byref(h)) == 1
 
 
+@pytest.mark.parametrize("form", [N.FORM_PLAIN, N.FORM_CHOSEN])
+def test_batch_mixed_sort_directions(gpu, form):
+    """Instances sorting in ascending and descending order in one batch (the
+    reference's `-order ascending`): each equals its solo plan bit for bit."""
+    ds = instances()[:6]
+    asc = [i % 2 == 1 for i in range(len(ds))]
+    metric = "twopass_signal2noise"
+    ref = []
+    for d, a in zip(ds, asc):
+        p = api.Plan(d.num_genes, d.num_samples, d.num_sets, d.num_perms, metric, form=form, ascending=a)
+        p.set_inputs(d.exprs, d.labels, d.set_offsets, d.set_genes)
+        p.execute()
+        ref.append(p.read())
+        p.close()
+    b = api.Batch(ds, metric, precision=32, form=form, ascending=asc)
+    b.execute()
+    b.synchronize()
+    for i in range(len(ds)):
+        es, st = b.read(i)
+        assert same(es, ref[i][0]) and same(st, ref[i][1]), i
+    b.close()
+
+
 def test_batch_single_instance_and_single_permutation(gpu):
     d1 = synthetic.make(4000, 30, 25, 1, seed=3, n_class_b=15, set_min=15, set_max=100)
     d2 = synthetic.make(1500, 22, 7, 33, seed=4, n_class_b=11, set_min=15, set_max=100)

@@ -184,6 +184,18 @@ def test_tiled_sort_edge_keys(gpu, G, double):
         assert H.es_close(r["es"], es_o, double).all(), metric
 
 
+@pytest.mark.parametrize("G,double", [(41003, False), (8194, True)], ids=["f32", "f64"])
+def test_tiled_sort_ascending(gpu, G, double):
+    """The tiled sort in ascending order (the reference's `-order ascending`),
+    ties and 160 permutations: the oracle's stable ascending order."""
+    d = synthetic.make(G, 10, 4, 160, seed=G + 1, n_class_b=5, set_min=5, set_max=300)
+    d.exprs[:, : G // 4] = d.exprs[:, [G // 2]]
+    r = run_plan(d, "twopass_t_test", double=double, ascending=True, tuning=dict(sort_variant=2))
+    sk, order = check_sort(r["keys"], r["order"], r["ranks"], r["sorted"], ascending=True)
+    es_o = oracle.es(sk, order, d.set_offsets, d.set_genes)
+    assert H.es_close(r["es"], es_o, double).all()
+
+
 @pytest.mark.parametrize("double", [False, True], ids=["f32", "f64"])
 def test_tiled_sort_all_keys_equal(gpu, double):
     """Every gene identical: every radix digit is uniform, no pass moves a key,

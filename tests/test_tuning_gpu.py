@@ -57,6 +57,21 @@ def test_tensor_core_tiles_are_bit_identical(gpu, data):
         assert same(a, b)
 
 
+@pytest.mark.parametrize("G,S,P", [(130, 7, 1), (257, 33, 129), (1000, 200, 300), (5000, 11, 2000)])
+@pytest.mark.parametrize("form", [N.FORM_CHOSEN, N.FORM_CHOSEN_FP64])
+def test_persistent_tensor_core_kernel_on_ragged_shapes(gpu, G, S, P, form):
+    """The persistent warp-specialised class statistics (the 128-permutation
+    tile: tiles of 128 genes x 128 permutations walked by one CTA per SM,
+    copies, MMAs and epilogue on separate warps) against the one-tile kernel
+    of the 256-permutation tile: partial gene and permutation tiles, a single
+    permutation, more tiles than SMs, K chunks not filled by the samples."""
+    d = synthetic.make(G, S, 5, P, seed=G + S, n_class_b=max(1, S // 3), set_min=1, set_max=min(60, G))
+    ref = run(d, form=form, chosen_tile=256)
+    got = run(d, form=form, chosen_tile=128)
+    for a, b in zip(ref, got):
+        assert same(a, b)
+
+
 def test_invalid_tuning_is_rejected(gpu, data):
     plan = api.Plan(data.num_genes, data.num_samples, data.num_sets, 64, 8)
     with pytest.raises(N.GseaError):
