@@ -134,6 +134,64 @@ __device__ __forceinline__ void consider(T val, int pos, T& best, int& bpos) {
 // `Wt` (every lane) comes from the marking.  Each word is cleared as it is
 // read.  `w0` = lane*WPL: the lane's first word, 16-byte aligned inside the
 // warp's region of WPL*32 words (bits at positions >= G are never set).
+// order-preserving signed 64-bit key of a double (an involution): the
+// integer order of the keys is the numeric order of non-NaN doubles, -0
+// below +0
+__device__ __forceinline__ long long okey(double v) {
+    const long long b = __double_as_longlong(v);
+    return b ^ ((b >> 63) & 0x7fffffffffffffffll);
+}
+__device__ __forceinline__ double okey_value(long long k) {
+    return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffll));
+}
+
+// One lane's walk over its hits in rank order (the direct procedure below):
+// its largest value after a hit (mx at pmx) and smallest before one (mn at
+// pmn) with the lane-local prefix Wl.  IKEY (doubles whose candidates are all
+// finite): the running extrema are compared as integer keys, on the integer
+// pipe instead of the FP64 pipe that bounds the FP64 kernel -- the same
+// results, since the keys order finite doubles as they compare except -0 /
+// +0, and a zero never decides a score (only a positive maximum or a
+// negative minimum counts).
+template <class T, int WPL, bool IKEY, class Mask>
+__device__ __forceinline__ void walk_hits(uint32_t* bm, int w0, Mask nzm, int cnt, int excl, const T* wt, T inv,
+                                          T d, Acc<T>& Wl, T& mx, int& pmx, T& mn, int& pmn) {
+    uint32_t cur = 0u;
+    int wi = 0;
+    long long kmx = 0, kmn = 0;
+    if constexpr (IKEY) {
+        kmx = okey(mx);
+        kmn = okey(mn);
+    }
+    for (int t = 0; t < cnt; t++) {
+        if (cur == 0u) {  // next nonzero word of the lane
+            wi = (WPL > 32 ? __ffsll((long long)nzm) : __ffs((int)nzm)) - 1;
+            nzm &= nzm - 1;
+            cur = bm[w0 + wi];
+            bm[w0 + wi] = 0u;
+        }
+        const int bit = __ffs(cur) - 1;
+        cur &= cur - 1;
+        const int r = ((w0 + wi) << 5) + bit;
+        const T md = -(T)(r - (excl + t)) * d;  // misses before this hit, times the decay
+        const T before = t > 0 ? Wl.scaled_plus(inv, md) : md;
+        Wl.add(wt[r]);
+        const T after = Wl.scaled_plus(inv, md);
+        if constexpr (IKEY) {
+            const long long kb = okey(before), ka = okey(after);
+            if (kb < kmn) { kmn = kb; pmn = r - 1; }
+            if (ka > kmx) { kmx = ka; pmx = r; }
+        } else {
+            if (before < mn) { mn = before; pmn = r - 1; }
+            if (after > mx) { mx = after; pmx = r; }
+        }
+    }
+    if constexpr (IKEY) {
+        mx = okey_value(kmx);
+        mn = okey_value(kmn);
+    }
+}
+
 template <class T, int WPL>
 __device__ __forceinline__ T set_score_direct(uint32_t* bm, int w0, const T* wt, const T* __restrict__ decay, int G,
                                               int lane, const Acc<T>& Wt) {
@@ -160,24 +218,13 @@ __device__ __forceinline__ T set_score_direct(uint32_t* bm, int w0, const T* wt,
     Acc<T> Wl;  // weight of this lane's hits so far
     T mx = -CUDART_INF, mn = CUDART_INF;
     int pmx = -1, pmn = -1;
-    uint32_t cur = 0u;
-    int wi = 0;
-    for (int t = 0; t < cnt; t++) {
-        if (cur == 0u) {  // next nonzero word of the lane
-            wi = (WPL > 32 ? __ffsll((long long)nzm) : __ffs((int)nzm)) - 1;
-            nzm &= nzm - 1;
-            cur = bm[w0 + wi];
-            bm[w0 + wi] = 0u;
-        }
-        const int bit = __ffs(cur) - 1;
-        cur &= cur - 1;
-        const int r = ((w0 + wi) << 5) + bit;
-        const T md = -(T)(r - (excl + t)) * d;  // misses before this hit, times the decay
-        const T before = t > 0 ? Wl.scaled_plus(inv, md) : md;
-        Wl.add(wt[r]);
-        const T after = Wl.scaled_plus(inv, md);
-        if (before < mn) { mn = before; pmn = r - 1; }
-        if (after > mx) { mx = after; pmx = r; }
+    if constexpr (std::is_same<T, double>::value) {
+        if (isfinite(Wt.value()) && isfinite(inv))  // warp-uniform: every candidate is finite
+            walk_hits<T, WPL, true>(bm, w0, nzm, cnt, excl, wt, inv, d, Wl, mx, pmx, mn, pmn);
+        else
+            walk_hits<T, WPL, false>(bm, w0, nzm, cnt, excl, wt, inv, d, Wl, mx, pmx, mn, pmn);
+    } else {
+        walk_hits<T, WPL, false>(bm, w0, nzm, cnt, excl, wt, inv, d, Wl, mx, pmx, mn, pmn);
     }
     Acc<T> W_incl = Wl;
 #pragma unroll
