@@ -1,7 +1,7 @@
 """NES of the tensor-core forms against FP64, with every exceedance traced.
 
-The benchmark spec's accuracy condition for the tensor-core forms is |dNES| <=
-1e-4 against an FP64 evaluation, with identical FDR < 0.25 calls.  The FP64
+The accuracy condition of the tensor-core forms is |dNES| <= 1e-4 against an
+FP64 evaluation, with identical FDR < 0.25 calls.  The FP64
 evaluation here is the plain form in double precision (every stage in FP64,
 pinned bit for bit to the FP64 oracle by the parity tests), run on the same
 inputs and the same label permutations.
@@ -40,7 +40,7 @@ import numpy as np
 from . import api
 from . import _native as N
 
-NES_TOL = 1e-4      # the benchmark spec's |dNES| bound
+NES_TOL = 1e-4      # the |dNES| bound of the tensor-core forms
 ES_ROUND = 2e-5     # |dES| below this is rounding of the fp32 path (scores are O(0.1-1))
 FDR_CALL = 0.25
 
