@@ -138,7 +138,7 @@ int main(int argc, char** argv) {
         }
     }
     if (has(argc, argv, "-cpu")) {
-        std::cout << "ERROR: this build computes on the GPU only; -cpu is not available. Exiting." << std::endl;
+        std::cout << "ERROR: gsea103 computes on the GPU only; -cpu is not available. Exiting." << std::endl;
         return 22;
     }
     if (has(argc, argv, "-gpu")) {
