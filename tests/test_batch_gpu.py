@@ -42,10 +42,14 @@ def same(a, b):
     return np.array_equal(a.view(u), b.view(u))
 
 
-@pytest.mark.parametrize("precision,form", [(32, N.FORM_PLAIN), (64, N.FORM_PLAIN), (32, N.FORM_CHOSEN)])
+@pytest.mark.parametrize("precision,form", [(32, N.FORM_PLAIN), (64, N.FORM_PLAIN), (32, N.FORM_CHOSEN),
+                                            (32, N.FORM_CHOSEN_FP64)])
 def test_batch_matches_solo_plans(gpu, precision, form):
     ds = instances()
     metrics = METRICS if form == N.FORM_PLAIN else ["twopass_signal2noise"] * len(ds)
+    if form == N.FORM_CHOSEN_FP64:  # every metric family of the tensor-core form in one batch
+        metrics = ["twopass_signal2noise", "naive_diff_of_classes", "onepass_t_test", "naive_ratio_of_classes",
+                   "stable_signal2noise", "naive_log2_ratio_of_classes", "overkill_t_test", "stable_t_test"]
     ref = [solo(d, m, precision, form) for d, m in zip(ds, metrics)]
     b = api.Batch(ds, metrics, precision=precision, form=form, streams=4)
     for rep in range(2):  # the second execute replays the captured graph
@@ -61,6 +65,9 @@ def test_batch_matches_solo_plans(gpu, precision, form):
     if form == N.FORM_CHOSEN:
         # permute 1 + metric 3 + sort classes + ES classes + statistics 9
         assert info["launches"] <= 1 + 3 + 7 + info["es_classes"] + 9, info
+    elif form == N.FORM_CHOSEN_FP64:
+        # the metric: 3 launches per metric family (5 families)
+        assert info["launches"] <= 1 + 3 * 5 + 7 + info["es_classes"] + 9, info
     else:
         # permute 1 + one metric launch per metric + sort classes (+ the fp64
         # instance beyond the register sort) + ES classes + statistics 9
