@@ -276,8 +276,9 @@ int gsea_stats_device_noalloc(const void* es, int64_t num_sets, int64_t num_perm
  *      0 / -1 leave a choice automatic.                                    */
 typedef struct gsea_tuning {
     int32_t metric_pb;    /* plain fp32 metric: permutations per thread, 4 or 8 */
-    int32_t chosen_tile;  /* tensor-core form: permutations per tile, 128 (two CTAs per SM, the
-                             automatic choice) or 256 (one CTA per SM) */
+    int32_t chosen_tile;  /* tensor-core form: permutations per tile, 128 (the automatic choice: one
+                             persistent CTA per SM walking the tiles, the copies, MMAs and
+                             epilogue on separate warps) or 256 (one tile per CTA) */
     int32_t sort_variant; /* 1 register radix sort (fp32, G <= 40,960: one CTA up to 20,480, a two-CTA
                              cluster exchanging through distributed shared memory beyond; fp64,
                              G <= 20,480: one CTA up to 10,240, a two-CTA cluster beyond), 2 tiled */
