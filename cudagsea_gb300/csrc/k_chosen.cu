@@ -13,22 +13,26 @@
 // Operands: x' and x'^2 are split into three BF16 parts each (hi + mid + lo
 // carries ~24 significant bits) stacked along K, the labels are exact 0/1 in
 // BF16 and repeated for each part, so one BF16 x BF16 -> FP32 GEMM of depth
-// 3*S gives each sum.  A CTA owns 128 genes x 128 (two CTAs per SM, 4
-// stages, the default) or 256 permutations (one CTA per SM, 6 stages):
+// 3*S gives each sum.  A tile is 128 genes x TN permutations:
 //   * two FP32 accumulators in tensor memory (SA in the first TN columns,
 //     SA2 in the next TN), allocated with tcgen05.alloc;
 //   * the operands are pre-arranged in the canonical no-swizzle K-major
 //     layout (8x8 core matrices of 128 bytes), 32 K-elements per chunk, so a
 //     chunk of A (8 KB), A2 (8 KB) and B (8 or 16 KB) is one contiguous 1-D
-//     TMA bulk copy each (cp.async.bulk) completing on an mbarrier; three or
-//     five stages in flight while one is multiplied, a stage refilled as
-//     soon as the MMAs of its chunk retired;
+//     TMA bulk copy each (cp.async.bulk) completing on an mbarrier, a stage
+//     refilled as soon as the MMAs of its chunk retired;
 //   * one thread issues tcgen05.mma (M=128, N=TN, K=16) with shared-memory
 //     descriptors and tcgen05.commit to the stage's mbarrier (the sums are
-//     the same MMA chain per element for either tile);
-//   * eight warps read the accumulators with tcgen05.ld (a warp reads its
-//     lane quarter, 32 lanes x 16 columns at a time, over half of the
-//     columns), finalise the metric and store the keys.
+//     the same MMA chain per element for every form below);
+//   * warps read the accumulators with tcgen05.ld (a warp reads its lane
+//     quarter, 32 lanes x 16 columns at a time), finalise the metric and
+//     store the keys.
+// TN = 128, the default: class_stats_persistent, one CTA per SM walking the
+// tiles, a copy thread, an MMA thread and sixteen epilogue warps, two
+// accumulator pairs so that a tile's epilogue overlaps the next tile's MMAs
+// (its own section below); TN = 256: class_stats_kernel, one tile per CTA,
+// 6 stages, one thread for copies and MMAs, eight epilogue warps after the
+// last commit.
 // Every mbarrier wait is bounded (about one second of clock); on expiry the
 // kernel records an error flag, waits a bounded time for its own copies and
 // MMAs, frees its tensor memory and returns -- no wait can hang the GPU.
