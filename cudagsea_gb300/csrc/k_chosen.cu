@@ -805,6 +805,18 @@ int sm_count() {
     return n;
 }
 
+using ClassStatsFn = void (*)(const unsigned char*, const unsigned char*, const unsigned char*, int, int, int,
+                             const float*, const double*, const double*, float, float, float*, int*);
+// the kernel of a tile width: persistent for 128 permutations, one tile per CTA otherwise
+template <int C, int TN>
+ClassStatsFn pick_class_stats(bool fp64_variance) {
+    using namespace chosen;
+    if constexpr (TN == PTN)
+        return fp64_variance ? class_stats_persistent<C, true> : class_stats_persistent<C, false>;
+    else
+        return fp64_variance ? class_stats_kernel<C, true, TN> : class_stats_kernel<C, false, TN>;
+}
+
 template <int TN>
 cudaError_t launch_chosen_tn(int comb, bool fp64_variance, const uint32_t* masks, int words, int G, int S,
                              int num_perms, int64_t nA, int64_t nB, const float* mu, const double* t1,
@@ -828,8 +840,7 @@ cudaError_t launch_chosen_tn(int comb, bool fp64_variance, const uint32_t* masks
     }
 #define GSEA_CHOSEN(C)                                                                                         \
     {                                                                                                          \
-        auto kern = TN == PTN ? (fp64_variance ? class_stats_persistent<C, true> : class_stats_persistent<C, false>) \
-                              : (fp64_variance ? class_stats_kernel<C, true, TN> : class_stats_kernel<C, false, TN>); \
+        auto kern = pick_class_stats<C, TN>(fp64_variance);                                                   \
         e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);                \
         if (e != cudaSuccess) return e;                                                                        \
         kern<<<grid, threads, smem, st>>>(A1, A2, Bm, chunks, G, num_perms, mu, t1, t2, (float)nA, (float)nB,  \
