@@ -21,6 +21,11 @@ Fixtures (compressed .npz):
   ties_<prec>.npz      integer-valued expressions (many tied metrics),
                        G=300, S=16, K=10, P=32, naive_diff and twopass_s2n
   tiny.npz             37 genes x 5 samples, 3 sets, 3 permutations
+  large_<G>.npz        G = 30,000 / 50,000 genes x 24 samples, 20 sets, 64
+                       permutations, twopass_signal2noise: the reference's ES
+                       matrix and statistics in fp32 and fp64
+                       (`python tests/golden/make_golden.py large` writes
+                       these alone)
   cli_result_*.txt     "RESULT:" lines of the reference CLI (-cpu) on .gct /
                        .cls / .gmt files of the 2,000 x 40 workload (256
                        permutations, twopass_signal2noise; single, double and
@@ -65,10 +70,36 @@ def ties_case():
     return d
 
 
+def large_case(G):
+    """G genes x 24 samples, 20 sets, 64 permutations: the sizes of the two-CTA
+    cluster sort (30,000 genes, fp32) and of the tiled sort (50,000 genes;
+    fp64 at both sizes)."""
+    return synthetic.make(G, 24, 20, 64, seed=G + 7, n_class_b=12, sd_range=(0.5, 2.0), n_shift=200,
+                          shift_range=(0.5, 1.5), set_min=15, set_max=400, enriched_frac=0.3,
+                          name=f"large_{G}x24_K20_P64")
+
+
+def write_large():
+    """The cluster and tiled sort paths against the reference itself."""
+    for G in (30000, 50000):
+        d = large_case(G)
+        out = {"input_sha": input_hash(d)}
+        for double in (False, True):
+            prec = "f64" if double else "f32"
+            es, st = oracle.ref_gsea(8, d.exprs, d.labels, d.set_offsets, d.set_genes, d.num_perms, double=double)
+            out[f"es_{prec}"] = es
+            out[f"stats_{prec}"] = st
+        np.savez_compressed(os.path.join(HERE, f"large_{G}.npz"), **out)
+
+
 def main():
     oracle.build_ref()
     if not oracle.ref_available():
         raise SystemExit("reference build not available")
+    if sys.argv[1:] == ["large"]:
+        write_large()
+        print("large fixtures written to", HERE)
+        return
     # --- permutation KAT
     S, nA = 40, 20
     labels = np.array([0] * nA + [1] * (S - nA), np.uint8)
@@ -106,6 +137,7 @@ def main():
             out[f"es_{m}"] = es
             out[f"stats_{m}"] = st
         np.savez_compressed(os.path.join(HERE, f"ties_{prec}.npz"), **out)
+    write_large()
     # --- tiny shapes
     d = synthetic.tiny()
     out = {"input_sha": input_hash(d)}

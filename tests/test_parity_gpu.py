@@ -124,6 +124,29 @@ def test_config1_vs_reference(gpu, double):
     np.testing.assert_array_equal(oracle.stats(es).view(np.uint8), st.view(np.uint8))
 
 
+@pytest.mark.parametrize("G", [30000, 50000])
+@pytest.mark.parametrize("double", [False, True], ids=["f32", "f64"])
+def test_large_genes_against_reference(gpu, G, double):
+    """30,000 and 50,000 genes -- the two-CTA cluster sort (fp32, 30,000) and
+    the tiled sort (the rest), the ES kernel's large size classes -- against
+    the reference's own CPU build (fixtures written by make_golden.py from
+    it): ES matrix, ES and NES within the tolerance, NP and FWER within 2/P."""
+    g = H.load(f"large_{G}.npz")
+    d = MG.large_case(G)
+    assert MG.input_hash(d) == str(g["input_sha"])
+    prec = "f64" if double else "f32"
+    es, st = api.gsea(d.exprs, d.labels, d.set_offsets, d.set_genes, d.num_perms, "twopass_signal2noise",
+                      precision=64 if double else 32)
+    K = d.num_sets
+    ref_es, ref = g[f"es_{prec}"], g[f"stats_{prec}"]
+    # the reference's CPU sort is unstable: a member tied with a non-member may
+    # take the other order in a rare permutation
+    assert H.es_close(es, ref_es, double).mean() > 0.999
+    assert H.es_close(st[:K], ref[:K], double).all()            # ES
+    assert H.es_close(st[K:2 * K], ref[K:2 * K], double).all()  # NES
+    np.testing.assert_allclose(st[2 * K:4 * K], ref[2 * K:4 * K], atol=2.0 / d.num_perms)  # NP, FWER
+
+
 @pytest.mark.parametrize("double", [False, True], ids=["f32", "f64"])
 def test_tie_heavy_data(gpu, double):
     g = H.load(f"ties_{'f64' if double else 'f32'}.npz")
