@@ -21,6 +21,11 @@ Fixtures (compressed .npz):
   ties_<prec>.npz      integer-valued expressions (many tied metrics),
                        G=300, S=16, K=10, P=32, naive_diff and twopass_s2n
   tiny.npz             37 genes x 5 samples, 3 sets, 3 permutations
+  full_<prec>.npz      the 20,000 x 200 workload (1,000 sets, 1,000
+                       permutations), all 14 metrics: the reference's final
+                       statistics and the ES of its first 4 permutations
+                       (`python tests/golden/make_golden.py full` writes these
+                       alone: ~30 s of the reference per metric and precision)
   large_<G>.npz        G = 30,000 / 50,000 genes x 24 samples, 20 sets, 64
                        permutations, twopass_signal2noise: the reference's ES
                        matrix and statistics in fp32 and fp64
@@ -92,6 +97,19 @@ def write_large():
         np.savez_compressed(os.path.join(HERE, f"large_{G}.npz"), **out)
 
 
+def write_full():
+    """The headline workload, every metric, both precisions."""
+    d = synthetic.full()
+    for double in (False, True):
+        prec = "f64" if double else "f32"
+        out = {"input_sha": input_hash(d)}
+        for m in range(14):
+            es, st = oracle.ref_gsea(m, d.exprs, d.labels, d.set_offsets, d.set_genes, d.num_perms, double=double)
+            out[f"stats_{m}"] = st
+            out[f"es_head_{m}"] = np.ascontiguousarray(es[:, :4])
+        np.savez_compressed(os.path.join(HERE, f"full_{prec}.npz"), **out)
+
+
 def main():
     oracle.build_ref()
     if not oracle.ref_available():
@@ -99,6 +117,10 @@ def main():
     if sys.argv[1:] == ["large"]:
         write_large()
         print("large fixtures written to", HERE)
+        return
+    if sys.argv[1:] == ["full"]:
+        write_full()
+        print("full-size fixtures written to", HERE)
         return
     # --- permutation KAT
     S, nA = 40, 20
@@ -138,6 +160,7 @@ def main():
             out[f"stats_{m}"] = st
         np.savez_compressed(os.path.join(HERE, f"ties_{prec}.npz"), **out)
     write_large()
+    write_full()
     # --- tiny shapes
     d = synthetic.tiny()
     out = {"input_sha": input_hash(d)}

@@ -325,10 +325,11 @@ def test_full_size_properties(gpu, metric, double):
     fp64: size-independent checks (finite |ES| <= 1, statistics bit-identical
     to the oracle's for the GPU's ES) and spot permutations against the
     oracle (keys bit-exact -- log2 metrics <= 2 ulp --, order equal to the
-    oracle's stable order of the GPU's keys, ES within tolerance).  The
-    packed metric unroll at 200 samples, the register sort at 20,000 genes
-    (fp32) / the tiled sort (fp64) and the 32-warp enrichment staging all run
-    at this size."""
+    oracle's stable order of the GPU's keys, ES within tolerance); and the
+    statistics against the reference's own CPU build on the same inputs
+    (`full_<prec>.npz`).  The packed metric unroll at 200 samples, the
+    register sort (fp32) / the two-CTA cluster sort (fp64) at 20,000 genes
+    and the 32-warp enrichment staging all run at this size."""
     from cudagsea_gb300.precision_check import _DeviceRows
     d = synthetic.full()
     dt = np.float64 if double else np.float32
@@ -356,6 +357,23 @@ def test_full_size_properties(gpu, metric, double):
         assert H.es_close(es[:, p], e1[:, 0], double).all(), p
     np.testing.assert_array_equal(oracle.stats(es).view(np.uint8), st.view(np.uint8))
     plan.close()
+    # the reference's own statistics: its CPU sort is unstable, so a set
+    # member tied with a non-member (and the log2 metrics' keys, <= 2 ulp
+    # apart) can move a set's ES by a step of the running sum; ties are
+    # common for the fp32 ratio metrics (quotients near 1 take few distinct
+    # float values: ~60 tied pairs among 20,000 keys)
+    g = H.load(f"full_{'f64' if double else 'f32'}.npz")
+    assert str(g["input_sha"]) == MG.input_hash(d)
+    ref = g[f"stats_{metric}"]
+    K = d.num_sets
+    for lo in (0, K):  # ES, NES: at least 97% of the sets within the tolerance,
+        # the rest within a few steps of the running sum (~5e-5 of ES each;
+        # NES: times the set's normalising factor)
+        assert H.es_close(st[lo:lo + K], ref[lo:lo + K], double).mean() >= 0.97
+        bound = 5e-3 * (np.maximum(1.0, np.abs(ref[lo:lo + K])) if lo else 1.0)
+        assert (np.abs(st[lo:lo + K] - ref[lo:lo + K]) <= bound).all()
+    np.testing.assert_allclose(st[2 * K:4 * K], ref[2 * K:4 * K], atol=2.0 / d.num_perms)  # NP, FWER
+    assert H.es_close(es[:, :4], g[f"es_head_{metric}"], double).mean() >= 0.97
     if metric == 8 and not double:
         # a sharded plan reproduces the columns
         tail = api.Plan(d.num_genes, d.num_samples, d.num_sets, 100, metric, perm_offset=900)
